@@ -1,0 +1,98 @@
+"""ctypes binding of libnbpm.so (declarations mirror include/nbpm.h).
+
+The product path has no fallback: if the library cannot be loaded, or no CUDA device is
+usable, calls fail with NbpmError instead of computing anything on the CPU.
+"""
+import ctypes
+import os
+
+from . import build as _build
+
+c_int, c_double, c_char_p, c_void_p, c_ll = ctypes.c_int, ctypes.c_double, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_longlong
+
+ERRORS = {0: "NBPM_OK", 1: "NBPM_ERR_SETTINGS", 2: "NBPM_ERR_SIZE", 3: "NBPM_ERR_EXPR", 4: "NBPM_ERR_CUDA",
+          5: "NBPM_ERR_MEMORY", 6: "NBPM_ERR_ARG", 7: "NBPM_ERR_INTERNAL"}
+FP64, FP32 = 0, 1
+
+
+class NbpmError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (ERRORS.get(code, code), msg))
+        self.code = code
+        self.msg = msg
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("precision", c_int), ("groups_per_pass", c_int), ("use_graph", c_int),
+                ("device", c_int), ("verbose", c_int)]
+
+
+class Timing(ctypes.Structure):
+    _fields_ = [("upload_ms", c_double), ("compute_ms", c_double), ("download_ms", c_double),
+                ("total_ms", c_double), ("voxel_steps", c_ll), ("kernel_launches", c_int)]
+
+
+class Sample(ctypes.Structure):
+    _fields_ = [("json_str", c_char_p), ("mask_formula", c_char_p), ("lc_field_vals", c_void_p),
+                ("n_lc_vals", c_int), ("mask_vals", c_void_p), ("n_mask_vals", c_int),
+                ("E_field_vals", c_void_p), ("n_E_vals", c_int)]
+
+
+EXPORTS = {
+    "nbpm_default_options": (None, [ctypes.POINTER(Options)]),
+    "nbpm_run_backend_without_mask": (c_int, [c_char_p, c_void_p, c_int, c_void_p, c_int]),
+    "nbpm_run_backend_with_mask": (c_int, [c_char_p, c_char_p, c_void_p, c_int, c_void_p, c_int, c_void_p, c_int]),
+    "nbpm_run_backend_ex": (c_int, [c_char_p, c_char_p, c_void_p, c_int, c_void_p, c_int, c_void_p, c_int,
+                                    ctypes.POINTER(Options), ctypes.POINTER(Timing)]),
+    "nbpm_run_batch": (c_int, [c_int, ctypes.POINTER(Sample), ctypes.POINTER(Options), ctypes.POINTER(Timing)]),
+    "nbpm_plan_create": (c_int, [c_int, ctypes.POINTER(Sample), ctypes.POINTER(Options), ctypes.POINTER(c_void_p)]),
+    "nbpm_plan_upload": (c_int, [c_void_p]),
+    "nbpm_plan_execute": (c_int, [c_void_p, ctypes.POINTER(Timing)]),
+    "nbpm_plan_download": (c_int, [c_void_p]),
+    "nbpm_plan_slab_ms": (c_int, [c_void_p, ctypes.POINTER(c_double)]),
+    "nbpm_plan_destroy": (c_int, [c_void_p]),
+    "nbpm_plan_device_bytes": (c_ll, [c_void_p]),
+    "nbpm_eval_index": (c_int, [c_char_p, c_double, ctypes.POINTER(c_double)]),
+    "nbpm_mask_weights": (c_int, [c_char_p, c_char_p, c_void_p, c_int, c_void_p, c_void_p]),
+    "nbpm_last_error": (c_char_p, []),
+    "nbpm_version": (c_char_p, []),
+}
+
+_lib = None
+
+
+def lib_path():
+    return _build.LIB
+
+
+def load(build_if_missing=True):
+    """Load libnbpm.so (building it first if needed); raise if it cannot be loaded."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if build_if_missing and _build._stale():
+        _build.build()
+    if not os.path.exists(path):
+        raise NbpmError(4, "libnbpm.so is not built (%s)" % path)
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in EXPORTS.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(rc):
+    if rc != 0:
+        msg = load().nbpm_last_error().decode("utf-8", "replace")
+        raise NbpmError(rc, msg)
+    return rc
+
+
+def options(precision=FP64, groups_per_pass=0, use_graph=1, device=0, verbose=0):
+    o = Options()
+    load().nbpm_default_options(ctypes.byref(o))
+    o.precision, o.groups_per_pass, o.use_graph, o.device, o.verbose = precision, groups_per_pass, use_graph, device, verbose
+    return o

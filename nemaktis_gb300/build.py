@@ -1,0 +1,51 @@
+"""Compile libnbpm.so (the sm_103a CUDA backend) in-tree with nvcc.
+
+Output: nemaktis_gb300/_build/libnbpm.so (git-ignored). One translation unit, one
+-gencode (compute_103a / sm_103a), so a rebuild on a fresh machine takes well under a minute.
+"""
+import os
+import shutil
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "libnbpm.so")
+SOURCES = ["nbpm.cu"]
+HEADERS = ["bpm_kernels.cuh", "fft_kernels.cuh", "cplx.cuh", "host_settings.h", "host_expr.h", "host_json.h"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc():
+    exe = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(exe):
+        raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libnbpm.so")
+    return exe
+
+
+def _stale():
+    if not os.path.exists(LIB):
+        return True
+    t = os.path.getmtime(LIB)
+    deps = [os.path.join(CSRC, f) for f in SOURCES + HEADERS]
+    deps.append(os.path.join(HERE, "..", "include", "nbpm.h"))
+    return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
+
+
+def build(force=False, verbose=False, extra=()):
+    """Build libnbpm.so if it is missing or older than its sources; returns its path."""
+    if not force and not _stale():
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    tmp = LIB + ".tmp%d" % os.getpid()
+    cmd = [nvcc(), "-O3", "-std=c++17", *ARCH, "-lineinfo", "-Xcompiler", "-fPIC,-fopenmp",
+           "-shared", "-o", tmp, *[os.path.join(CSRC, f) for f in SOURCES], "-lgomp", *extra]
+    if verbose:
+        print(" ".join(cmd))
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force=True, verbose=True))

@@ -1,0 +1,704 @@
+// sm_103a kernels of the bpm z-stepping loop.
+//
+// Data layout in HBM (one sample):
+//   director  dir[iz][iy][ix][c]            FP64, c < 3 (director) or 6 (Q-tensor)
+//   fields    F[slot][comp][iy][ix]          cx<R>; slot = pol + 2*(q + Nq*lambda): the same
+//                                            order as the (Nl,Nq,4,Ny,Nx) user buffer
+//   eps ring  Q[2][group][NQ][iy][ix]        FP64 per-voxel derived permittivity, planes iz
+//                                            and iz+1 of every wavelength group
+//   coef      C[group][NCOEF][iy][ix]        cx<R>: 3 phase-operator entries and the 40
+//                                            entries of mu*R (DX, DY, DXDY stencils x 4 blocks)
+//   factors   X/Y[group][comp][NFAC][p]      cx<R>: pre-factored periodic line solves
+// A "group" is one wavelength: every (q, pol) slot of the group shares eps, R, the phase
+// operator and the line-solve factorisations.
+#pragma once
+
+#include <cstdint>
+
+#include "cplx.cuh"
+
+namespace nbpm {
+
+// Per-voxel derived permittivity components (PermittivityTensorField.cpp:3-99).
+enum { Q_XXTR = 0, Q_YYTR, Q_XYTR, Q_XXS, Q_YYS, Q_XYS, Q_VX, Q_VY, Q_IZZ, NQ };
+// Coefficient planes: phase operator (xx, yy, xy), then mu*R stencils.
+enum { C_PH = 0, C_DX = 3, C_DY = 15, C_DXDY = 27, NCOEF = 43 };
+// FP64 copies of the diagonal-block stencils used by the line factorisations:
+// index dir*6 + comp*3 + k (dir 0 = DX, 1 = DY; comp 0 = block 00, 1 = block 11).
+enum { NDIAG = 12 };
+// Line-solve factor planes.
+enum { F_INF = 0, F_RB, F_GAM, F_COR, F_W, NFAC };
+
+struct GroupParams {
+	double wavelength, k0, dX, dY, dZ;
+	double no, ne, ne_imag, nhost, nin, nout_fresnel;
+	double absorp_im;  // imaginary part of 1 + i*ne_imag/(ne-no)
+	double nref;
+};
+
+struct ShiftParams {
+	int active;       // 0: identity (q = 0)
+	int msx, msy;     // integer parts of the shifts
+	double wx[4], wy[4];
+	double ph_re, ph_im;
+};
+
+struct Geom {
+	int Nx, Ny, N;
+	int Nz;
+	int spg;          // slots per group = 2*Nq
+	int Nq;
+};
+
+// ---------------------------------------------------------------------------------------
+// Permittivity per voxel from the director or Q-tensor (PermittivityTensorField.cpp:19-99).
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ void eps_voxel(const double* __restrict__ dir, int fd, bool m,
+		const GroupParams& gp, double e[6]) {
+	double eps_perp = gp.no * gp.no;
+	double eps_a = gp.ne * gp.ne - eps_perp;
+	double eps_host = gp.nhost * gp.nhost;
+	if(!m) {
+		e[0] = e[1] = e[2] = eps_host;
+		e[3] = e[4] = e[5] = 0;
+		return;
+	}
+	if(fd == 3) {
+		double n0 = dir[0], n1 = dir[1], n2 = dir[2];
+		e[0] = eps_perp + eps_a * (n0 * n0);
+		e[1] = eps_perp + eps_a * (n1 * n1);
+		e[2] = eps_perp + eps_a * (n2 * n2);
+		e[3] = eps_a * n0 * n1;
+		e[4] = eps_a * n0 * n2;
+		e[5] = eps_a * n1 * n2;
+	}
+	else {
+		double ea = 2 * eps_a / 3, ei = eps_perp + eps_a / 3.;
+		e[0] = ei + ea * dir[0];
+		e[1] = ei + ea * dir[1];
+		e[2] = ei + ea * dir[2];
+		e[3] = ea * dir[3];
+		e[4] = ea * dir[4];
+		e[5] = ea * dir[5];
+	}
+}
+
+__device__ __forceinline__ double neff_of(double xxtr, double yytr, double xytr) {
+	double det = xxtr * yytr - xytr * xytr;
+	double tr = 0.5 * (xxtr + yytr);
+	if(tr * tr - det < 1e-8) return sqrt(tr);
+	double r = sqrt(tr * tr - det);
+	return (sqrt(tr + r) + sqrt(tr - r)) / 2.;
+}
+
+// One transverse plane of derived quantities for every group of the pass.
+__global__ void k_eps_plane(const double* __restrict__ dir, int fd, const uint8_t* __restrict__ mask,
+		int N, int iz, const GroupParams* __restrict__ gps, double* __restrict__ out) {
+	int p = blockIdx.x * blockDim.x + threadIdx.x;
+	int g = blockIdx.y;
+	if(p >= N) return;
+	size_t v = (size_t)iz * N + p;
+	GroupParams gp = gps[g];
+	double e[6];
+	eps_voxel(dir + v * fd, fd, mask ? mask[v] != 0 : true, gp, e);
+	double xxtr = e[0] - (e[4] * e[4]) / e[2];
+	double yytr = e[1] - (e[5] * e[5]) / e[2];
+	double xytr = e[3] - e[4] * e[5] / e[2];
+	double neff = neff_of(xxtr, yytr, xytr);
+	double* o = out + (size_t)g * NQ * N + p;
+	o[Q_XXTR * N] = xxtr;
+	o[Q_YYTR * N] = yytr;
+	o[Q_XYTR * N] = xytr;
+	o[Q_XXS * N] = neff + (xxtr - yytr) / (4 * neff);
+	o[Q_YYS * N] = neff + (yytr - xxtr) / (4 * neff);
+	o[Q_XYS * N] = xytr / (2 * neff);
+	o[Q_VX * N] = e[4] / e[2];
+	o[Q_VY * N] = e[5] / e[2];
+	o[Q_IZZ * N] = 1. / e[2];
+}
+
+// Partial sums of neff over the volume for nref (PermittivityTensorField.cpp:183-211),
+// in a fixed block order so the reduction is deterministic.
+__global__ void k_neff_partial(const double* __restrict__ dir, int fd, const uint8_t* __restrict__ mask,
+		size_t nvox, const GroupParams* __restrict__ gps, double* __restrict__ partial) {
+	__shared__ double sh[256];
+	int g = blockIdx.y;
+	GroupParams gp = gps[g];
+	double acc = 0;
+	for(size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvox; v += (size_t)gridDim.x * blockDim.x) {
+		double e[6];
+		eps_voxel(dir + v * fd, fd, mask ? mask[v] != 0 : true, gp, e);
+		double xxtr = e[0] - (e[4] * e[4]) / e[2];
+		double yytr = e[1] - (e[5] * e[5]) / e[2];
+		double xytr = e[3] - e[4] * e[5] / e[2];
+		acc += neff_of(xxtr, yytr, xytr);
+	}
+	sh[threadIdx.x] = acc;
+	__syncthreads();
+	for(int s = blockDim.x / 2; s > 0; s >>= 1) {
+		if(threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+		__syncthreads();
+	}
+	if(threadIdx.x == 0) partial[(size_t)g * gridDim.x + blockIdx.x] = sh[0];
+}
+
+// ---------------------------------------------------------------------------------------
+// Per-slab operator coefficients, FP64 arithmetic:
+//  * phase operator exp(i*a*d) (PhaseEvolutionOperator.cpp:34-63)
+//  * mu*R with R = i*W + (D*S^-1 + S^-1*D)/4, D = D0 + D1*K (ParaxialPrimaryEvolution-
+//    Operator.cpp:212-490), written per stencil entry: S^-1 and K at the column point for
+//    D*S^-1 and D1*K, S^-1 at the row point for S^-1*D, the walk-off split between row
+//    and column points. D1 uses the reference's neighbour indices (ix==Nx-1 -> 1,
+//    ix==0 -> Nx-2) while the stencil columns wrap with period Nx-1.
+// ---------------------------------------------------------------------------------------
+struct CoefCtx {
+	const double* A;
+	const double* B;
+	int N, Nx;
+	double hmu, rxx, ryy, rxy, va0, va1;
+	__device__ __forceinline__ double avg(int q, int x, int y) const {
+		int i = x + Nx * y;
+		return (A[q * N + i] + B[q * N + i]) / 2;
+	}
+	__device__ __forceinline__ double vsum(int a, int x, int y) const {
+		int i = x + Nx * y, q = a == 0 ? Q_VX : Q_VY;
+		return A[q * N + i] + B[q * N + i];
+	}
+	__device__ __forceinline__ void sinv(int x, int y, double& ixx, double& iyy, double& ixy) const {
+		double exx = avg(Q_XXS, x, y), eyy = avg(Q_YYS, x, y), exy = avg(Q_XYS, x, y);
+		double det = exx * eyy - exy * exy;
+		ixx = eyy / det; iyy = exx / det; ixy = -exy / det;
+	}
+	// One stencil entry of mu*R for the 4 blocks (00, 01, 10, 11). D is the real 2x2 entry
+	// of D at this (row, column) pair; dd is the first-derivative weight of the walk-off
+	// (0 for none) acting on component bT.
+	__device__ void entry(double D00, double D01, double D10, double D11, int cxp, int cyp,
+			double dd, int bT, cx<double> out[4]) const {
+		double re[4] = {0, 0, 0, 0}, im[4] = {0, 0, 0, 0};
+		if(dd != 0) {
+			double vb0 = vsum(0, cxp, cyp), vb1 = vsum(1, cxp, cyp);
+			im[0 + bT] += dd * (0.25 * va0);
+			im[2 + bT] += dd * (0.25 * va1);
+			im[2 * bT + 0] += dd * (0.25 * vb0);
+			im[2 * bT + 1] += dd * (0.25 * vb1);
+		}
+		double cxx, cyy, cxy;
+		sinv(cxp, cyp, cxx, cyy, cxy);
+		double Dm[2][2] = {{D00, D01}, {D10, D11}};
+		for(int a = 0; a < 2; a++) {
+			re[2 * a] += 0.25 * Dm[a][0] * cxx;
+			re[2 * a] += 0.25 * Dm[a][1] * cxy;
+			re[2 * a + 1] += 0.25 * Dm[a][0] * cxy;
+			re[2 * a + 1] += 0.25 * Dm[a][1] * cyy;
+		}
+		for(int b = 0; b < 2; b++) {
+			re[b] += 0.25 * rxx * Dm[0][b];
+			re[b] += 0.25 * rxy * Dm[1][b];
+			re[2 + b] += 0.25 * rxy * Dm[0][b];
+			re[2 + b] += 0.25 * ryy * Dm[1][b];
+		}
+		for(int b = 0; b < 4; b++) out[b] = mk(-hmu * im[b], hmu * re[b]);  // i*hmu*(re+i*im)
+	}
+};
+
+template <typename S>
+__global__ void k_coef(const double* __restrict__ QA, const double* __restrict__ QB,
+		const double* __restrict__ wts, int iz, Geom G, const GroupParams* __restrict__ gps,
+		cx<S>* __restrict__ coef, cx<double>* __restrict__ diag) {
+	int p = blockIdx.x * blockDim.x + threadIdx.x;
+	int g = blockIdx.y;
+	int N = G.N, Nx = G.Nx, Ny = G.Ny;
+	if(p >= N) return;
+	int ix = p % Nx, iy = p / Nx;
+	const GroupParams gp = gps[g];
+	const double* A = QA + (size_t)g * NQ * N;
+	const double* B = QB + (size_t)g * NQ * N;
+	cx<S>* C = coef + (size_t)g * NCOEF * N + p;
+	cx<double>* Dg = diag + (size_t)g * NDIAG * N + p;
+
+	// Phase operator.
+	{
+		double w0 = 0.5, w1 = 0.5;
+		if(wts) { size_t vi = (size_t)iz * N + p; w0 = wts[2 * vi]; w1 = wts[2 * vi + 1]; }
+		double hz = 0.5 * gp.dZ;
+		double dxx = hz * (w0 * A[Q_XXS * N + p] + w1 * B[Q_XXS * N + p] - gp.no);
+		double dyy = hz * (w0 * A[Q_YYS * N + p] + w1 * B[Q_YYS * N + p] - gp.no);
+		double dxy = hz * (w0 * A[Q_XYS * N + p] + w1 * B[Q_XYS * N + p]);
+		double diff = (dxx - dyy) / 2., tr = (dxx + dyy) / 2.;
+		double det = sqrt(dxy * dxy + diff * diff);
+		cx<double> a = mk(1.0, gp.absorp_im);
+		cx<double> sinc = mk(1.0, 0.0);
+		if(!(fabs(det) < 1e-8)) { cx<double> sn = csin_d(det * a); sinc = mk(sn.x / det, sn.y / det); }
+		cx<double> e = cexp_d(mk(-a.y * tr, a.x * tr));  // exp(i*a*tr)
+		cx<double> c = ccos_d(det * a);
+		cx<double> ids = mk(0.0, diff) * sinc;
+		C[(size_t)(C_PH + 0) * N] = cvt<S>(e * (c + ids));
+		C[(size_t)(C_PH + 1) * N] = cvt<S>(e * (c - ids));
+		C[(size_t)(C_PH + 2) * N] = cvt<S>(((e * mk(0.0, 1.0)) * dxy) * sinc);
+	}
+
+	CoefCtx X;
+	X.A = A; X.B = B; X.N = N; X.Nx = Nx;
+	X.hmu = gp.dZ / 2.;
+	X.sinv(ix, iy, X.rxx, X.ryy, X.rxy);
+	X.va0 = X.vsum(0, ix, iy);
+	X.va1 = X.vsum(1, ix, iy);
+	const double dX = gp.dX, dY = gp.dY;
+	auto ezz = [&](int x, int y) { int i = x + Nx * y; return (A[Q_IZZ * N + i] + B[Q_IZZ * N + i]) / 2; };
+	double e0 = ezz(ix, iy);
+	int pxq = (ix == Nx - 1) ? 1 : ix + 1, mxq = (ix == 0) ? Nx - 2 : ix - 1;
+	int pyq = (iy == Ny - 1) ? 1 : iy + 1, myq = (iy == 0) ? Ny - 2 : iy - 1;
+	int pxs = (ix == Nx - 2) ? 0 : ix + 1, mxs = (ix == 0) ? Nx - 2 : ix - 1;
+	int pys = (iy == Ny - 2) ? 0 : iy + 1, mys = (iy == 0) ? Ny - 2 : iy - 1;
+	cx<double> r[4];
+	const cx<double> z = mk(0.0, 0.0);
+
+	// DX: rows ix < Nx-1 when Nx > 3; k = 0 mx, 1 centre, 2 px.
+	{
+		bool ok = Nx > 3 && ix < Nx - 1;
+		double cm = 0, cp = 0, c0 = 0;
+		if(ok) {
+			cm = 0.5 * (ezz(mxq, iy) + e0) / (dX * dX);
+			cp = 0.5 * (ezz(pxq, iy) + e0) / (dX * dX);
+			c0 = -cm - cp;
+		}
+		const int cols[3] = {mxs, ix, pxs};
+		const double c1[3] = {cm, c0, cp};
+		const double L[3] = {1. / (dX * dX), -2. / (dX * dX), 1. / (dX * dX)};
+		const double dd[3] = {-0.5 / dX, 0, 0.5 / dX};
+		for(int k = 0; k < 3; k++) {
+			if(ok) {
+				int cxp = cols[k];
+				double kxx = X.avg(Q_XXTR, cxp, iy), kxy = X.avg(Q_XYTR, cxp, iy);
+				X.entry(c1[k] * kxx, c1[k] * kxy, 0.0, L[k], cxp, iy, dd[k], 0, r);
+			}
+			else r[0] = r[1] = r[2] = r[3] = z;
+			for(int b = 0; b < 4; b++) C[(size_t)(C_DX + 3 * b + k) * N] = cvt<S>(r[b]);
+			Dg[(size_t)(0 * 6 + 0 * 3 + k) * N] = r[0];
+			Dg[(size_t)(0 * 6 + 1 * 3 + k) * N] = r[3];
+		}
+	}
+	// DY: rows iy < Ny-1 when Ny > 3; k = 0 my, 1 centre, 2 py.
+	{
+		bool ok = Ny > 3 && iy < Ny - 1;
+		double cm = 0, cp = 0, c0 = 0;
+		if(ok) {
+			cp = 0.5 * (ezz(ix, pyq) + e0) / (dY * dY);
+			cm = 0.5 * (ezz(ix, myq) + e0) / (dY * dY);
+			c0 = -cm - cp;
+		}
+		const int rows[3] = {mys, iy, pys};
+		const double c1[3] = {cm, c0, cp};
+		const double L[3] = {1. / (dY * dY), -2. / (dY * dY), 1. / (dY * dY)};
+		const double dd[3] = {-0.5 / dY, 0, 0.5 / dY};
+		for(int k = 0; k < 3; k++) {
+			if(ok) {
+				int cyp = rows[k];
+				double kyy = X.avg(Q_YYTR, ix, cyp), kxy = X.avg(Q_XYTR, ix, cyp);
+				X.entry(L[k], 0.0, c1[k] * kxy, c1[k] * kyy, ix, cyp, dd[k], 1, r);
+			}
+			else r[0] = r[1] = r[2] = r[3] = z;
+			for(int b = 0; b < 4; b++) C[(size_t)(C_DY + 3 * b + k) * N] = cvt<S>(r[b]);
+			Dg[(size_t)(1 * 6 + 0 * 3 + k) * N] = r[0];
+			Dg[(size_t)(1 * 6 + 1 * 3 + k) * N] = r[3];
+		}
+	}
+	// DXDY: rows ix < Nx-1, iy < Ny-1 when Nx > 3 and Ny > 3; k = pxpy, mxpy, pxmy, mxmy.
+	{
+		bool ok = Nx > 3 && Ny > 3 && ix < Nx - 1 && iy < Ny - 1;
+		double a1 = 0, c1 = 0, a2 = 0, c2 = 0;
+		if(ok) {
+			a1 = 0.25 * ezz(pxq, iy) / (dX * dY); c1 = 0.25 * ezz(mxq, iy) / (dX * dY);
+			a2 = 0.25 * ezz(ix, pyq) / (dX * dY); c2 = 0.25 * ezz(ix, myq) / (dX * dY);
+		}
+		const double g0[4] = {-0.25 / (dX * dY), 0.25 / (dX * dY), 0.25 / (dX * dY), -0.25 / (dX * dY)};
+		const double d01[4] = {a1, -c1, -a1, c1};
+		const double d10[4] = {a2, -a2, -c2, c2};
+		const int cxs[4] = {pxs, mxs, pxs, mxs};
+		const int cys[4] = {pys, pys, mys, mys};
+		for(int k = 0; k < 4; k++) {
+			if(ok) {
+				double kxx = X.avg(Q_XXTR, cxs[k], cys[k]), kyy = X.avg(Q_YYTR, cxs[k], cys[k]);
+				double kxy = X.avg(Q_XYTR, cxs[k], cys[k]);
+				X.entry(d01[k] * kxy, g0[k] + d01[k] * kyy, g0[k] + d10[k] * kxx, d10[k] * kxy,
+					cxs[k], cys[k], 0.0, 0, r);
+			}
+			else r[0] = r[1] = r[2] = r[3] = z;
+			for(int b = 0; b < 4; b++) C[(size_t)(C_DXDY + 4 * b + k) * N] = cvt<S>(r[b]);
+		}
+	}
+}
+
+// ---------------------------------------------------------------------------------------
+// Pre-factorisation of the periodic line solves (I - mu*R_cc) x = b, one thread per
+// (group, comp, line), FP64. Restates shifted_block_vmult_inv (BlockSparseMatrix.cpp:
+// 195-258 and 386-449): Thomas sweep with beta0 = 2*mid0 and the Sherman-Morrison corner
+// vector corr (corr0 = -1/2). Everything that does not depend on the right-hand side is
+// computed here once per (wavelength, slab) and shared by all (q, pol) slots:
+//   F_INF  inf_i           F_RB  1/beta_i        F_GAM gamma_i
+//   F_COR  corr_i after back-substitution
+//   F_W    w_i = prod_{j<i}(-gamma_j), so that the back-substituted x_0 = sum_i w_i d_i
+//          is formed during the forward sweep
+// plus per line r0 = inf0/mid0 and rden = 1/(1 + corr0 - r0*corr_{L-2}) in FP64.
+// scr holds FP64 gamma and forward corr: [group][comp][2][N].
+// ---------------------------------------------------------------------------------------
+template <typename S>
+__global__ void k_factor(int dirn, Geom G, int ngroups, const cx<double>* __restrict__ diag,
+		cx<S>* __restrict__ fac, cx<double>* __restrict__ lsc, cx<double>* __restrict__ scr) {
+	int Nx = G.Nx, Ny = G.Ny, N = G.N;
+	int L = dirn == 0 ? Nx : Ny;
+	int nlines = dirn == 0 ? Ny : Nx;
+	int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if(t >= ngroups * 2 * nlines || L <= 3) return;
+	int line = t % nlines;
+	int c = (t / nlines) % 2;
+	int g = t / (2 * nlines);
+	const cx<double>* Dg = diag + (size_t)g * NDIAG * N + (size_t)(dirn * 6 + c * 3) * N;
+	cx<S>* Fc = fac + ((size_t)g * 2 + c) * NFAC * N;
+	cx<double>* sG = scr + ((size_t)g * 2 + c) * 2 * N;
+	cx<double>* sC = sG + N;
+	cx<double>* ls = lsc + (((size_t)g * 2 + c) * nlines + line) * 2;
+	const int stride = dirn == 0 ? 1 : Nx;
+	const int base = dirn == 0 ? Nx * line : line;
+	auto P = [&](int i) { return base + i * stride; };
+	const cx<double> one = mk(1.0, 0.0);
+	auto sup = [&](int i) { return -Dg[2 * (size_t)N + P(i)]; };
+	auto mid = [&](int i) { return one - Dg[1 * (size_t)N + P(i)]; };
+	auto inf = [&](int i) { return -Dg[P(i)]; };
+
+	cx<double> beta = 2.0 * mid(0);
+	Fc[F_RB * N + P(0)] = cvt<S>(crecip(beta));
+	Fc[F_INF * N + P(0)] = mk<S>(0, 0);
+	cx<double> corr = mk(-0.5, 0.0);
+	sC[P(0)] = corr;
+	for(int i = 1; i < L - 2; i++) {
+		cx<double> gam = cdiv(sup(i - 1), beta);
+		sG[P(i - 1)] = gam;
+		Fc[F_GAM * N + P(i - 1)] = cvt<S>(gam);
+		cx<double> in = inf(i);
+		beta = mid(i) - in * gam;
+		Fc[F_RB * N + P(i)] = cvt<S>(crecip(beta));
+		Fc[F_INF * N + P(i)] = cvt<S>(in);
+		corr = cdiv(-(in * corr), beta);
+		sC[P(i)] = corr;
+	}
+	cx<double> gl = cdiv(sup(L - 3), beta);
+	sG[P(L - 3)] = gl;
+	Fc[F_GAM * N + P(L - 3)] = cvt<S>(gl);
+	cx<double> inL = inf(L - 2);
+	beta = mid(L - 2) + cdiv(sup(L - 2) * inf(0), mid(0)) - inL * gl;
+	Fc[F_RB * N + P(L - 2)] = cvt<S>(crecip(beta));
+	Fc[F_INF * N + P(L - 2)] = cvt<S>(inL);
+	cx<double> corr_last = cdiv(sup(L - 2) - inL * corr, beta);
+	Fc[F_COR * N + P(L - 2)] = cvt<S>(corr_last);
+	Fc[F_GAM * N + P(L - 2)] = mk<S>(0, 0);
+	cx<double> cn = corr_last;
+	for(int i = L - 2; i > 0; i--) {
+		cx<double> cv = sC[P(i - 1)] - sG[P(i - 1)] * cn;
+		Fc[F_COR * N + P(i - 1)] = cvt<S>(cv);
+		cn = cv;
+	}
+	cx<double> w = one;
+	Fc[F_W * N + P(0)] = cvt<S>(w);
+	for(int i = 1; i < L - 1; i++) {
+		w = -(w * sG[P(i - 1)]);
+		Fc[F_W * N + P(i)] = cvt<S>(w);
+	}
+	cx<double> r0 = cdiv(inf(0), mid(0));
+	ls[0] = r0;
+	ls[1] = crecip(one + cn - r0 * corr_last);
+}
+
+// ---------------------------------------------------------------------------------------
+// Right-hand-side kernels over all (point, slot) pairs of a pass.
+// ---------------------------------------------------------------------------------------
+template <typename R>
+struct Stencil {
+	const cx<R>* C;
+	int N, Nx, Ny;
+	__device__ __forceinline__ cx<R> c(int plane, int p) const { return C[(size_t)plane * N + p]; }
+	// DX block b at row (x, y): columns mx, x, px with period Nx-1.
+	__device__ __forceinline__ cx<R> dx(int b, int x, int y, const cx<R>* s) const {
+		int p = x + Nx * y;
+		int mx = x == 0 ? Nx - 2 : x - 1, px = x == Nx - 2 ? 0 : x + 1;
+		int base = C_DX + 3 * b;
+		return c(base, p) * s[mx + Nx * y] + c(base + 1, p) * s[p] + c(base + 2, p) * s[px + Nx * y];
+	}
+	__device__ __forceinline__ cx<R> dy(int b, int x, int y, const cx<R>* s) const {
+		int p = x + Nx * y;
+		int my = y == 0 ? Ny - 2 : y - 1, py = y == Ny - 2 ? 0 : y + 1;
+		int base = C_DY + 3 * b;
+		return c(base, p) * s[x + Nx * my] + c(base + 1, p) * s[p] + c(base + 2, p) * s[x + Nx * py];
+	}
+	__device__ __forceinline__ cx<R> dxdy(int b, int x, int y, const cx<R>* s) const {
+		int p = x + Nx * y;
+		int mx = x == 0 ? Nx - 2 : x - 1, px = x == Nx - 2 ? 0 : x + 1;
+		int my = y == 0 ? Ny - 2 : y - 1, py = y == Ny - 2 ? 0 : y + 1;
+		int base = C_DXDY + 4 * b;
+		return c(base, p) * s[px + Nx * py] + c(base + 1, p) * s[mx + Nx * py] +
+			c(base + 2, p) * s[px + Nx * my] + c(base + 3, p) * s[mx + Nx * my];
+	}
+};
+
+// Step kinds of the composite stencil kernel (ParaxialPrimaryEvolutionOperator.cpp:153-207
+// with the duplicate-row/column fix-ups of BlockSparseMatrix.cpp folded in analytically).
+enum { ST_EXPL_Y = 0, ST_EXPL_X = 1, ST_WOOD_X = 2, ST_WOOD_Y = 3 };
+
+template <typename R, int KIND>
+__global__ void k_stencil(Geom G, int slot0, const cx<R>* __restrict__ coef, const cx<R>* __restrict__ src,
+		cx<R>* __restrict__ dst) {
+	int p = blockIdx.x * blockDim.x + threadIdx.x;
+	int N = G.N, Nx = G.Nx, Ny = G.Ny;
+	if(p >= N) return;
+	int s = blockIdx.y;
+	int g = (slot0 + s) / G.spg - slot0 / G.spg;
+	Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
+	const cx<R>* f0 = src + (size_t)s * 2 * N;
+	const cx<R>* f1 = f0 + N;
+	int ix = p % Nx, iy = p / Nx;
+	int xx = ix == Nx - 1 ? 0 : ix, yy = iy == Ny - 1 ? 0 : iy;
+	bool ax = Nx > 3, ay = Ny > 3;
+	cx<R> T0 = mk<R>(0, 0), T1 = mk<R>(0, 0);
+	if(KIND == ST_EXPL_Y) {
+		if(ay) {
+			T0 = st.dy(0, ix, yy, f0) + st.dy(1, ix, yy, f1);
+			if(ax) T1 = st.dy(3, xx, yy, f1) + st.dxdy(3, xx, yy, f1) + st.dy(2, xx, yy, f0) + st.dxdy(2, xx, yy, f0);
+			else T1 = st.dy(3, ix, yy, f1) + st.dy(2, ix, yy, f0);
+		}
+		dst[(size_t)s * 2 * N + p] = f0[p] + T0;
+		dst[(size_t)s * 2 * N + N + p] = f1[p] + T1;
+	}
+	else if(KIND == ST_EXPL_X) {
+		if(ax) {
+			if(ay) T0 = st.dx(0, xx, yy, f0) + st.dxdy(0, xx, yy, f0) + st.dx(1, xx, yy, f1) + st.dxdy(1, xx, yy, f1);
+			else T0 = st.dx(0, xx, iy, f0) + st.dx(1, xx, iy, f1);
+			T1 = st.dx(3, xx, iy, f1) + st.dx(2, xx, iy, f0);
+		}
+		dst[(size_t)s * 2 * N + p] = f0[p] + T0;
+		dst[(size_t)s * 2 * N + N + p] = f1[p] + T1;
+	}
+	else if(KIND == ST_WOOD_X) {
+		if(ax) {
+			if(ay) T0 = st.dx(1, xx, yy, f1) + st.dxdy(1, xx, yy, f1) + st.dxdy(0, xx, yy, f0);
+			else T0 = st.dx(1, xx, iy, f1);
+			T1 = st.dx(2, xx, iy, f0);
+		}
+		dst[(size_t)s * 2 * N + p] = T0;
+		dst[(size_t)s * 2 * N + N + p] = T1;
+	}
+	else {
+		if(ay) {
+			T0 = st.dy(1, ix, yy, f1);
+			if(ax) T1 = st.dy(2, xx, yy, f0) + st.dxdy(2, xx, yy, f0) + st.dxdy(3, xx, yy, f1);
+			else T1 = st.dy(2, ix, yy, f0);
+		}
+		dst[(size_t)s * 2 * N + p] = T0;
+		dst[(size_t)s * 2 * N + N + p] = T1;
+	}
+}
+
+// Periodic line solve with the pre-factored Thomas/Sherman-Morrison data. One thread per
+// (line, comp, slot). dst may alias src. If acc_out is set: acc_out = acc_in + x.
+template <typename R, int DIRN>
+__global__ void k_solve(Geom G, int slot0, int nslots, const cx<R>* __restrict__ fac,
+		const cx<double>* __restrict__ lsc, const cx<R>* src, cx<R>* dst,
+		const cx<R>* acc_in, cx<R>* acc_out) {
+	int Nx = G.Nx, Ny = G.Ny, N = G.N;
+	int L = DIRN == 0 ? Nx : Ny;
+	int nlines = DIRN == 0 ? Ny : Nx;
+	int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if(t >= nslots * 2 * nlines) return;
+	int line = t % nlines;
+	int c = (t / nlines) % 2;
+	int s = t / (2 * nlines);
+	int g = (slot0 + s) / G.spg - slot0 / G.spg;
+	size_t off = (size_t)s * 2 * N + (size_t)c * N;
+	const cx<R>* S = src + off;
+	cx<R>* D = dst + off;
+	const int stride = DIRN == 0 ? 1 : Nx;
+	const int base = DIRN == 0 ? Nx * line : line;
+	if(L <= 3) {
+		for(int i = 0; i < L; i++) {
+			int q = base + i * stride;
+			cx<R> x = S[q];
+			D[q] = x;
+			if(acc_out) acc_out[off + q] = acc_in[off + q] + x;
+		}
+		return;
+	}
+	const cx<R>* Fc = fac + ((size_t)g * 2 + c) * NFAC * N;
+	const cx<double>* ls = lsc + (((size_t)g * 2 + c) * nlines + line) * 2;
+	// forward sweep
+	int q = base;
+	cx<R> d = S[q] * Fc[F_RB * N + q];
+	cx<R> acc = d;
+	D[q] = d;
+	for(int i = 1; i < L - 1; i++) {
+		q += stride;
+		cx<R> sv = S[q];
+		d = (sv - Fc[F_INF * N + q] * d) * Fc[F_RB * N + q];
+		acc += Fc[F_W * N + q] * d;
+		D[q] = d;
+	}
+	cx<double> frac = (cvt<double>(acc) - ls[0] * cvt<double>(d)) * ls[1];
+	cx<R> fr = cvt<R>(frac);
+	// backward sweep with the Sherman-Morrison correction applied on the way
+	cx<R> dn = d;
+	cx<R> x = dn - fr * Fc[F_COR * N + q];
+	D[q] = x;
+	if(acc_out) acc_out[off + q] = acc_in[off + q] + x;
+	for(int i = L - 2; i > 0; i--) {
+		q -= stride;
+		cx<R> dp = D[q] - Fc[F_GAM * N + q] * dn;
+		x = dp - fr * Fc[F_COR * N + q];
+		D[q] = x;
+		if(acc_out) acc_out[off + q] = acc_in[off + q] + x;
+		dn = dp;
+	}
+	int qe = base + (L - 1) * stride;
+	D[qe] = x;  // duplicate point = x_0
+	if(acc_out) acc_out[off + qe] = acc_in[off + qe] + x;
+}
+
+// Point-wise symmetric 2x2 phase operator (PhaseEvolutionOperator.cpp:14-32).
+template <typename R>
+__global__ void k_phase(Geom G, int slot0, const cx<R>* __restrict__ coef, cx<R>* F) {
+	int p = blockIdx.x * blockDim.x + threadIdx.x;
+	if(p >= G.N) return;
+	int s = blockIdx.y;
+	int N = G.N;
+	int g = (slot0 + s) / G.spg - slot0 / G.spg;
+	const cx<R>* C = coef + (size_t)g * NCOEF * N + p;
+	cx<R> oxx = C[(C_PH + 0) * (size_t)N], oyy = C[(C_PH + 1) * (size_t)N], oxy = C[(C_PH + 2) * (size_t)N];
+	cx<R>* f = F + (size_t)s * 2 * N + p;
+	cx<R> a = f[0], b = f[N];
+	f[0] = oxx * a + oxy * b;
+	f[N] = oxy * a + oyy * b;
+}
+
+// Transverse translation for tilted incidence (SimpleShiftOperator.cpp:52-93): 4-tap cubic
+// interpolation with period Nx-1 / Ny-1 (wrap rule SimpleShiftOperator.h:24-39).
+__device__ __forceinline__ int ref_wrap(int i, int n) {
+	if(i > n - 2) return i % (n - 1);
+	if(i < 0) return i + (1 - i / (n - 1)) * (n - 1);
+	return i;
+}
+
+template <typename R>
+__global__ void k_shift_x(Geom G, int slot0, const ShiftParams* __restrict__ sp, const cx<R>* __restrict__ F,
+		cx<R>* __restrict__ T) {
+	int p = blockIdx.x * blockDim.x + threadIdx.x;
+	if(p >= G.N) return;
+	int s = blockIdx.y;
+	int gs = slot0 + s;
+	int gq = (gs / G.spg) * G.Nq + (gs / 2) % G.Nq;
+	const ShiftParams P = sp[gq];
+	if(!P.active) return;
+	int N = G.N, Nx = G.Nx;
+	int ix = p % Nx, iy = p / Nx;
+	for(int c = 0; c < 2; c++) {
+		const cx<R>* f = F + (size_t)s * 2 * N + (size_t)c * N;
+		cx<R> v;
+		if(Nx > 3) {
+			v = mk<R>(0, 0);
+			for(int k = 0; k < 4; k++)
+				v += (R)P.wx[k] * f[ref_wrap(ix + P.msx - 1 + k, Nx) + Nx * iy];
+		}
+		else v = f[p];
+		T[(size_t)s * 2 * N + (size_t)c * N + p] = v;
+	}
+}
+
+template <typename R>
+__global__ void k_shift_y(Geom G, int slot0, const ShiftParams* __restrict__ sp, const cx<R>* __restrict__ T,
+		cx<R>* __restrict__ F) {
+	int p = blockIdx.x * blockDim.x + threadIdx.x;
+	if(p >= G.N) return;
+	int s = blockIdx.y;
+	int gs = slot0 + s;
+	int gq = (gs / G.spg) * G.Nq + (gs / 2) % G.Nq;
+	const ShiftParams P = sp[gq];
+	if(!P.active) return;
+	int N = G.N, Nx = G.Nx, Ny = G.Ny;
+	int ix = p % Nx, iy = p / Nx;
+	cx<R> ph = mk<R>((R)P.ph_re, (R)P.ph_im);
+	for(int c = 0; c < 2; c++) {
+		const cx<R>* t = T + (size_t)s * 2 * N + (size_t)c * N;
+		cx<R> v;
+		if(Ny > 3) {
+			v = mk<R>(0, 0);
+			for(int k = 0; k < 4; k++)
+				v += (R)P.wy[k] * t[ix + Nx * ref_wrap(iy + P.msy - 1 + k, Ny)];
+		}
+		else v = t[p];
+		F[(size_t)s * 2 * N + (size_t)c * N + p] = v * ph;
+	}
+}
+
+// Entrance field: beam profile with polarisation angle pi/2*pol (BPMIteration.cpp:87-109,
+// BeamProfile.cpp:17-39) followed by the input Fresnel operator (FresnelOperator.cpp:16-38)
+// built on sqrt(eps_tr) at iz = 0.
+template <typename R>
+__global__ void k_init_fields(Geom G, int slot0, const GroupParams* __restrict__ gps, const double* __restrict__ Q0,
+		int beam_type, double waist, double dx, double dy, cx<R>* F) {
+	int p = blockIdx.x * blockDim.x + threadIdx.x;
+	if(p >= G.N) return;
+	int s = blockIdx.y;
+	int N = G.N, Nx = G.Nx, Ny = G.Ny;
+	int gs = slot0 + s;
+	int g = gs / G.spg - slot0 / G.spg;
+	int pol = gs % 2;
+	const double PI_REF = 3.1415926535897932;
+	double th = 0.5 * PI_REF * pol;
+	double x = ((p % Nx) - (Nx - 1) / 2.) * dx, y = ((p / Nx) - (Ny - 1) / 2.) * dy;
+	double amp = beam_type == 1 ? exp(-(x * x + y * y) / (2 * waist * waist)) : 1.0;
+	double ex = cos(th) * amp, ey = sin(th) * amp;
+	const double* Q = Q0 + (size_t)g * NQ * N;
+	double nxx = Q[Q_XXS * N + p], nyy = Q[Q_YYS * N + p], nxy = Q[Q_XYS * N + p];
+	double n = gps[g].nin;
+	double det = (n + nxx) * (n + nyy) - nxy * nxy;
+	double a = 2 * n * (n + nyy) / det * ex - 2 * n * nxy / det * ey;
+	double b = -2 * n * nxy / det * ex + 2 * n * (n + nxx) / det * ey;
+	F[(size_t)s * 2 * N + p] = mk<R>((R)a, 0);
+	F[(size_t)s * 2 * N + N + p] = mk<R>((R)b, 0);
+}
+
+// Output Fresnel operator at iz = Nz-1 (FresnelOperator.cpp:45-69).
+template <typename R>
+__global__ void k_fresnel_out(Geom G, int slot0, const GroupParams* __restrict__ gps, const double* __restrict__ QL,
+		cx<R>* F) {
+	int p = blockIdx.x * blockDim.x + threadIdx.x;
+	if(p >= G.N) return;
+	int s = blockIdx.y;
+	int N = G.N;
+	int g = (slot0 + s) / G.spg - slot0 / G.spg;
+	const double* Q = QL + (size_t)g * NQ * N;
+	double nxx = Q[Q_XXS * N + p], nyy = Q[Q_YYS * N + p], nxy = Q[Q_XYS * N + p];
+	double n = gps[g].nout_fresnel;
+	double det = (n + nxx) * (n + nyy) - nxy * nxy;
+	double axx = 2. * (1. - n * (n + nyy) / det), ayy = 2. * (1. - n * (n + nxx) / det), axy = 2. * (n * nxy / det);
+	cx<R>* f = F + (size_t)s * 2 * N + p;
+	cx<double> a = cvt<double>(f[0]), b = cvt<double>(f[N]);
+	f[0] = cvt<R>(axx * a + axy * b);
+	f[N] = cvt<R>(ayy * b + axy * a);
+}
+
+template <typename R>
+__global__ void k_copy(size_t n, const cx<R>* __restrict__ a, cx<R>* __restrict__ b) {
+	size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+	if(i < n) b[i] = a[i];
+}
+
+template <typename R>
+__global__ void k_widen(size_t n, const cx<R>* __restrict__ a, cx<double>* __restrict__ b) {
+	size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+	if(i < n) b[i] = cvt<double>(a[i]);
+}
+
+template <typename R>
+__global__ void k_narrow(size_t n, const cx<double>* __restrict__ a, cx<R>* __restrict__ b) {
+	size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+	if(i < n) b[i] = cvt<R>(a[i]);
+}
+
+}  // namespace nbpm

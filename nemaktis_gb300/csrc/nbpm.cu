@@ -1,0 +1,746 @@
+// libnbpm: host orchestration and C ABI of the GB300 bpm backend.
+//
+// Replaces the reference's backend entry (BeamPropagationSolver/src/PythonBackend/
+// bpm_backend.cpp:7-164) and the orchestration of BPMIteration::propagate_fields
+// (BeamPropagationLib/BPMIteration.cpp:53-177) + ScreenOutput::apply_no_export
+// (PostprocessorLib/ScreenOutput.cpp:184-224). All arithmetic runs in the kernels of
+// bpm_kernels.cuh and fft_kernels.cuh; the host parses, validates, allocates, uploads and
+// launches (inside one captured CUDA graph per plan).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/nbpm.h"
+#include "bpm_kernels.cuh"
+#include "fft_kernels.cuh"
+#include "host_settings.h"
+
+namespace nbpm {
+
+static thread_local std::string g_last_error;
+
+#define CK(call)                                                                                   \
+	do {                                                                                           \
+		cudaError_t e_ = (call);                                                                   \
+		if(e_ != cudaSuccess) {                                                                    \
+			if(e_ == cudaErrorMemoryAllocation)                                                    \
+				throw BackendError(E_MEMORY, std::string("CUDA out of memory: ") + #call);         \
+			throw BackendError(E_CUDA, std::string(cudaGetErrorString(e_)) + " at " + #call);      \
+		}                                                                                          \
+	} while(0)
+
+// ---------------------------------------------------------------------------------------
+// Device memory owner.
+// ---------------------------------------------------------------------------------------
+struct DevBuf {
+	void* p = nullptr;
+	size_t bytes = 0;
+	DevBuf() = default;
+	DevBuf(const DevBuf&) = delete;
+	DevBuf& operator=(const DevBuf&) = delete;
+	~DevBuf() { if(p) cudaFree(p); }
+	void alloc(size_t b) {
+		if(p) { cudaFree(p); p = nullptr; }
+		bytes = b;
+		if(b) CK(cudaMalloc(&p, b));
+	}
+	template <typename T> T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+struct SampleHost {
+	BackendSettings s;
+	const double* lc = nullptr;
+	int fd = 3;
+	std::vector<unsigned char> mask;
+	std::vector<double> wts;
+	bool has_mask = false, has_wts = false;
+	double* E = nullptr;  // user buffer, complex128 interleaved
+	int G = 0, Nq = 0, spg = 0, slots = 0;
+	Geom geom;
+	size_t nvox = 0;
+	std::vector<GroupParams> gps;
+	std::vector<ShiftParams> shifts;
+	bool any_shift = false;
+	ScreenParams sp;
+	// device
+	DevBuf dir, dmask, dwts, F, E0, gpsd, shiftd, partial, wl, nout, qv;
+};
+
+static std::vector<int> fft_radices(int n) {
+	std::vector<int> r;
+	while(n % 4 == 0 && n > 1) { r.push_back(4); n /= 4; }
+	while(n % 2 == 0) { r.push_back(2); n /= 2; }
+	for(int p = 3; n > 1 && p * p <= n; p += 2)
+		while(n % p == 0) { r.push_back(p); n /= p; }
+	if(n > 1) r.push_back(n);
+	return r;
+}
+
+// Nearest-index divisions used by the shift operator are computed on the device from nref;
+// this kernel restates the SimpleShiftOperator constructor (SimpleShiftOperator.cpp:3-50).
+__global__ void k_nref_final(int ngroups, int nblocks, size_t nvox, const double* __restrict__ partial,
+		GroupParams* gps) {
+	int g = blockIdx.x * blockDim.x + threadIdx.x;
+	if(g >= ngroups) return;
+	double s = 0;
+	for(int b = 0; b < nblocks; b++) s += partial[(size_t)g * nblocks + b];
+	gps[g].nref = s / (double)nvox;
+}
+
+__global__ void k_shift_params(int ngroups, int Nq, int Nx, int Ny, const GroupParams* __restrict__ gps,
+		const double* __restrict__ qv, ShiftParams* sp) {
+	int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if(t >= ngroups * Nq) return;
+	int g = t / Nq, q = t % Nq;
+	double qx = qv[2 * q], qy = qv[2 * q + 1];
+	ShiftParams P;
+	P.active = !(qx == 0 && qy == 0);
+	double nref = gps[g].nref, dZ = gps[g].dZ, dX = gps[g].dX;
+	double arg = -dZ * (qx * qx + qy * qy) / (4 * nref);  // exp(-i*dZ*|q|^2/(4 nref))
+	double s, c;
+	sincos(arg, &s, &c);
+	P.ph_re = c; P.ph_im = s;
+	P.msx = P.msy = 0;
+	for(int k = 0; k < 4; k++) { P.wx[k] = 0; P.wy[k] = 0; }
+	P.wx[1] = P.wy[1] = 1;
+	if(Nx > 3) {
+		double xs = -dZ * qx / (2 * nref * dX);
+		double ms = floor(xs), nu = xs - ms;
+		P.msx = (int)ms;
+		P.wx[0] = -nu * (1 - nu) * (1 - nu) / 2;
+		P.wx[1] = (1 - nu) * (1 + nu - 3 * nu * nu / 2);
+		P.wx[2] = nu * (1 + 4 * nu - 3 * nu * nu) / 2;
+		P.wx[3] = -nu * nu * (1 - nu) / 2;
+	}
+	if(Ny > 3) {
+		double ys = -dZ * qy / (2 * nref * dX);  // the reference divides by the x spacing
+		double ms = floor(ys), nu = ys - ms;
+		P.msy = (int)ms;
+		P.wy[0] = -nu * (1 - nu) * (1 - nu) / 2;
+		P.wy[1] = (1 - nu) * (1 + nu - 3 * nu * nu / 2);
+		P.wy[2] = nu * (1 + 4 * nu - 3 * nu * nu) / 2;
+		P.wy[3] = -nu * nu * (1 - nu) / 2;
+	}
+	sp[t] = P;
+}
+
+// ---------------------------------------------------------------------------------------
+// Plan
+// ---------------------------------------------------------------------------------------
+struct PlanBase {
+	virtual ~PlanBase() {}
+	virtual void upload() = 0;
+	virtual void execute(nbpm_timing* t) = 0;
+	virtual void download() = 0;
+	virtual long long device_bytes() const = 0;
+	virtual double slab_ms() const = 0;
+};
+
+template <typename R>
+struct Plan : PlanBase {
+	nbpm_options opt;
+	std::vector<std::unique_ptr<SampleHost>> S;
+	cudaStream_t stream = nullptr;
+	cudaGraphExec_t gexec = nullptr;
+	cudaEvent_t ev[6];
+	// workspace (shared by passes, sized for the largest)
+	DevBuf T, T2, Qring, coef, diag, facx, facy, lscx, lscy, scr, stage, twx, twy;
+	std::vector<DevBuf*> tw_bufs;
+	std::vector<std::unique_ptr<DevBuf>> tw_store;
+	std::vector<std::pair<int, cx<R>*>> tw_tables;
+	int launches = 0;
+	long long dev_bytes = 0;
+	double last_slab_ms = 0;
+	size_t smem_limit = 0;
+
+	Plan(const nbpm_options& o) : opt(o) {
+		for(auto& e : ev) e = nullptr;
+	}
+	~Plan() override {
+		if(gexec) cudaGraphExecDestroy(gexec);
+		for(auto& e : ev) if(e) cudaEventDestroy(e);
+		if(stream) cudaStreamDestroy(stream);
+	}
+
+	cx<R>* twiddles(int n) {
+		for(auto& t : tw_tables) if(t.first == n) return t.second;
+		std::vector<cx<R>> h(n);
+		const double PI_REF = 3.1415926535897932;
+		for(int k = 0; k < n; k++) {
+			double a = 2 * PI_REF * (double)k / (double)n;
+			h[k] = mk<R>((R)std::cos(a), (R)(-std::sin(a)));
+		}
+		tw_store.emplace_back(new DevBuf());
+		tw_store.back()->alloc(sizeof(cx<R>) * n);
+		CK(cudaMemcpy(tw_store.back()->p, h.data(), sizeof(cx<R>) * n, cudaMemcpyHostToDevice));
+		dev_bytes += sizeof(cx<R>) * n;
+		tw_tables.emplace_back(n, tw_store.back()->as<cx<R>>());
+		return tw_tables.back().second;
+	}
+
+	void setup(int ns, const nbpm_sample* samples) {
+		for(int i = 0; i < ns; i++) {
+			const nbpm_sample& in = samples[i];
+			if(!in.json_str || !in.lc_field_vals || !in.E_field_vals)
+				throw BackendError(E_ARG, "null pointer argument");
+			std::unique_ptr<SampleHost> h(new SampleHost());
+			h->s = parse_settings(in.json_str);
+			auto& s = h->s;
+			size_t nv = (size_t)s.Nx * s.Ny * s.Nz;
+			h->nvox = nv;
+			// VectorField(mesh, vals, n) (VectorField.cpp:27-40 / :43-58)
+			if(in.n_lc_vals < 0 || nv == 0) throw BackendError(E_SIZE, "Wrong dimension for the user pointer array (VectorField)");
+			int fd = (int)((size_t)in.n_lc_vals / nv);
+			if((size_t)in.n_lc_vals != nv * (size_t)fd)
+				throw BackendError(E_SIZE, in.mask_vals ? "Wrong dimension for the user pointer array"
+					: "Wrong dimension for the user pointer array (VectorField)");
+			if(in.mask_vals && (size_t)in.n_mask_vals != nv)
+				throw BackendError(E_SIZE, "Wrong dimension for the mask pointer array");
+			if(fd != 3 && fd != 6)
+				throw BackendError(E_SIZE, "Unexpected dimension for the LC orientational field, should be 3 or 6.");
+			h->fd = fd;
+			h->lc = in.lc_field_vals;
+			h->G = (int)s.wavelengths.size();
+			h->Nq = (int)s.q.size();
+			h->spg = 2 * h->Nq;
+			h->slots = h->G * h->spg;
+			// ScreenOpticalFieldCollection (OpticalFieldCollection.cpp:37-39)
+			long long need = (long long)h->slots * 2 * s.Nx * s.Ny;
+			if((long long)in.n_E_vals != need)
+				throw BackendError(E_SIZE, "Wrong dimension for the user pointer array (OpticalFieldCollection)");
+			if(s.iso_thick.size() > 8) throw BackendError(E_SETTINGS, "At most 8 isotropic layers are supported");
+			h->E = in.E_field_vals;
+			if(in.mask_vals) {
+				h->has_mask = true;
+				mask_weights(s, in.mask_vals, in.mask_formula ? std::string(in.mask_formula) : std::string(),
+					h->mask, h->wts);
+				h->has_wts = false;
+				for(double w : h->wts) if(w != 0.5) { h->has_wts = true; break; }
+			}
+			h->geom.Nx = s.Nx; h->geom.Ny = s.Ny; h->geom.N = s.Nx * s.Ny; h->geom.Nz = s.Nz;
+			h->geom.spg = h->spg; h->geom.Nq = h->Nq;
+			const double PI_REF = 3.1415926535897932;
+			for(int g = 0; g < h->G; g++) {
+				GroupParams gp;
+				gp.wavelength = s.wavelengths[g];
+				gp.k0 = 2 * PI_REF / gp.wavelength;
+				gp.dX = gp.k0 * s.dx; gp.dY = gp.k0 * s.dy; gp.dZ = gp.k0 * s.dz;
+				gp.no = s.no[g]; gp.ne = s.ne[g]; gp.ne_imag = s.ne_imag[g];
+				gp.nhost = s.nhost[g]; gp.nin = s.nin[g];
+				gp.nout_fresnel = s.iso_index.size() > 0 ? s.iso_index[0] : s.nout[g];
+				gp.absorp_im = gp.ne_imag / (gp.ne - gp.no);
+				gp.nref = 0;
+				h->gps.push_back(gp);
+			}
+			for(auto& q : s.q) if(!(q.first == 0 && q.second == 0)) h->any_shift = true;
+			ScreenParams& sp = h->sp;
+			sp.Nx = s.Nx; sp.Ny = s.Ny; sp.Nq = h->Nq; sp.n_iso = (int)s.iso_thick.size();
+			sp.dx = s.dx; sp.dy = s.dy; sp.NA = s.NA;
+			// ScreenOutput ctor (ScreenOutput.cpp:32-38): z_foc -= t_p * nout(0.6) / n_p
+			double zf = s.z_foc;
+			for(size_t l = 0; l < s.iso_thick.size(); l++) zf -= s.iso_thick[l] * s.nout_06 / s.iso_index[l];
+			sp.z_foc = zf;
+			for(int l = 0; l < 8; l++) sp.thick[l] = l < sp.n_iso ? s.iso_thick[l] : 0;
+			for(int l = 0; l < 9; l++) sp.index[l] = l < sp.n_iso ? s.iso_index[l] : 1;
+			S.push_back(std::move(h));
+		}
+		// Host-side validation is complete; only now touch the device.
+		CK(cudaSetDevice(opt.device));
+		CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+		for(auto& e : ev) CK(cudaEventCreate(&e));
+		int dev = opt.device;
+		int optin = 0;
+		CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+		smem_limit = (size_t)optin;
+		CK(cudaFuncSetAttribute(k_fft_lines<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit));
+		allocate();
+	}
+
+	int gpp(const SampleHost& h) const {
+		int g = opt.groups_per_pass <= 0 ? h.G : std::min(opt.groups_per_pass, h.G);
+		return std::max(1, g);
+	}
+
+	void allocate() {
+		size_t maxT = 0, maxQ = 0, maxC = 0, maxD = 0, maxFx = 0, maxL = 0, maxScr = 0, maxStage = 0;
+		for(auto& hp : S) {
+			SampleHost& h = *hp;
+			size_t N = h.geom.N;
+			int ng = gpp(h);
+			maxT = std::max(maxT, (size_t)ng * h.spg * 2 * N);
+			maxQ = std::max(maxQ, (size_t)2 * ng * NQ * N);
+			maxC = std::max(maxC, (size_t)ng * NCOEF * N);
+			maxD = std::max(maxD, (size_t)ng * NDIAG * N);
+			maxFx = std::max(maxFx, (size_t)ng * 2 * NFAC * N);
+			maxL = std::max(maxL, (size_t)ng * 2 * std::max(h.s.Nx, h.s.Ny) * 2);
+			maxScr = std::max(maxScr, (size_t)ng * 2 * 2 * N);
+			if(sizeof(R) != sizeof(double)) maxStage = std::max(maxStage, (size_t)h.slots * 2 * N);
+			// per-sample buffers
+			h.dir.alloc(sizeof(double) * h.nvox * h.fd);
+			if(h.has_mask) h.dmask.alloc(h.nvox);
+			if(h.has_wts) h.dwts.alloc(sizeof(double) * h.wts.size());
+			h.F.alloc(sizeof(cx<R>) * (size_t)h.slots * 2 * N);
+			if(h.s.beam_type == 2) h.E0.alloc(sizeof(cx<R>) * (size_t)h.slots * 2 * N);
+			h.gpsd.alloc(sizeof(GroupParams) * h.G);
+			h.shiftd.alloc(sizeof(ShiftParams) * h.G * h.Nq);
+			h.partial.alloc(sizeof(double) * h.G * 1024);
+			h.wl.alloc(sizeof(double) * h.G);
+			h.nout.alloc(sizeof(double) * h.G);
+			h.qv.alloc(sizeof(double) * 2 * h.Nq);
+			dev_bytes += h.dir.bytes + h.dmask.bytes + h.dwts.bytes + h.F.bytes + h.E0.bytes;
+			twiddles(h.s.Nx);
+			twiddles(h.s.Ny);
+		}
+		T.alloc(sizeof(cx<R>) * maxT);
+		T2.alloc(sizeof(cx<R>) * maxT);
+		Qring.alloc(sizeof(double) * maxQ);
+		coef.alloc(sizeof(cx<R>) * maxC);
+		diag.alloc(sizeof(cx<double>) * maxD);
+		facx.alloc(sizeof(cx<R>) * maxFx);
+		facy.alloc(sizeof(cx<R>) * maxFx);
+		lscx.alloc(sizeof(cx<double>) * maxL);
+		lscy.alloc(sizeof(cx<double>) * maxL);
+		scr.alloc(sizeof(cx<double>) * maxScr);
+		stage.alloc(sizeof(cx<double>) * maxStage);
+		dev_bytes += T.bytes + T2.bytes + Qring.bytes + coef.bytes + diag.bytes + facx.bytes + facy.bytes +
+			lscx.bytes + lscy.bytes + scr.bytes + stage.bytes;
+	}
+
+	void upload() override {
+		for(auto& hp : S) {
+			SampleHost& h = *hp;
+			CK(cudaMemcpyAsync(h.dir.p, h.lc, h.dir.bytes, cudaMemcpyHostToDevice, stream));
+			if(h.has_mask) CK(cudaMemcpyAsync(h.dmask.p, h.mask.data(), h.nvox, cudaMemcpyHostToDevice, stream));
+			if(h.has_wts) CK(cudaMemcpyAsync(h.dwts.p, h.wts.data(), h.dwts.bytes, cudaMemcpyHostToDevice, stream));
+			CK(cudaMemcpyAsync(h.gpsd.p, h.gps.data(), h.gpsd.bytes, cudaMemcpyHostToDevice, stream));
+			CK(cudaMemcpyAsync(h.wl.p, h.s.wavelengths.data(), h.wl.bytes, cudaMemcpyHostToDevice, stream));
+			CK(cudaMemcpyAsync(h.nout.p, h.s.nout.data(), h.nout.bytes, cudaMemcpyHostToDevice, stream));
+			std::vector<double> qflat;
+			for(auto& q : h.s.q) { qflat.push_back(q.first); qflat.push_back(q.second); }
+			CK(cudaMemcpyAsync(h.qv.p, qflat.data(), h.qv.bytes, cudaMemcpyHostToDevice, stream));
+			CK(cudaStreamSynchronize(stream));  // qflat lifetime
+			if(h.s.beam_type == 2) {
+				size_t n = (size_t)h.slots * 2 * h.geom.N;
+				if(sizeof(R) == sizeof(double)) {
+					CK(cudaMemcpyAsync(h.E0.p, h.E, n * sizeof(cx<double>), cudaMemcpyHostToDevice, stream));
+				}
+				else {
+					CK(cudaMemcpyAsync(stage.p, h.E, n * sizeof(cx<double>), cudaMemcpyHostToDevice, stream));
+					k_narrow<R><<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, stage.as<cx<double>>(), h.E0.as<cx<R>>());
+					CK(cudaGetLastError());
+				}
+			}
+		}
+		CK(cudaStreamSynchronize(stream));
+	}
+
+	void download() override {
+		for(auto& hp : S) {
+			SampleHost& h = *hp;
+			size_t n = (size_t)h.slots * 2 * h.geom.N;
+			if(sizeof(R) == sizeof(double)) {
+				CK(cudaMemcpyAsync(h.E, h.F.p, n * sizeof(cx<double>), cudaMemcpyDeviceToHost, stream));
+			}
+			else {
+				k_widen<R><<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, h.F.as<cx<R>>(), stage.as<cx<double>>());
+				CK(cudaGetLastError());
+				CK(cudaMemcpyAsync(h.E, stage.p, n * sizeof(cx<double>), cudaMemcpyDeviceToHost, stream));
+			}
+		}
+		CK(cudaStreamSynchronize(stream));
+	}
+
+	// ---- launch helpers (count launches while recording) ----
+	dim3 pgrid(int N, int ny) { return dim3((unsigned)((N + 255) / 256), (unsigned)ny); }
+
+	void fft2(SampleHost& h, cx<R>* F, int nplanes, int sign) {
+		int Nx = h.s.Nx, Ny = h.s.Ny;
+		for(int pass = 0; pass < 2; pass++) {
+			int n = pass == 0 ? Nx : Ny;
+			if(n == 1) continue;
+			FftPlan1D P;
+			auto rad = fft_radices(n);
+			if((int)rad.size() > FFT_MAX_STAGES) throw BackendError(E_INTERNAL, "FFT plan too deep");
+			P.n = n; P.nst = (int)rad.size();
+			for(int i = 0; i < P.nst; i++) P.radix[i] = rad[i];
+			size_t per_line = 2 * (size_t)(n + 1) * sizeof(cx<R>);
+			if(per_line > smem_limit)
+				throw BackendError(E_SETTINGS, "FFT line length " + std::to_string(n) + " exceeds shared memory");
+			int lpb = (int)std::max<size_t>(1, std::min<size_t>(64, (size_t)(48 * 1024) / per_line));
+			if(pass == 1) lpb = std::max(lpb, std::min(16, (int)(smem_limit / per_line)));
+			lpb = std::max(1, std::min(lpb, (int)(smem_limit / per_line)));
+			size_t smem = per_line * lpb;
+			int nlines, lpp;
+			long long ps = (long long)Nx * Ny, ls, es;
+			if(pass == 0) { nlines = nplanes * Ny; lpp = Ny; ls = Nx; es = 1; }
+			else { nlines = nplanes * Nx; lpp = Nx; ls = 1; es = Nx; }
+			int blocks = (nlines + lpb - 1) / lpb;
+			int threads = std::min(256, std::max(32, ((lpb * n / 2) + 31) / 32 * 32));
+			k_fft_lines<R><<<blocks, threads, smem, stream>>>(F, P, nlines, lpp, ps, ls, es, lpb, twiddles(n), sign);
+			CK(cudaGetLastError());
+			launches++;
+		}
+	}
+
+	void record() {
+		launches = 0;
+		for(auto& hp : S) record_sample(*hp);
+	}
+
+	void record_sample(SampleHost& h) {
+		const Geom Gm = h.geom;
+		const int N = Gm.N, Nx = Gm.Nx, Ny = Gm.Ny, Nz = Gm.Nz;
+		const int Nw = h.s.n_woodbury;
+		cx<R>* F = h.F.as<cx<R>>();
+		// nref for every group, then shift parameters (device side)
+		{
+			int nb = (int)std::min<size_t>(1024, (h.nvox + 255) / 256);
+			k_neff_partial<<<dim3(nb, h.G), 256, 0, stream>>>(h.dir.as<double>(), h.fd,
+				h.has_mask ? h.dmask.as<uint8_t>() : nullptr, h.nvox, h.gpsd.as<GroupParams>(), h.partial.as<double>());
+			k_nref_final<<<(h.G + 63) / 64, 64, 0, stream>>>(h.G, nb, h.nvox, h.partial.as<double>(), h.gpsd.as<GroupParams>());
+			k_shift_params<<<(h.G * h.Nq + 63) / 64, 64, 0, stream>>>(h.G, h.Nq, Nx, Ny, h.gpsd.as<GroupParams>(),
+				h.qv.as<double>(), h.shiftd.as<ShiftParams>());
+			CK(cudaGetLastError());
+			launches += 3;
+		}
+		int ngp = gpp(h);
+		for(int ga = 0; ga < h.G; ga += ngp) {
+			int ng = std::min(ngp, h.G - ga);
+			int slot0 = ga * h.spg, nsl = ng * h.spg;
+			const GroupParams* gps = h.gpsd.as<GroupParams>() + ga;
+			cx<R>* Fp = F + (size_t)slot0 * 2 * N;
+			cx<R>* Tb = T.as<cx<R>>();
+			cx<R>* T2b = T2.as<cx<R>>();
+			double* Q0 = Qring.as<double>();
+			double* Q1 = Q0 + (size_t)ng * NQ * N;
+			double* Qr[2] = {Q0, Q1};
+			const uint8_t* mk_ = h.has_mask ? h.dmask.as<uint8_t>() : nullptr;
+			const double* wts = h.has_wts ? h.dwts.as<double>() : nullptr;
+			cx<R>* C = coef.as<cx<R>>();
+			cx<double>* Dg = diag.as<cx<double>>();
+
+			k_eps_plane<<<pgrid(N, ng), 256, 0, stream>>>(h.dir.as<double>(), h.fd, mk_, N, 0, gps, Qr[0]);
+			launches++;
+			if(h.s.beam_type != 2) {
+				k_init_fields<R><<<pgrid(N, nsl), 256, 0, stream>>>(Gm, slot0, gps, Qr[0], h.s.beam_type, h.s.waist,
+					h.s.dx, h.s.dy, Fp);
+			}
+			else {
+				size_t n = (size_t)nsl * 2 * N;
+				k_copy<R><<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, h.E0.as<cx<R>>() + (size_t)slot0 * 2 * N, Fp);
+			}
+			launches++;
+			CK(cudaGetLastError());
+			for(int iz = 0; iz < Nz - 1; iz++) {
+				double* QA = Qr[iz & 1];
+				double* QB = Qr[(iz + 1) & 1];
+				k_eps_plane<<<pgrid(N, ng), 256, 0, stream>>>(h.dir.as<double>(), h.fd, mk_, N, iz + 1, gps, QB);
+				k_coef<R><<<pgrid(N, ng), 128, 0, stream>>>(QA, QB, wts, iz, Gm, gps, C, Dg);
+				int lx = ng * 2 * Ny, ly = ng * 2 * Nx;
+				k_factor<R><<<(lx + 63) / 64, 64, 0, stream>>>(0, Gm, ng, Dg, facx.as<cx<R>>(), lscx.as<cx<double>>(),
+					scr.as<cx<double>>());
+				k_factor<R><<<(ly + 63) / 64, 64, 0, stream>>>(1, Gm, ng, Dg, facy.as<cx<R>>(), lscy.as<cx<double>>(),
+					scr.as<cx<double>>());
+				launches += 4;
+				CK(cudaGetLastError());
+				// shift -> phase -> ADI -> phase -> shift (BPMIteration.cpp:133-146)
+				rec_shift(h, slot0, nsl, Fp, T2b);
+				k_phase<R><<<pgrid(N, nsl), 256, 0, stream>>>(Gm, slot0, C, Fp);
+				launches++;
+				rec_adi(h, Gm, slot0, nsl, Nw, C, Fp, Tb, T2b);
+				k_phase<R><<<pgrid(N, nsl), 256, 0, stream>>>(Gm, slot0, C, Fp);
+				launches++;
+				rec_shift(h, slot0, nsl, Fp, T2b);
+				CK(cudaGetLastError());
+			}
+			k_fresnel_out<R><<<pgrid(N, nsl), 256, 0, stream>>>(Gm, slot0, gps, Qr[(Nz - 1) & 1], Fp);
+			launches++;
+			CK(cudaGetLastError());
+		}
+		// Screen filter over every plane of the sample (ScreenOutput.cpp:184-224).
+		int nplanes = h.slots * 2;
+		fft2(h, F, nplanes, -1);
+		k_screen_filter<R><<<pgrid(N, h.G * h.Nq), 128, 0, stream>>>(F, h.sp, 0, h.wl.as<double>(),
+			h.nout.as<double>(), h.qv.as<double>());
+		launches++;
+		CK(cudaGetLastError());
+		fft2(h, F, nplanes, +1);
+	}
+
+	void rec_shift(SampleHost& h, int slot0, int nsl, cx<R>* Fp, cx<R>* T2b) {
+		if(!h.any_shift) return;
+		const Geom Gm = h.geom;
+		k_shift_x<R><<<pgrid(Gm.N, nsl), 256, 0, stream>>>(Gm, slot0, h.shiftd.as<ShiftParams>(), Fp, T2b);
+		k_shift_y<R><<<pgrid(Gm.N, nsl), 256, 0, stream>>>(Gm, slot0, h.shiftd.as<ShiftParams>(), T2b, Fp);
+		launches += 2;
+	}
+
+	void rec_solve(int dirn, const Geom& Gm, int slot0, int nsl, const cx<R>* src, cx<R>* dst,
+			const cx<R>* acc_in, cx<R>* acc_out) {
+		int nlines = dirn == 0 ? Gm.Ny : Gm.Nx;
+		int nt = nsl * 2 * nlines;
+		if(dirn == 0)
+			k_solve<R, 0><<<(nt + 127) / 128, 128, 0, stream>>>(Gm, slot0, nsl, facx.as<cx<R>>(),
+				lscx.as<cx<double>>(), src, dst, acc_in, acc_out);
+		else
+			k_solve<R, 1><<<(nt + 127) / 128, 128, 0, stream>>>(Gm, slot0, nsl, facy.as<cx<R>>(),
+				lscy.as<cx<double>>(), src, dst, acc_in, acc_out);
+		launches++;
+	}
+
+	// ParaxialPrimaryEvolutionOperator::apply (ParaxialPrimaryEvolutionOperator.cpp:153-209).
+	void rec_adi(SampleHost& h, const Geom& Gm, int slot0, int nsl, int Nw, const cx<R>* C, cx<R>* Fp,
+			cx<R>* Tb, cx<R>* T2b) {
+		const int N = Gm.N;
+		dim3 gr = pgrid(N, nsl);
+		for(int dirn = 0; dirn < 2; dirn++) {
+			// explicit half-step in the other direction, then implicit solve + Woodbury
+			if(dirn == 0) k_stencil<R, ST_EXPL_Y><<<gr, 256, 0, stream>>>(Gm, slot0, C, Fp, T2b);
+			else k_stencil<R, ST_EXPL_X><<<gr, 256, 0, stream>>>(Gm, slot0, C, Fp, T2b);
+			launches++;
+			rec_solve(dirn, Gm, slot0, nsl, T2b, Tb, nullptr, nullptr);
+			cx<R>* cur = Tb;
+			cx<R>* oth = T2b;
+			if(Nw == 0) {
+				size_t n = (size_t)nsl * 2 * N;
+				k_copy<R><<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, Tb, Fp);
+				launches++;
+			}
+			for(int it = 1; it <= Nw; it++) {
+				if(dirn == 0) k_stencil<R, ST_WOOD_X><<<gr, 256, 0, stream>>>(Gm, slot0, C, cur, oth);
+				else k_stencil<R, ST_WOOD_Y><<<gr, 256, 0, stream>>>(Gm, slot0, C, cur, oth);
+				launches++;
+				rec_solve(dirn, Gm, slot0, nsl, oth, oth, it == 1 ? Tb : Fp, Fp);
+				std::swap(cur, oth);
+			}
+		}
+		(void)h;
+	}
+
+	void execute(nbpm_timing* tm) override {
+		CK(cudaSetDevice(opt.device));
+		if(opt.use_graph) {
+			if(!gexec) {
+				cudaGraph_t graph;
+				CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+				try { record(); }
+				catch(...) {
+					cudaStreamEndCapture(stream, &graph);
+					if(graph) cudaGraphDestroy(graph);
+					throw;
+				}
+				CK(cudaStreamEndCapture(stream, &graph));
+				CK(cudaGraphInstantiate(&gexec, graph, 0));
+				cudaGraphDestroy(graph);
+			}
+			CK(cudaEventRecord(ev[0], stream));
+			CK(cudaGraphLaunch(gexec, stream));
+			CK(cudaEventRecord(ev[1], stream));
+		}
+		else {
+			CK(cudaEventRecord(ev[0], stream));
+			record();
+			CK(cudaEventRecord(ev[1], stream));
+		}
+		CK(cudaStreamSynchronize(stream));
+		CK(cudaGetLastError());
+		float ms = 0;
+		CK(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+		last_slab_ms = 0;
+		if(tm) {
+			tm->compute_ms = ms;
+			tm->kernel_launches = launches;
+			long long vs = 0;
+			for(auto& hp : S) vs += (long long)hp->geom.N * (hp->geom.Nz - 1) * hp->slots;
+			tm->voxel_steps = vs;
+		}
+	}
+
+	long long device_bytes() const override { return dev_bytes; }
+	double slab_ms() const override { return last_slab_ms; }
+};
+
+}  // namespace nbpm
+
+using namespace nbpm;
+
+struct nbpm_plan {
+	std::unique_ptr<PlanBase> impl;
+};
+
+static int fail(int code, const std::string& msg) {
+	g_last_error = msg;
+	return code;
+}
+
+#define API_GUARD(...)                                                         \
+	try { __VA_ARGS__ }                                                                 \
+	catch(BackendError& e) { return fail(e.code, e.what()); }                    \
+	catch(std::bad_alloc&) { return fail(E_MEMORY, "host out of memory"); }      \
+	catch(std::exception& e) { return fail(E_INTERNAL, e.what()); }              \
+	catch(...) { return fail(E_INTERNAL, "unknown exception"); }
+
+extern "C" {
+
+void nbpm_default_options(nbpm_options* o) {
+	if(!o) return;
+	o->precision = NBPM_FP64;
+	o->groups_per_pass = 0;
+	o->use_graph = 1;
+	o->device = 0;
+	o->verbose = 0;
+}
+
+const char* nbpm_last_error(void) { return g_last_error.c_str(); }
+
+int nbpm_eval_index(const char* expr, double lambda, double* out) {
+	g_last_error.clear();
+	API_GUARD({
+		if(!expr || !out) return fail(E_ARG, "null argument");
+		*out = eval_index(expr, lambda, "expression");
+		return 0;
+	})
+}
+
+int nbpm_mask_weights(const char* json_str, const char* mask_formula, const double* mask_vals, int n_mask_vals,
+		unsigned char* mask_out, double* weights_out) {
+	g_last_error.clear();
+	API_GUARD({
+		if(!json_str || !mask_vals || !mask_out || !weights_out) return fail(E_ARG, "null argument");
+		BackendSettings s = parse_settings(json_str);
+		size_t nv = (size_t)s.Nx * s.Ny * s.Nz;
+		if((size_t)n_mask_vals != nv) return fail(E_SIZE, "Wrong dimension for the mask pointer array");
+		std::vector<unsigned char> m;
+		std::vector<double> w;
+		mask_weights(s, mask_vals, mask_formula ? mask_formula : "", m, w);
+		std::memcpy(mask_out, m.data(), m.size());
+		if(!w.empty()) std::memcpy(weights_out, w.data(), w.size() * sizeof(double));
+		return 0;
+	})
+}
+const char* nbpm_version(void) { return "nbpm 0.1.0 (sm_103a)"; }
+
+int nbpm_plan_create(int n_samples, const nbpm_sample* samples, const nbpm_options* opts, nbpm_plan** out) {
+	g_last_error.clear();
+	API_GUARD({
+		if(!out || n_samples <= 0 || !samples) return fail(E_ARG, "invalid plan arguments");
+		*out = nullptr;
+		nbpm_options o;
+		nbpm_default_options(&o);
+		if(opts) o = *opts;
+		if(o.precision != NBPM_FP64 && o.precision != NBPM_FP32) return fail(E_ARG, "unknown precision");
+		std::unique_ptr<nbpm_plan> p(new nbpm_plan());
+		if(o.precision == NBPM_FP64) {
+			auto* pl = new Plan<double>(o);
+			p->impl.reset(pl);
+			pl->setup(n_samples, samples);
+		}
+		else {
+			auto* pl = new Plan<float>(o);
+			p->impl.reset(pl);
+			pl->setup(n_samples, samples);
+		}
+		*out = p.release();
+		return 0;
+	})
+}
+
+int nbpm_plan_upload(nbpm_plan* p) {
+	API_GUARD({
+		if(!p) return fail(E_ARG, "null plan");
+		p->impl->upload();
+		return 0;
+	})
+}
+
+int nbpm_plan_execute(nbpm_plan* p, nbpm_timing* t) {
+	API_GUARD({
+		if(!p) return fail(E_ARG, "null plan");
+		p->impl->execute(t);
+		return 0;
+	})
+}
+
+int nbpm_plan_download(nbpm_plan* p) {
+	API_GUARD({
+		if(!p) return fail(E_ARG, "null plan");
+		p->impl->download();
+		return 0;
+	})
+}
+
+int nbpm_plan_slab_ms(nbpm_plan* p, double* ms) {
+	if(!p || !ms) return fail(E_ARG, "null argument");
+	*ms = p->impl->slab_ms();
+	return 0;
+}
+
+long long nbpm_plan_device_bytes(const nbpm_plan* p) { return p ? p->impl->device_bytes() : 0; }
+
+int nbpm_plan_destroy(nbpm_plan* p) {
+	delete p;
+	return 0;
+}
+
+int nbpm_run_batch(int n_samples, const nbpm_sample* samples, const nbpm_options* opts, nbpm_timing* timing) {
+	g_last_error.clear();
+	nbpm_plan* p = nullptr;
+	int rc = nbpm_plan_create(n_samples, samples, opts, &p);
+	if(rc) return rc;
+	std::unique_ptr<nbpm_plan> guard(p);
+	API_GUARD({
+		auto t0 = std::chrono::steady_clock::now();
+		p->impl->upload();
+		auto t1 = std::chrono::steady_clock::now();
+		nbpm_timing tm{};
+		p->impl->execute(&tm);
+		auto t2 = std::chrono::steady_clock::now();
+		p->impl->download();
+		auto t3 = std::chrono::steady_clock::now();
+		if(timing) {
+			*timing = tm;
+			timing->upload_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+			timing->download_ms = std::chrono::duration<double, std::milli>(t3 - t2).count();
+			timing->total_ms = std::chrono::duration<double, std::milli>(t3 - t0).count();
+		}
+		return 0;
+	})
+}
+
+int nbpm_run_backend_ex(const char* json_str, const char* mask_formula, const double* lc_field_vals,
+		int n_lc_vals, const double* mask_vals, int n_mask_vals, double* E_field_vals, int n_E_vals,
+		const nbpm_options* opts, nbpm_timing* timing) {
+	nbpm_sample s;
+	s.json_str = json_str;
+	s.mask_formula = mask_formula;
+	s.lc_field_vals = lc_field_vals;
+	s.n_lc_vals = n_lc_vals;
+	s.mask_vals = mask_vals;
+	s.n_mask_vals = n_mask_vals;
+	s.E_field_vals = E_field_vals;
+	s.n_E_vals = n_E_vals;
+	return nbpm_run_batch(1, &s, opts, timing);
+}
+
+int nbpm_run_backend_without_mask(const char* json_str, const double* lc_field_vals, int n_lc_vals,
+		double* E_field_vals, int n_E_vals) {
+	return nbpm_run_backend_ex(json_str, nullptr, lc_field_vals, n_lc_vals, nullptr, 0, E_field_vals, n_E_vals,
+		nullptr, nullptr);
+}
+
+int nbpm_run_backend_with_mask(const char* json_str, const char* mask_formula, const double* lc_field_vals,
+		int n_lc_vals, const double* mask_vals, int n_mask_vals, double* E_field_vals, int n_E_vals) {
+	return nbpm_run_backend_ex(json_str, mask_formula ? mask_formula : "", lc_field_vals, n_lc_vals,
+		mask_vals, n_mask_vals, E_field_vals, n_E_vals, nullptr, nullptr);
+}
+
+}  // extern "C"
