@@ -1,0 +1,391 @@
+"""Benchmark of the GB300 bpm backend (one JSON line on stdout).
+
+Metric: voxel-steps/s (one transverse point advanced one z-slab for one (wavelength,
+wave vector, polarisation) propagation). A "step" is one full run of the workload: every
+slab of every propagation plus the screen filter, with inputs resident in HBM (``value``).
+``e2e`` is the same metric through the reference-facing C ABI call
+(nbpm_run_backend_ex) with pinned host buffers: director upload, the run and the
+complex128 field download inside the timed region.
+
+Default workload: batched Koehler micrograph, 256x256x64 mesh, 16 wavelengths x 13 wave
+vectors x 2 polarisations = 416 propagations, FP32 batched mode. The FP64 plain mode (one
+wavelength per launch) is measured on the same workload beside it, and the FP32 result's
+relative L2 error against the FP64 result is reported.
+
+--impl reference times the CPU oracle (FP64 C++/OpenMP restatement of the reference; the
+reference itself cannot be built here) on a bounded sample of the same workload.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+MEASURED = os.path.join(HERE, "MEASURED_PEAKS.json")
+
+
+def peaks():
+    try:
+        with open(MEASURED) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            if len(r) >= 9:
+                for k, n in enumerate(names):
+                    if r[5 + k].lower().startswith("active"):
+                        reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def workload(name):
+    from nemaktis_gb300 import workloads as W
+    if name == "config3":
+        c = W.config3()
+        c["desc"] = "batched Koehler micrograph 256x256x64 d=0.25um, 16 wavelengths x 13 q x 2 pol (416 propagations)"
+        c["Nz"] = 64
+        return [c]
+    if name == "config1":
+        c = W.config1()
+        c["desc"] = "twisted nematic 64x64x40 d=0.25um, 1 wavelength x 1 q x 2 pol"
+        c["Nz"] = 40
+        return [c]
+    if name == "config2":
+        c = W.config2()
+        c["desc"] = "cholesteric droplet 512x512x128 d=0.2um (mask + formula), 1 wavelength x 1 q x 2 pol"
+        c["Nz"] = 128
+        return [c]
+    if name == "config4":
+        out = []
+        for i in range(4):
+            c = W.config4_sample(i)
+            c["Nz"] = W.CONFIG4_MESHES[i][2]
+            out.append(c)
+        out[0]["desc"] = "4 uneven samples 1024^2x200, 768^2x160, 512^2x96, 256^2x48 d=0.2um, 4 wl x 7 q x 2 pol"
+        return out
+    raise SystemExit("unknown workload " + name)
+
+
+def voxel_steps(samples):
+    from nemaktis_gb300 import workloads as W
+    return sum(W.voxel_steps(c["shape"], c["Nz"]) for c in samples)
+
+
+def pinned(shape, dtype):
+    import torch
+    n = int(np.prod(shape)) * np.dtype(dtype).itemsize
+    t = torch.empty(n, dtype=torch.uint8, pin_memory=True)
+    a = t.numpy().view(dtype).reshape(shape)
+    return a, t
+
+
+def run_ours(args):
+    import torch
+    from nemaktis_gb300 import _lib, api
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    lib = _lib.load()
+    samples = workload(args.workload)
+    vs = voxel_steps(samples)
+    prec = "fp32" if args.precision == "fp32" else "fp64"
+
+    # Device-resident plan for the timed value.
+    bufs = []
+    for c in samples:
+        E = np.zeros(c["shape"], np.complex128)
+        bufs.append({"json": c["json"], "lc": c["lc"], "E": E, "mask": c.get("mask"), "formula": c.get("formula")})
+    plan = api.Plan(bufs, precision=prec, groups_per_pass=0)
+    plan.upload()
+    for _ in range(args.warmup):
+        plan.execute()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    clk = Clocks(local)
+    clk.start()
+    t0 = time.perf_counter()
+    ms = []
+    launches = 0
+    for _ in range(args.steps):
+        t = plan.execute()
+        ms.append(t["compute_ms"])
+        launches += t["kernel_launches"]
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clocks = clk.stop()
+    dev_ms = float(np.sum(ms))
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([dev_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        dev_ms = float(tt.item())
+    value = vs * args.steps * world / (dev_ms / 1e3)
+    plan.download()
+    out32 = [b["E"].copy() for b in bufs]
+    prof = profile_kernels(plan, lib)
+    plan.close()
+
+    # FP64 plain path on the same workload (one wavelength per launch), one step.
+    fp64 = None
+    if not args.skip_fp64:
+        b64 = []
+        for c in samples:
+            b64.append({"json": c["json"], "lc": c["lc"], "E": np.zeros(c["shape"], np.complex128),
+                        "mask": c.get("mask"), "formula": c.get("formula")})
+        p64 = api.Plan(b64, precision="fp64", groups_per_pass=1)
+        p64.upload()
+        p64.execute()
+        t64 = p64.execute()
+        p64.download()
+        p64.close()
+        err = float(np.sqrt(sum(np.linalg.norm(a - b["E"]) ** 2 for a, b in zip(out32, b64)) /
+                            sum(np.linalg.norm(b["E"]) ** 2 for b in b64)))
+        fp64 = {"value": vs / (t64["compute_ms"] / 1e3), "unit": "voxel-steps/s", "ms_per_step": t64["compute_ms"],
+                "mode": "FP64, one wavelength per launch", "fp32_rel_l2_vs_fp64": err,
+                "speedup_fp32_batched": value / world / (vs / (t64["compute_ms"] / 1e3))}
+
+    # End-to-end through the C ABI with pinned host buffers.
+    e2e = e2e_measure(samples, prec, args.e2e_steps)
+
+    hbm, src = peaks()
+    roof = None
+    if prof:
+        top = max(prof, key=lambda k: prof[k]["ms"])
+        r = prof[top]
+        ach = r["bytes"] / (r["ms"] / r["launches"] / 1e3) / 1e9 / r["launches"] if r["launches"] else 0
+        roof = {"bound": "hbm", "kernel": top, "achieved": ach, "peak": hbm, "unit": "GB/s",
+                "frac": ach / hbm, "peak_source": src, "traffic": None,
+                "share_of_step": r["ms"] / sum(v["ms"] for v in prof.values()),
+                "algorithmic_bytes_per_launch": r["bytes"] / max(1, r["launches"])}
+    cpu = None
+    if rank == 0 and not args.skip_cpu:
+        cpu = cpu_baseline(samples, args.cpu_seconds)
+    line = {
+        "metric": "voxel-steps/s FP32-batched vs FP64 plain, 1 GB300, <=1e-4 rel err; p50/p99 latency",
+        "value": value, "unit": "voxel-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak" if world > 1 else "weak",
+        "vs_baseline": None, "dtype": "complex-f32 (f64 phase argument, Sherman-Morrison scalar, coefficients)"
+        if prec == "fp32" else "complex-f64",
+        "data": "synthetic (seeded director fields, no dataset)",
+        "config": {"workload": samples[0]["desc"], "precision": prec, "voxel_steps_per_step": vs,
+                   "l2": "inputs larger than L2 (field planes %.0f MB per step)" %
+                         (sum(np.prod(c["shape"]) for c in samples) * (8 if prec == "fp32" else 16) / 1e6),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "clocks": clocks, "gpu_launches": launches, "wall_s": wall,
+        "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "fp64_plain": fp64,
+        "kernel_profile": {k: {"ms_per_step": v["ms"], "launches_per_step": v["launches"]} for k, v in (prof or {}).items()},
+    }
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def profile_kernels(plan, lib):
+    """Per-kernel event timing of one eager execution (nbpm_plan_profile), if available."""
+    try:
+        f = lib.nbpm_plan_profile
+    except AttributeError:
+        return None
+    n = 32
+    names = (ctypes.c_char * 48 * n)()
+    ms = (ctypes.c_double * n)()
+    cnt = (ctypes.c_int * n)()
+    by = (ctypes.c_double * n)()
+    k = ctypes.c_int(n)
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                  ctypes.POINTER(ctypes.c_int)]
+    rc = f(plan._h, names, ms, cnt, by, ctypes.byref(k))
+    if rc != 0:
+        return None
+    out = {}
+    for i in range(k.value):
+        nm = bytes(names[i]).split(b"\0")[0].decode()
+        out[nm] = {"ms": ms[i], "launches": cnt[i], "bytes": by[i]}
+    return out
+
+
+def e2e_measure(samples, prec, steps):
+    from nemaktis_gb300 import _lib
+    lib = _lib.load()
+    keep = []
+    arr = (_lib.Sample * len(samples))()
+    h2d = d2h = 0
+    for i, c in enumerate(samples):
+        lc, t1 = pinned(c["lc"].shape, np.float64)
+        lc[...] = c["lc"]
+        E, t2 = pinned(c["shape"], np.complex128)
+        E[...] = 0
+        mask = None
+        if c.get("mask") is not None:
+            mask, t3 = pinned(c["mask"].shape, np.float64)
+            mask[...] = c["mask"]
+            keep.append(t3)
+            h2d += mask.nbytes
+        js = c["json"].encode()
+        fm = c.get("formula")
+        fm = None if fm is None else fm.encode()
+        keep += [lc, E, mask, t1, t2, js, fm]
+        arr[i] = _lib.Sample(js, fm, lc.ctypes.data, lc.size, None if mask is None else mask.ctypes.data,
+                             0 if mask is None else mask.size, E.ctypes.data, E.size)
+        h2d += lc.nbytes
+        d2h += E.nbytes
+    o = _lib.options(precision=_lib.FP32 if prec == "fp32" else _lib.FP64)
+    t = _lib.Timing()
+    _lib.check(lib.nbpm_run_batch(len(samples), arr, ctypes.byref(o), ctypes.byref(t)))  # warm-up
+    walls = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        _lib.check(lib.nbpm_run_batch(len(samples), arr, ctypes.byref(o), ctypes.byref(t)))
+        walls.append(time.perf_counter() - t0)
+    vs = voxel_steps(samples)
+    w = float(np.median(walls))
+    return {"value": vs / w, "unit": "voxel-steps/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "ms_per_step": w * 1e3, "api": "nbpm_run_batch (C ABI, pinned host buffers)",
+            "breakdown_ms": {"upload": t.upload_ms, "compute": t.compute_ms, "download": t.download_ms,
+                             "total": t.total_ms}}
+
+
+def cpu_baseline(samples, seconds):
+    """Oracle (FP64 C++/OpenMP) on a bounded sample: the first wavelength and the first
+    wave vector of the first sample (2 polarisations), every slab, plus its screen filter."""
+    import json as _json
+    import oracle
+    c = samples[0]
+    j = _json.loads(c["json"])
+    co = j["Physics settings"]["Coefficients"]
+    co["Wavelengths"] = co["Wavelengths"][:1]
+    co["Wavevectors"] = co["Wavevectors"][:2]
+    js = _json.dumps(j)
+    Nl, Nq, _, Ny, Nx = c["shape"]
+    shape = (1, 1, 4, Ny, Nx)
+    vs = Nx * Ny * (c["Nz"] - 1) * 2
+    runs, t0 = 0, time.perf_counter()
+    while True:
+        E = np.zeros(shape, np.complex128)
+        if c.get("mask") is not None:
+            oracle.run_backend_with_mask(js, c.get("formula") or "", c["lc"], c["mask"], E)
+        else:
+            oracle.run_backend_without_mask(js, c["lc"], E)
+        runs += 1
+        el = time.perf_counter() - t0
+        if el > seconds or runs >= 50:
+            break
+    return {"value": vs * runs / el, "unit": "voxel-steps/s", "cores": oracle.num_threads(), "kind": "port",
+            "sample": "1 wavelength x 1 q x 2 pol of the workload's first sample, all %d slabs, %d run(s), %.1f s"
+                      % (c["Nz"] - 1, runs, el)}
+
+
+def run_reference(args):
+    world, rank, local = dist_env()
+    if rank != 0:
+        return
+    samples = workload(args.workload)
+    ms = []
+    cpu = None
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(samples, args.cpu_seconds / max(1, args.steps))
+        if i >= args.warmup:
+            ms.append(r)
+            cpu = r
+    v = float(np.median([r["value"] for r in ms]))
+    line = {"impl": "reference", "metric": "voxel-steps/s FP32-batched vs FP64 plain, 1 GB300, <=1e-4 rel err; p50/p99 latency",
+            "value": v, "unit": "voxel-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "complex-f64",
+            "data": "synthetic (seeded director fields, no dataset)",
+            "config": {"workload": samples[0]["desc"], "precision": "fp64 CPU oracle (reference not buildable here)"},
+            "cpu_baseline": {"value": v, "unit": "voxel-steps/s", "cores": cpu["cores"], "kind": "port",
+                             "sample": cpu["sample"]},
+            "e2e": {"value": v, "unit": "voxel-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="config3", choices=["config1", "config2", "config3", "config4"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-fp64", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -101,6 +101,11 @@ int nbpm_plan_download(nbpm_plan* plan);
 int nbpm_plan_slab_ms(nbpm_plan* plan, double* ms);
 int nbpm_plan_destroy(nbpm_plan* plan);
 
+/* Runs the plan once without a graph, timing every kernel launch with CUDA events on the
+ * plan's stream. Fills up to *n entries (kernel name, total ms, launches, algorithmic bytes
+ * moved by those launches) and sets *n to the number of entries written. */
+int nbpm_plan_profile(nbpm_plan* plan, char (*names)[48], double* ms, int* launches, double* bytes, int* n);
+
 /* Device memory the plan holds, bytes. */
 long long nbpm_plan_device_bytes(const nbpm_plan* plan);
 

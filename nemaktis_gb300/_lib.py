@@ -52,6 +52,7 @@ EXPORTS = {
     "nbpm_plan_slab_ms": (c_int, [c_void_p, ctypes.POINTER(c_double)]),
     "nbpm_plan_destroy": (c_int, [c_void_p]),
     "nbpm_plan_device_bytes": (c_ll, [c_void_p]),
+    "nbpm_plan_profile": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, ctypes.POINTER(c_int)]),
     "nbpm_eval_index": (c_int, [c_char_p, c_double, ctypes.POINTER(c_double)]),
     "nbpm_mask_weights": (c_int, [c_char_p, c_char_p, c_void_p, c_int, c_void_p, c_void_p]),
     "nbpm_last_error": (c_char_p, []),

@@ -635,6 +635,36 @@ __global__ void k_shift_y(Geom G, int slot0, const ShiftParams* __restrict__ sp,
 	}
 }
 
+// For q = 0 the shift operator reduces to its periodic wrap: the x pass copies column 0 onto
+// the duplicate column Nx-1, then the y pass copies row 0 onto row Ny-1 (the interpolation
+// weights are exactly 0/1/0/0 and the phase factor is exactly 1). This kernel writes those
+// border values directly; one thread per border point of a (slot, comp) plane.
+template <typename R>
+__global__ void k_sync_dup(Geom G, int slot0, const ShiftParams* __restrict__ sp, cx<R>* F) {
+	int Nx = G.Nx, Ny = G.Ny, N = G.N;
+	int t = blockIdx.x * blockDim.x + threadIdx.x;
+	int nb = (Ny - 1) + (Nx - 1) + 1;
+	if(t >= nb) return;
+	int s = blockIdx.y;
+	int gs = slot0 + s;
+	int gq = (gs / G.spg) * G.Nq + (gs / 2) % G.Nq;
+	if(sp[gq].active) return;
+	bool ax = Nx > 3, ay = Ny > 3;
+	int dst, src = -1;
+	if(t < Ny - 1) { dst = (Nx - 1) + Nx * t; if(ax) src = Nx * t; }
+	else if(t < Ny - 1 + Nx - 1) { int ix = t - (Ny - 1); dst = ix + Nx * (Ny - 1); if(ay) src = ix; }
+	else {
+		dst = (Nx - 1) + Nx * (Ny - 1);
+		if(ax && ay) src = 0;
+		else if(ay) src = Nx - 1;
+		else if(ax) src = Nx * (Ny - 1);
+	}
+	if(src < 0 || src == dst) return;
+	cx<R>* f = F + (size_t)s * 2 * N;
+	f[dst] = f[src];
+	f[N + dst] = f[N + src];
+}
+
 // Entrance field: beam profile with polarisation angle pi/2*pol (BPMIteration.cpp:87-109,
 // BeamProfile.cpp:17-39) followed by the input Fresnel operator (FresnelOperator.cpp:16-38)
 // built on sqrt(eps_tr) at iz = 0.

@@ -69,7 +69,7 @@ struct SampleHost {
 	size_t nvox = 0;
 	std::vector<GroupParams> gps;
 	std::vector<ShiftParams> shifts;
-	bool any_shift = false;
+	bool any_shift = false, any_zero_q = false;
 	ScreenParams sp;
 	// device
 	DevBuf dir, dmask, dwts, F, E0, gpsd, shiftd, partial, wl, nout, qv;
@@ -143,6 +143,8 @@ struct PlanBase {
 	virtual void download() = 0;
 	virtual long long device_bytes() const = 0;
 	virtual double slab_ms() const = 0;
+	virtual void profile(std::vector<std::string>& names, std::vector<double>& ms, std::vector<int>& cnt,
+		std::vector<double>& bytes) = 0;
 };
 
 template <typename R>
@@ -159,6 +161,33 @@ struct Plan : PlanBase {
 	std::vector<std::pair<int, cx<R>*>> tw_tables;
 	int launches = 0;
 	long long dev_bytes = 0;
+	// Live per-kernel timing (nbpm_plan_profile): events around every launch of an eager run.
+	struct ProfRec { const char* name; double bytes; cudaEvent_t a, b; };
+	bool profiling = false;
+	std::vector<ProfRec> prof;
+	std::vector<cudaEvent_t> evpool;
+	size_t evnext = 0;
+	cudaEvent_t pool_event() {
+		if(evnext == evpool.size()) {
+			cudaEvent_t e;
+			CK(cudaEventCreate(&e));
+			evpool.push_back(e);
+		}
+		return evpool[evnext++];
+	}
+	template <typename F>
+	void launch(const char* name, double bytes, F&& fn) {
+		if(profiling) {
+			ProfRec r{name, bytes, pool_event(), pool_event()};
+			CK(cudaEventRecord(r.a, stream));
+			fn();
+			CK(cudaEventRecord(r.b, stream));
+			prof.push_back(r);
+		}
+		else fn();
+		CK(cudaGetLastError());
+		launches++;
+	}
 	double last_slab_ms = 0;
 	size_t smem_limit = 0;
 
@@ -166,6 +195,7 @@ struct Plan : PlanBase {
 		for(auto& e : ev) e = nullptr;
 	}
 	~Plan() override {
+		for(auto e : evpool) cudaEventDestroy(e);
 		if(gexec) cudaGraphExecDestroy(gexec);
 		for(auto& e : ev) if(e) cudaEventDestroy(e);
 		if(stream) cudaStreamDestroy(stream);
@@ -241,7 +271,10 @@ struct Plan : PlanBase {
 				gp.nref = 0;
 				h->gps.push_back(gp);
 			}
-			for(auto& q : s.q) if(!(q.first == 0 && q.second == 0)) h->any_shift = true;
+			for(auto& q : s.q) {
+				if(!(q.first == 0 && q.second == 0)) h->any_shift = true;
+				else h->any_zero_q = true;
+			}
 			ScreenParams& sp = h->sp;
 			sp.Nx = s.Nx; sp.Ny = s.Ny; sp.Nq = h->Nq; sp.n_iso = (int)s.iso_thick.size();
 			sp.dx = s.dx; sp.dy = s.dy; sp.NA = s.NA;
@@ -360,7 +393,7 @@ struct Plan : PlanBase {
 	}
 
 	// ---- launch helpers (count launches while recording) ----
-	dim3 pgrid(int N, int ny) { return dim3((unsigned)((N + 255) / 256), (unsigned)ny); }
+	dim3 pgrid(int N, int ny, int threads = 256) { return dim3((unsigned)((N + threads - 1) / threads), (unsigned)ny); }
 
 	void fft2(SampleHost& h, cx<R>* F, int nplanes, int sign) {
 		int Nx = h.s.Nx, Ny = h.s.Ny;
@@ -385,9 +418,11 @@ struct Plan : PlanBase {
 			else { nlines = nplanes * Nx; lpp = Nx; ls = 1; es = Nx; }
 			int blocks = (nlines + lpb - 1) / lpb;
 			int threads = std::min(256, std::max(32, ((lpb * n / 2) + 31) / 32 * 32));
-			k_fft_lines<R><<<blocks, threads, smem, stream>>>(F, P, nlines, lpp, ps, ls, es, lpb, twiddles(n), sign);
-			CK(cudaGetLastError());
-			launches++;
+			cx<R>* tw = twiddles(n);
+			double bytes = 2.0 * sizeof(cx<R>) * (double)nplanes * Nx * Ny;
+			launch(pass == 0 ? "fft_rows" : "fft_cols", bytes, [&] {
+				k_fft_lines<R><<<blocks, threads, smem, stream>>>(F, P, nlines, lpp, ps, ls, es, lpb, tw, sign);
+			});
 		}
 	}
 
@@ -400,17 +435,25 @@ struct Plan : PlanBase {
 		const Geom Gm = h.geom;
 		const int N = Gm.N, Nx = Gm.Nx, Ny = Gm.Ny, Nz = Gm.Nz;
 		const int Nw = h.s.n_woodbury;
+		const double sc = sizeof(cx<R>);
 		cx<R>* F = h.F.as<cx<R>>();
+		const uint8_t* mk_ = h.has_mask ? h.dmask.as<uint8_t>() : nullptr;
+		const double* wts = h.has_wts ? h.dwts.as<double>() : nullptr;
 		// nref for every group, then shift parameters (device side)
 		{
 			int nb = (int)std::min<size_t>(1024, (h.nvox + 255) / 256);
-			k_neff_partial<<<dim3(nb, h.G), 256, 0, stream>>>(h.dir.as<double>(), h.fd,
-				h.has_mask ? h.dmask.as<uint8_t>() : nullptr, h.nvox, h.gpsd.as<GroupParams>(), h.partial.as<double>());
-			k_nref_final<<<(h.G + 63) / 64, 64, 0, stream>>>(h.G, nb, h.nvox, h.partial.as<double>(), h.gpsd.as<GroupParams>());
-			k_shift_params<<<(h.G * h.Nq + 63) / 64, 64, 0, stream>>>(h.G, h.Nq, Nx, Ny, h.gpsd.as<GroupParams>(),
-				h.qv.as<double>(), h.shiftd.as<ShiftParams>());
-			CK(cudaGetLastError());
-			launches += 3;
+			launch("neff_partial", (double)h.nvox * h.fd * 8 * h.G, [&] {
+				k_neff_partial<<<dim3(nb, h.G), 256, 0, stream>>>(h.dir.as<double>(), h.fd, mk_, h.nvox,
+					h.gpsd.as<GroupParams>(), h.partial.as<double>());
+			});
+			launch("nref_final", 8.0 * nb * h.G, [&] {
+				k_nref_final<<<(h.G + 63) / 64, 64, 0, stream>>>(h.G, nb, h.nvox, h.partial.as<double>(),
+					h.gpsd.as<GroupParams>());
+			});
+			launch("shift_params", sizeof(ShiftParams) * h.G * h.Nq, [&] {
+				k_shift_params<<<(h.G * h.Nq + 63) / 64, 64, 0, stream>>>(h.G, h.Nq, Nx, Ny, h.gpsd.as<GroupParams>(),
+					h.qv.as<double>(), h.shiftd.as<ShiftParams>());
+			});
 		}
 		int ngp = gpp(h);
 		for(int ga = 0; ga < h.G; ga += ngp) {
@@ -423,107 +466,173 @@ struct Plan : PlanBase {
 			double* Q0 = Qring.as<double>();
 			double* Q1 = Q0 + (size_t)ng * NQ * N;
 			double* Qr[2] = {Q0, Q1};
-			const uint8_t* mk_ = h.has_mask ? h.dmask.as<uint8_t>() : nullptr;
-			const double* wts = h.has_wts ? h.dwts.as<double>() : nullptr;
 			cx<R>* C = coef.as<cx<R>>();
 			cx<double>* Dg = diag.as<cx<double>>();
+			const double eps_bytes = (double)N * ng * (h.fd * 8 + (mk_ ? 1 : 0) + NQ * 8);
+			const double field_pts = (double)N * nsl;
 
-			k_eps_plane<<<pgrid(N, ng), 256, 0, stream>>>(h.dir.as<double>(), h.fd, mk_, N, 0, gps, Qr[0]);
-			launches++;
+			launch("eps_plane", eps_bytes, [&] {
+				k_eps_plane<<<pgrid(N, ng), 256, 0, stream>>>(h.dir.as<double>(), h.fd, mk_, N, 0, gps, Qr[0]);
+			});
 			if(h.s.beam_type != 2) {
-				k_init_fields<R><<<pgrid(N, nsl), 256, 0, stream>>>(Gm, slot0, gps, Qr[0], h.s.beam_type, h.s.waist,
-					h.s.dx, h.s.dy, Fp);
+				launch("init_fields", field_pts * 2 * sc + (double)N * ng * 3 * 8, [&] {
+					k_init_fields<R><<<pgrid(N, nsl), 256, 0, stream>>>(Gm, slot0, gps, Qr[0], h.s.beam_type,
+						h.s.waist, h.s.dx, h.s.dy, Fp);
+				});
 			}
 			else {
 				size_t n = (size_t)nsl * 2 * N;
-				k_copy<R><<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, h.E0.as<cx<R>>() + (size_t)slot0 * 2 * N, Fp);
+				launch("copy_fields", 2.0 * n * sc, [&] {
+					k_copy<R><<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, h.E0.as<cx<R>>() + (size_t)slot0 * 2 * N, Fp);
+				});
 			}
-			launches++;
-			CK(cudaGetLastError());
 			for(int iz = 0; iz < Nz - 1; iz++) {
 				double* QA = Qr[iz & 1];
 				double* QB = Qr[(iz + 1) & 1];
-				k_eps_plane<<<pgrid(N, ng), 256, 0, stream>>>(h.dir.as<double>(), h.fd, mk_, N, iz + 1, gps, QB);
-				k_coef<R><<<pgrid(N, ng), 128, 0, stream>>>(QA, QB, wts, iz, Gm, gps, C, Dg);
+				launch("eps_plane", eps_bytes, [&] {
+					k_eps_plane<<<pgrid(N, ng), 256, 0, stream>>>(h.dir.as<double>(), h.fd, mk_, N, iz + 1, gps, QB);
+				});
+				launch("coef", (double)N * ng * (2 * NQ * 8 + NCOEF * sc + NDIAG * 16 + (wts ? 16 : 0)), [&] {
+					k_coef<R><<<pgrid(N, ng, 128), 128, 0, stream>>>(QA, QB, wts, iz, Gm, gps, C, Dg);
+				});
 				int lx = ng * 2 * Ny, ly = ng * 2 * Nx;
-				k_factor<R><<<(lx + 63) / 64, 64, 0, stream>>>(0, Gm, ng, Dg, facx.as<cx<R>>(), lscx.as<cx<double>>(),
-					scr.as<cx<double>>());
-				k_factor<R><<<(ly + 63) / 64, 64, 0, stream>>>(1, Gm, ng, Dg, facy.as<cx<R>>(), lscy.as<cx<double>>(),
-					scr.as<cx<double>>());
-				launches += 4;
-				CK(cudaGetLastError());
+				const double fb = (double)N * ng * 2 * (3 * 16 + NFAC * sc + 4 * 16);
+				launch("factor_x", fb, [&] {
+					k_factor<R><<<(lx + 63) / 64, 64, 0, stream>>>(0, Gm, ng, Dg, facx.as<cx<R>>(),
+						lscx.as<cx<double>>(), scr.as<cx<double>>());
+				});
+				launch("factor_y", fb, [&] {
+					k_factor<R><<<(ly + 63) / 64, 64, 0, stream>>>(1, Gm, ng, Dg, facy.as<cx<R>>(),
+						lscy.as<cx<double>>(), scr.as<cx<double>>());
+				});
 				// shift -> phase -> ADI -> phase -> shift (BPMIteration.cpp:133-146)
 				rec_shift(h, slot0, nsl, Fp, T2b);
-				k_phase<R><<<pgrid(N, nsl), 256, 0, stream>>>(Gm, slot0, C, Fp);
-				launches++;
-				rec_adi(h, Gm, slot0, nsl, Nw, C, Fp, Tb, T2b);
-				k_phase<R><<<pgrid(N, nsl), 256, 0, stream>>>(Gm, slot0, C, Fp);
-				launches++;
+				launch("phase", field_pts * 4 * sc + (double)N * ng * 3 * sc, [&] {
+					k_phase<R><<<pgrid(N, nsl), 256, 0, stream>>>(Gm, slot0, C, Fp);
+				});
+				rec_adi(h, Gm, slot0, nsl, ng, Nw, C, Fp, Tb, T2b);
+				launch("phase", field_pts * 4 * sc + (double)N * ng * 3 * sc, [&] {
+					k_phase<R><<<pgrid(N, nsl), 256, 0, stream>>>(Gm, slot0, C, Fp);
+				});
 				rec_shift(h, slot0, nsl, Fp, T2b);
-				CK(cudaGetLastError());
 			}
-			k_fresnel_out<R><<<pgrid(N, nsl), 256, 0, stream>>>(Gm, slot0, gps, Qr[(Nz - 1) & 1], Fp);
-			launches++;
-			CK(cudaGetLastError());
+			launch("fresnel_out", field_pts * 4 * sc + (double)N * ng * 3 * 8, [&] {
+				k_fresnel_out<R><<<pgrid(N, nsl), 256, 0, stream>>>(Gm, slot0, gps, Qr[(Nz - 1) & 1], Fp);
+			});
 		}
 		// Screen filter over every plane of the sample (ScreenOutput.cpp:184-224).
 		int nplanes = h.slots * 2;
 		fft2(h, F, nplanes, -1);
-		k_screen_filter<R><<<pgrid(N, h.G * h.Nq), 128, 0, stream>>>(F, h.sp, 0, h.wl.as<double>(),
-			h.nout.as<double>(), h.qv.as<double>());
-		launches++;
-		CK(cudaGetLastError());
+		launch("screen_filter", (double)N * h.slots * 4 * sc, [&] {
+			k_screen_filter<R><<<pgrid(N, h.G * h.Nq, 128), 128, 0, stream>>>(F, h.sp, 0, h.wl.as<double>(),
+				h.nout.as<double>(), h.qv.as<double>());
+		});
 		fft2(h, F, nplanes, +1);
 	}
 
+	// SimpleShiftOperator::apply for every slot: interpolation kernels for tilted slots, the
+	// duplicate-border copy for q = 0 slots.
 	void rec_shift(SampleHost& h, int slot0, int nsl, cx<R>* Fp, cx<R>* T2b) {
-		if(!h.any_shift) return;
 		const Geom Gm = h.geom;
-		k_shift_x<R><<<pgrid(Gm.N, nsl), 256, 0, stream>>>(Gm, slot0, h.shiftd.as<ShiftParams>(), Fp, T2b);
-		k_shift_y<R><<<pgrid(Gm.N, nsl), 256, 0, stream>>>(Gm, slot0, h.shiftd.as<ShiftParams>(), T2b, Fp);
-		launches += 2;
+		const double sc = sizeof(cx<R>);
+		if(h.any_shift) {
+			launch("shift_x", (double)Gm.N * nsl * 4 * sc, [&] {
+				k_shift_x<R><<<pgrid(Gm.N, nsl), 256, 0, stream>>>(Gm, slot0, h.shiftd.as<ShiftParams>(), Fp, T2b);
+			});
+			launch("shift_y", (double)Gm.N * nsl * 4 * sc, [&] {
+				k_shift_y<R><<<pgrid(Gm.N, nsl), 256, 0, stream>>>(Gm, slot0, h.shiftd.as<ShiftParams>(), T2b, Fp);
+			});
+		}
+		if(h.any_zero_q) {
+			int nb = Gm.Nx + Gm.Ny - 1;
+			launch("sync_dup", (double)nb * nsl * 4 * sc, [&] {
+				k_sync_dup<R><<<dim3((unsigned)((nb + 127) / 128), (unsigned)nsl), 128, 0, stream>>>(Gm, slot0,
+					h.shiftd.as<ShiftParams>(), Fp);
+			});
+		}
 	}
 
-	void rec_solve(int dirn, const Geom& Gm, int slot0, int nsl, const cx<R>* src, cx<R>* dst,
+	void rec_solve(int dirn, const Geom& Gm, int slot0, int nsl, int ng, const cx<R>* src, cx<R>* dst,
 			const cx<R>* acc_in, cx<R>* acc_out) {
 		int nlines = dirn == 0 ? Gm.Ny : Gm.Nx;
 		int nt = nsl * 2 * nlines;
+		const double sc = sizeof(cx<R>);
+		double bytes = (double)Gm.N * nsl * 2 * sc * (acc_out ? 4 : 2) + (double)Gm.N * ng * 2 * NFAC * sc;
 		if(dirn == 0)
-			k_solve<R, 0><<<(nt + 127) / 128, 128, 0, stream>>>(Gm, slot0, nsl, facx.as<cx<R>>(),
-				lscx.as<cx<double>>(), src, dst, acc_in, acc_out);
+			launch("solve_x", bytes, [&] {
+				k_solve<R, 0><<<(nt + 127) / 128, 128, 0, stream>>>(Gm, slot0, nsl, facx.as<cx<R>>(),
+					lscx.as<cx<double>>(), src, dst, acc_in, acc_out);
+			});
 		else
-			k_solve<R, 1><<<(nt + 127) / 128, 128, 0, stream>>>(Gm, slot0, nsl, facy.as<cx<R>>(),
-				lscy.as<cx<double>>(), src, dst, acc_in, acc_out);
-		launches++;
+			launch("solve_y", bytes, [&] {
+				k_solve<R, 1><<<(nt + 127) / 128, 128, 0, stream>>>(Gm, slot0, nsl, facy.as<cx<R>>(),
+					lscy.as<cx<double>>(), src, dst, acc_in, acc_out);
+			});
 	}
 
 	// ParaxialPrimaryEvolutionOperator::apply (ParaxialPrimaryEvolutionOperator.cpp:153-209).
-	void rec_adi(SampleHost& h, const Geom& Gm, int slot0, int nsl, int Nw, const cx<R>* C, cx<R>* Fp,
+	void rec_adi(SampleHost& h, const Geom& Gm, int slot0, int nsl, int ng, int Nw, const cx<R>* C, cx<R>* Fp,
 			cx<R>* Tb, cx<R>* T2b) {
 		const int N = Gm.N;
+		const double sc = sizeof(cx<R>);
 		dim3 gr = pgrid(N, nsl);
+		const double fp = (double)N * nsl;
 		for(int dirn = 0; dirn < 2; dirn++) {
 			// explicit half-step in the other direction, then implicit solve + Woodbury
-			if(dirn == 0) k_stencil<R, ST_EXPL_Y><<<gr, 256, 0, stream>>>(Gm, slot0, C, Fp, T2b);
-			else k_stencil<R, ST_EXPL_X><<<gr, 256, 0, stream>>>(Gm, slot0, C, Fp, T2b);
-			launches++;
-			rec_solve(dirn, Gm, slot0, nsl, T2b, Tb, nullptr, nullptr);
+			if(dirn == 0)
+				launch("expl_y", fp * 4 * sc + (double)N * ng * 20 * sc, [&] {
+					k_stencil<R, ST_EXPL_Y><<<gr, 256, 0, stream>>>(Gm, slot0, C, Fp, T2b);
+				});
+			else
+				launch("expl_x", fp * 4 * sc + (double)N * ng * 20 * sc, [&] {
+					k_stencil<R, ST_EXPL_X><<<gr, 256, 0, stream>>>(Gm, slot0, C, Fp, T2b);
+				});
+			rec_solve(dirn, Gm, slot0, nsl, ng, T2b, Tb, nullptr, nullptr);
 			cx<R>* cur = Tb;
 			cx<R>* oth = T2b;
 			if(Nw == 0) {
 				size_t n = (size_t)nsl * 2 * N;
-				k_copy<R><<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, Tb, Fp);
-				launches++;
+				launch("copy_fields", 2.0 * n * sc, [&] {
+					k_copy<R><<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, Tb, Fp);
+				});
 			}
 			for(int it = 1; it <= Nw; it++) {
-				if(dirn == 0) k_stencil<R, ST_WOOD_X><<<gr, 256, 0, stream>>>(Gm, slot0, C, cur, oth);
-				else k_stencil<R, ST_WOOD_Y><<<gr, 256, 0, stream>>>(Gm, slot0, C, cur, oth);
-				launches++;
-				rec_solve(dirn, Gm, slot0, nsl, oth, oth, it == 1 ? Tb : Fp, Fp);
+				if(dirn == 0)
+					launch("wood_x", fp * 4 * sc + (double)N * ng * 14 * sc, [&] {
+						k_stencil<R, ST_WOOD_X><<<gr, 256, 0, stream>>>(Gm, slot0, C, cur, oth);
+					});
+				else
+					launch("wood_y", fp * 4 * sc + (double)N * ng * 14 * sc, [&] {
+						k_stencil<R, ST_WOOD_Y><<<gr, 256, 0, stream>>>(Gm, slot0, C, cur, oth);
+					});
+				rec_solve(dirn, Gm, slot0, nsl, ng, oth, oth, it == 1 ? Tb : Fp, Fp);
 				std::swap(cur, oth);
 			}
 		}
 		(void)h;
+	}
+
+	// One eager execution with events around every launch; per-kernel totals.
+	void profile(std::vector<std::string>& names, std::vector<double>& ms, std::vector<int>& cnt,
+			std::vector<double>& bytes) override {
+		CK(cudaSetDevice(opt.device));
+		profiling = true;
+		prof.clear();
+		evnext = 0;
+		try { record(); }
+		catch(...) { profiling = false; throw; }
+		profiling = false;
+		CK(cudaStreamSynchronize(stream));
+		for(auto& r : prof) {
+			float t = 0;
+			CK(cudaEventElapsedTime(&t, r.a, r.b));
+			size_t k = 0;
+			for(; k < names.size(); k++) if(names[k] == r.name) break;
+			if(k == names.size()) { names.push_back(r.name); ms.push_back(0); cnt.push_back(0); bytes.push_back(0); }
+			ms[k] += t;
+			cnt[k] += 1;
+			bytes[k] += r.bytes;
+		}
 	}
 
 	void execute(nbpm_timing* tm) override {
@@ -682,6 +791,25 @@ int nbpm_plan_slab_ms(nbpm_plan* p, double* ms) {
 	if(!p || !ms) return fail(E_ARG, "null argument");
 	*ms = p->impl->slab_ms();
 	return 0;
+}
+
+int nbpm_plan_profile(nbpm_plan* p, char (*names)[48], double* ms, int* launches, double* bytes, int* n) {
+	API_GUARD({
+		if(!p || !names || !ms || !launches || !bytes || !n) return fail(E_ARG, "null argument");
+		std::vector<std::string> nm;
+		std::vector<double> t, b;
+		std::vector<int> c;
+		p->impl->profile(nm, t, c, b);
+		int k = std::min<int>(*n, (int)nm.size());
+		for(int i = 0; i < k; i++) {
+			std::snprintf(names[i], 48, "%s", nm[i].c_str());
+			ms[i] = t[i];
+			launches[i] = c[i];
+			bytes[i] = b[i];
+		}
+		*n = k;
+		return 0;
+	})
 }
 
 long long nbpm_plan_device_bytes(const nbpm_plan* p) { return p ? p->impl->device_bytes() : 0; }
