@@ -103,6 +103,11 @@ def workload(name):
         c["desc"] = "batched Koehler micrograph 256x256x64 d=0.25um, 16 wavelengths x 13 q x 2 pol (416 propagations)"
         c["Nz"] = 64
         return [c]
+    if name == "config3s":
+        c = W.config3(dims=(256, 256, 8), n_wavelengths=8)
+        c["desc"] = "reduced batched Koehler case for profiling: 256x256x8, 8 wavelengths x 13 q x 2 pol"
+        c["Nz"] = 8
+        return [c]
     if name == "config1":
         c = W.config1()
         c["desc"] = "twisted nematic 64x64x40 d=0.25um, 1 wavelength x 1 q x 2 pol"
@@ -182,6 +187,14 @@ def run_ours(args):
     value = vs * args.steps * world / (dev_ms / 1e3)
     plan.download()
     out32 = [b["E"].copy() for b in bufs]
+    if args.only_value:
+        plan.close()
+        if rank == 0:
+            print(json.dumps({"metric": "voxel-steps/s", "value": value, "unit": "voxel-steps/s", "steps": args.steps,
+                              "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
+                              "config": {"workload": samples[0]["desc"], "precision": prec},
+                              "gpu_launches": launches, "clocks": clocks}))
+        return
     prof = profile_kernels(plan, lib)
     plan.close()
 
@@ -365,12 +378,13 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="config3", choices=["config1", "config2", "config3", "config4"])
+    ap.add_argument("--workload", default="config3", choices=["config1", "config2", "config3", "config3s", "config4"])
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--only-value", action="store_true", help="time the device-resident run only")
     args = ap.parse_args()
     world, rank, local = dist_env()
     if world > 1:

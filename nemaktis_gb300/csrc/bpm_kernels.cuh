@@ -27,7 +27,9 @@ enum { C_PH = 0, C_DX = 3, C_DY = 15, C_DXDY = 27, NCOEF = 43 };
 // index dir*6 + comp*3 + k (dir 0 = DX, 1 = DY; comp 0 = block 00, 1 = block 11).
 enum { NDIAG = 12 };
 // Line-solve factor planes.
-enum { F_INF = 0, F_RB, F_GAM, F_COR, F_W, NFAC };
+// F_A = alpha_i = -inf_i/beta_i (forward recurrence d_i = alpha_i d_{i-1} + b_i/beta_i),
+// F_RB = 1/beta_i, F_W = w_i, F_C = -gamma_i (backward recurrence), F_COR = corr_i.
+enum { F_A = 0, F_RB, F_W, F_C, F_COR, NFAC };
 
 struct GroupParams {
 	double wavelength, k0, dX, dY, dZ;
@@ -335,16 +337,19 @@ __global__ void k_coef(const double* __restrict__ QA, const double* __restrict__
 // 195-258 and 386-449): Thomas sweep with beta0 = 2*mid0 and the Sherman-Morrison corner
 // vector corr (corr0 = -1/2). Everything that does not depend on the right-hand side is
 // computed here once per (wavelength, slab) and shared by all (q, pol) slots:
-//   F_INF  inf_i           F_RB  1/beta_i        F_GAM gamma_i
+//   F_A    alpha_i = -inf_i/beta_i   F_RB  1/beta_i        F_C   -gamma_i
 //   F_COR  corr_i after back-substitution
 //   F_W    w_i = prod_{j<i}(-gamma_j), so that the back-substituted x_0 = sum_i w_i d_i
 //          is formed during the forward sweep
+// The forward sweep is then d_i = alpha_i d_{i-1} + b_i/beta_i and the backward sweep
+// x_{i-1} = d_{i-1} - gamma_{i-1} x_i: both first-order affine recurrences whose
+// coefficients do not depend on b, which is what the chunked solves below exploit.
 // plus per line r0 = inf0/mid0 and rden = 1/(1 + corr0 - r0*corr_{L-2}) in FP64.
 // scr holds FP64 gamma and forward corr: [group][comp][2][N].
 // ---------------------------------------------------------------------------------------
 template <typename S>
-__global__ void k_factor(int dirn, Geom G, int ngroups, const cx<double>* __restrict__ diag,
-		cx<S>* __restrict__ fac, cx<double>* __restrict__ lsc, cx<double>* __restrict__ scr) {
+__global__ void k_factor(int dirn, Geom G, int ngroups, int chunkM, const cx<double>* __restrict__ diag,
+		cx<S>* __restrict__ fac, size_t plane, cx<double>* __restrict__ lsc, cx<double>* __restrict__ scr) {
 	int Nx = G.Nx, Ny = G.Ny, N = G.N;
 	int L = dirn == 0 ? Nx : Ny;
 	int nlines = dirn == 0 ? Ny : Nx;
@@ -354,55 +359,75 @@ __global__ void k_factor(int dirn, Geom G, int ngroups, const cx<double>* __rest
 	int c = (t / nlines) % 2;
 	int g = t / (2 * nlines);
 	const cx<double>* Dg = diag + (size_t)g * NDIAG * N + (size_t)(dirn * 6 + c * 3) * N;
-	cx<S>* Fc = fac + ((size_t)g * 2 + c) * NFAC * N;
+	cx<S>* Fc = fac + ((size_t)g * 2 + c) * NFAC * plane;
 	cx<double>* sG = scr + ((size_t)g * 2 + c) * 2 * N;
 	cx<double>* sC = sG + N;
 	cx<double>* ls = lsc + (((size_t)g * 2 + c) * nlines + line) * 2;
 	const int stride = dirn == 0 ? 1 : Nx;
 	const int base = dirn == 0 ? Nx * line : line;
+	// point index of element i (stencil coefficient / scratch layout)
 	auto P = [&](int i) { return base + i * stride; };
+	// factor storage index: natural layout, or chunk-interleaved x-line layout where element
+	// i = lane*M + k of a line sits at k*32 + lane (coalesced for one-warp-per-line solves)
+	auto Q = [&](int i) -> size_t {
+		if(chunkM <= 0) return (size_t)P(i);
+		return (size_t)line * 32 * chunkM + (size_t)(i % chunkM) * 32 + (i / chunkM);
+	};
 	const cx<double> one = mk(1.0, 0.0);
 	auto sup = [&](int i) { return -Dg[2 * (size_t)N + P(i)]; };
 	auto mid = [&](int i) { return one - Dg[1 * (size_t)N + P(i)]; };
 	auto inf = [&](int i) { return -Dg[P(i)]; };
 
 	cx<double> beta = 2.0 * mid(0);
-	Fc[F_RB * N + P(0)] = cvt<S>(crecip(beta));
-	Fc[F_INF * N + P(0)] = mk<S>(0, 0);
+	cx<double> rb = crecip(beta);
+	Fc[F_RB * plane + Q(0)] = cvt<S>(rb);
+	Fc[F_A * plane + Q(0)] = mk<S>(0, 0);
 	cx<double> corr = mk(-0.5, 0.0);
 	sC[P(0)] = corr;
 	for(int i = 1; i < L - 2; i++) {
-		cx<double> gam = cdiv(sup(i - 1), beta);
+		cx<double> gam = sup(i - 1) * rb;
 		sG[P(i - 1)] = gam;
-		Fc[F_GAM * N + P(i - 1)] = cvt<S>(gam);
+		Fc[F_C * plane + Q(i - 1)] = cvt<S>(-gam);
 		cx<double> in = inf(i);
 		beta = mid(i) - in * gam;
-		Fc[F_RB * N + P(i)] = cvt<S>(crecip(beta));
-		Fc[F_INF * N + P(i)] = cvt<S>(in);
-		corr = cdiv(-(in * corr), beta);
+		rb = crecip(beta);
+		Fc[F_RB * plane + Q(i)] = cvt<S>(rb);
+		Fc[F_A * plane + Q(i)] = cvt<S>(-(in * rb));
+		corr = -(in * corr) * rb;
 		sC[P(i)] = corr;
 	}
-	cx<double> gl = cdiv(sup(L - 3), beta);
+	cx<double> gl = sup(L - 3) * rb;
 	sG[P(L - 3)] = gl;
-	Fc[F_GAM * N + P(L - 3)] = cvt<S>(gl);
+	Fc[F_C * plane + Q(L - 3)] = cvt<S>(-gl);
 	cx<double> inL = inf(L - 2);
 	beta = mid(L - 2) + cdiv(sup(L - 2) * inf(0), mid(0)) - inL * gl;
-	Fc[F_RB * N + P(L - 2)] = cvt<S>(crecip(beta));
-	Fc[F_INF * N + P(L - 2)] = cvt<S>(inL);
-	cx<double> corr_last = cdiv(sup(L - 2) - inL * corr, beta);
-	Fc[F_COR * N + P(L - 2)] = cvt<S>(corr_last);
-	Fc[F_GAM * N + P(L - 2)] = mk<S>(0, 0);
+	rb = crecip(beta);
+	Fc[F_RB * plane + Q(L - 2)] = cvt<S>(rb);
+	Fc[F_A * plane + Q(L - 2)] = cvt<S>(-(inL * rb));
+	cx<double> corr_last = (sup(L - 2) - inL * corr) * rb;
+	Fc[F_COR * plane + Q(L - 2)] = cvt<S>(corr_last);
+	Fc[F_C * plane + Q(L - 2)] = mk<S>(0, 0);
 	cx<double> cn = corr_last;
 	for(int i = L - 2; i > 0; i--) {
 		cx<double> cv = sC[P(i - 1)] - sG[P(i - 1)] * cn;
-		Fc[F_COR * N + P(i - 1)] = cvt<S>(cv);
+		Fc[F_COR * plane + Q(i - 1)] = cvt<S>(cv);
 		cn = cv;
 	}
 	cx<double> w = one;
-	Fc[F_W * N + P(0)] = cvt<S>(w);
+	Fc[F_W * plane + Q(0)] = cvt<S>(w);
 	for(int i = 1; i < L - 1; i++) {
 		w = -(w * sG[P(i - 1)]);
-		Fc[F_W * N + P(i)] = cvt<S>(w);
+		Fc[F_W * plane + Q(i)] = cvt<S>(w);
+	}
+	if(chunkM > 0) {
+		// padding elements of the interleaved layout act as identity maps
+		for(int i = L - 1; i < 32 * chunkM; i++) {
+			Fc[F_A * plane + Q(i)] = mk<S>(0, 0);
+			Fc[F_RB * plane + Q(i)] = mk<S>(0, 0);
+			Fc[F_W * plane + Q(i)] = mk<S>(0, 0);
+			Fc[F_C * plane + Q(i)] = mk<S>(0, 0);
+			Fc[F_COR * plane + Q(i)] = mk<S>(0, 0);
+		}
 	}
 	cx<double> r0 = cdiv(inf(0), mid(0));
 	ls[0] = r0;
@@ -497,10 +522,11 @@ __global__ void k_stencil(Geom G, int slot0, const cx<R>* __restrict__ coef, con
 	}
 }
 
-// Periodic line solve with the pre-factored Thomas/Sherman-Morrison data. One thread per
-// (line, comp, slot). dst may alias src. If acc_out is set: acc_out = acc_in + x.
+// Periodic line solve with the pre-factored Thomas/Sherman-Morrison data, sequential form:
+// one thread per (line, comp, slot). Used for lines too long for the chunked kernels.
+// dst may alias src. If acc_out is set: acc_out = acc_in + x.
 template <typename R, int DIRN>
-__global__ void k_solve(Geom G, int slot0, int nslots, const cx<R>* __restrict__ fac,
+__global__ void k_solve(Geom G, int slot0, int nslots, const cx<R>* __restrict__ fac, size_t plane,
 		const cx<double>* __restrict__ lsc, const cx<R>* src, cx<R>* dst,
 		const cx<R>* acc_in, cx<R>* acc_out) {
 	int Nx = G.Nx, Ny = G.Ny, N = G.N;
@@ -526,31 +552,28 @@ __global__ void k_solve(Geom G, int slot0, int nslots, const cx<R>* __restrict__
 		}
 		return;
 	}
-	const cx<R>* Fc = fac + ((size_t)g * 2 + c) * NFAC * N;
+	const cx<R>* Fc = fac + ((size_t)g * 2 + c) * NFAC * plane;
 	const cx<double>* ls = lsc + (((size_t)g * 2 + c) * nlines + line) * 2;
-	// forward sweep
 	int q = base;
-	cx<R> d = S[q] * Fc[F_RB * N + q];
+	cx<R> d = S[q] * Fc[F_RB * plane + q];
 	cx<R> acc = d;
 	D[q] = d;
 	for(int i = 1; i < L - 1; i++) {
 		q += stride;
-		cx<R> sv = S[q];
-		d = (sv - Fc[F_INF * N + q] * d) * Fc[F_RB * N + q];
-		acc += Fc[F_W * N + q] * d;
+		d = Fc[F_A * plane + q] * d + S[q] * Fc[F_RB * plane + q];
+		acc += Fc[F_W * plane + q] * d;
 		D[q] = d;
 	}
 	cx<double> frac = (cvt<double>(acc) - ls[0] * cvt<double>(d)) * ls[1];
 	cx<R> fr = cvt<R>(frac);
-	// backward sweep with the Sherman-Morrison correction applied on the way
 	cx<R> dn = d;
-	cx<R> x = dn - fr * Fc[F_COR * N + q];
+	cx<R> x = dn - fr * Fc[F_COR * plane + q];
 	D[q] = x;
 	if(acc_out) acc_out[off + q] = acc_in[off + q] + x;
 	for(int i = L - 2; i > 0; i--) {
 		q -= stride;
-		cx<R> dp = D[q] - Fc[F_GAM * N + q] * dn;
-		x = dp - fr * Fc[F_COR * N + q];
+		cx<R> dp = D[q] + Fc[F_C * plane + q] * dn;
+		x = dp - fr * Fc[F_COR * plane + q];
 		D[q] = x;
 		if(acc_out) acc_out[off + q] = acc_in[off + q] + x;
 		dn = dp;
@@ -558,6 +581,240 @@ __global__ void k_solve(Geom G, int slot0, int nslots, const cx<R>* __restrict__
 	int qe = base + (L - 1) * stride;
 	D[qe] = x;  // duplicate point = x_0
 	if(acc_out) acc_out[off + qe] = acc_in[off + qe] + x;
+}
+
+template <typename R>
+__device__ __forceinline__ cx<R> shfl_up_c(cx<R> v, int d) {
+	return mk<R>(__shfl_up_sync(0xffffffffu, v.x, d), __shfl_up_sync(0xffffffffu, v.y, d));
+}
+template <typename R>
+__device__ __forceinline__ cx<R> shfl_down_c(cx<R> v, int d) {
+	return mk<R>(__shfl_down_sync(0xffffffffu, v.x, d), __shfl_down_sync(0xffffffffu, v.y, d));
+}
+template <typename R>
+__device__ __forceinline__ cx<R> shfl_idx_c(cx<R> v, int l) {
+	return mk<R>(__shfl_sync(0xffffffffu, v.x, l), __shfl_sync(0xffffffffu, v.y, l));
+}
+template <typename R>
+__device__ __forceinline__ cx<R> shfl_xor_c(cx<R> v, int m) {
+	return mk<R>(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+}
+
+// x-line solve, chunked parallel form: one warp per (line, group, comp); lane l owns the
+// unknowns [l*M, l*M+M) of the line. The forward and backward recurrences are composed per
+// chunk, combined by warp-shuffle scans and replayed, so every sweep is parallel over
+// 32 lanes. The line is staged through shared memory for coalesced global accesses, the
+// factor planes are stored chunk-interleaved (element l*M+k at k*32+l). Each warp loops over
+// every (q, pol) slot of its wavelength group. Block = LT warps = LT consecutive lines.
+template <typename R, int M>
+__global__ void __launch_bounds__(128) k_solve_xc(Geom G, int slot0, int ng, const cx<R>* __restrict__ fac,
+		size_t plane, const cx<double>* __restrict__ lsc, const cx<R>* src, cx<R>* dst,
+		const cx<R>* acc_in, cx<R>* acc_out) {
+	extern __shared__ unsigned char smem_raw[];
+	const int LT = blockDim.x / 32;
+	const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+	const int Nx = G.Nx, Ny = G.Ny, N = G.N;
+	const int iy = blockIdx.x * LT + warp;
+	if(iy >= Ny) return;
+	const int g = blockIdx.y / 2, c = blockIdx.y % 2;
+	const int n_unk = Nx - 1;
+	cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw) + (size_t)warp * 32 * (M + 1);
+	const cx<R>* Fc = fac + ((size_t)g * 2 + c) * NFAC * plane + (size_t)iy * 32 * M;
+	const cx<double>* ls = lsc + (((size_t)g * 2 + c) * Ny + iy) * 2;
+	const cx<double> r0 = ls[0], rden = ls[1];
+	const int i0 = lane * M;
+	const int last = n_unk - 1, lane_last = last / M, k_last = last % M;
+	const cx<R> one = mk<R>(1, 0), zero = mk<R>(0, 0);
+	for(int sl = 0; sl < G.spg; sl++) {
+		const size_t off = ((size_t)g * G.spg + sl) * 2 * N + (size_t)c * N + (size_t)iy * Nx;
+		for(int e = lane; e < n_unk; e += 32) buf[(e / M) * (M + 1) + e % M] = src[off + e];
+		__syncwarp();
+		cx<R> v[M];
+		cx<R> A = one, B = zero;
+#pragma unroll
+		for(int k = 0; k < M; k++) {
+			v[k] = zero;
+			if(i0 + k < n_unk) {
+				cx<R> a = Fc[F_A * plane + k * 32 + lane];
+				cx<R> b = buf[lane * (M + 1) + k] * Fc[F_RB * plane + k * 32 + lane];
+				v[k] = b;
+				B = a * B + b;
+				A = a * A;
+			}
+		}
+#pragma unroll
+		for(int o = 1; o < 32; o <<= 1) {
+			cx<R> Ap = shfl_up_c(A, o), Bp = shfl_up_c(B, o);
+			if(lane >= o) { B = A * Bp + B; A = A * Ap; }
+		}
+		cx<R> d = shfl_up_c(B, 1);
+		if(lane == 0) d = zero;
+		cx<R> acc = zero, dl = zero;
+#pragma unroll
+		for(int k = 0; k < M; k++) {
+			if(i0 + k < n_unk) {
+				d = Fc[F_A * plane + k * 32 + lane] * d + v[k];
+				v[k] = d;
+				acc += Fc[F_W * plane + k * 32 + lane] * d;
+			}
+			if(k == k_last) dl = d;
+		}
+#pragma unroll
+		for(int o = 16; o > 0; o >>= 1) acc += shfl_xor_c(acc, o);
+		dl = shfl_idx_c(dl, lane_last);
+		const cx<R> fr = cvt<R>((cvt<double>(acc) - r0 * cvt<double>(dl)) * rden);
+		A = one; B = zero;
+#pragma unroll
+		for(int k = M - 1; k >= 0; k--) {
+			if(i0 + k < n_unk) {
+				cx<R> cc = Fc[F_C * plane + k * 32 + lane];
+				B = cc * B + v[k];
+				A = cc * A;
+			}
+		}
+#pragma unroll
+		for(int o = 1; o < 32; o <<= 1) {
+			cx<R> An = shfl_down_c(A, o), Bn = shfl_down_c(B, o);
+			if(lane + o < 32) { B = A * Bn + B; A = A * An; }
+		}
+		cx<R> dd = shfl_down_c(B, 1);
+		if(lane == 31) dd = zero;
+#pragma unroll
+		for(int k = M - 1; k >= 0; k--) {
+			if(i0 + k < n_unk) {
+				dd = Fc[F_C * plane + k * 32 + lane] * dd + v[k];
+				buf[lane * (M + 1) + k] = dd - fr * Fc[F_COR * plane + k * 32 + lane];
+			}
+		}
+		__syncwarp();
+		for(int e = lane; e < Nx; e += 32) {
+			int ee = e == Nx - 1 ? 0 : e;
+			cx<R> x = buf[(ee / M) * (M + 1) + ee % M];
+			dst[off + e] = x;
+			if(acc_out) acc_out[off + e] = acc_in[off + e] + x;
+		}
+		__syncwarp();
+	}
+}
+
+// y-line solve, chunked parallel form: block = 32 adjacent columns (lanes, coalesced) x WY
+// warps; warp w owns the rows [w*M, w*M+M) of the 32 lines. Chunk maps are combined across
+// warps through shared memory. Each block loops over the (q, pol) slots of its group.
+template <typename R, int M>
+__global__ void __launch_bounds__(1024) k_solve_yc(Geom G, int slot0, int ng, const cx<R>* __restrict__ fac,
+		size_t plane, const cx<double>* __restrict__ lsc, const cx<R>* src, cx<R>* dst,
+		const cx<R>* acc_in, cx<R>* acc_out) {
+	extern __shared__ unsigned char smem_raw[];
+	const int WY = blockDim.y;
+	const int lane = threadIdx.x, w = threadIdx.y;
+	const int Nx = G.Nx, Ny = G.Ny, N = G.N;
+	const int ix = blockIdx.x * 32 + lane;
+	const bool col = ix < Nx;
+	const int g = blockIdx.y / 2, c = blockIdx.y % 2;
+	const int n_unk = Ny - 1;
+	cx<R>* sA = reinterpret_cast<cx<R>*>(smem_raw);
+	cx<R>* sB = sA + WY * 32;
+	cx<R>* sD = sB + WY * 32;
+	cx<R>* sP = sD + WY * 32;
+	cx<R>* sL = sP + WY * 32;
+	cx<R>* sF = sL + 32;
+	const cx<R>* Fc = fac + ((size_t)g * 2 + c) * NFAC * plane;
+	const int i0 = w * M;
+	const cx<R> one = mk<R>(1, 0), zero = mk<R>(0, 0);
+	cx<double> r0 = mk(0.0, 0.0), rden = mk(0.0, 0.0);
+	if(col) {
+		const cx<double>* ls = lsc + (((size_t)g * 2 + c) * Nx + ix) * 2;
+		r0 = ls[0]; rden = ls[1];
+	}
+	for(int sl = 0; sl < G.spg; sl++) {
+		const size_t off = ((size_t)g * G.spg + sl) * 2 * N + (size_t)c * N;
+		cx<R> v[M];
+		cx<R> A = one, B = zero;
+#pragma unroll
+		for(int k = 0; k < M; k++) {
+			v[k] = zero;
+			int i = i0 + k;
+			if(col && i < n_unk) {
+				size_t q = (size_t)ix + (size_t)Nx * i;
+				cx<R> a = Fc[F_A * plane + q];
+				cx<R> b = src[off + q] * Fc[F_RB * plane + q];
+				v[k] = b;
+				B = a * B + b;
+				A = a * A;
+			}
+		}
+		sA[w * 32 + lane] = A;
+		sB[w * 32 + lane] = B;
+		__syncthreads();
+		if(w == 0) {
+			cx<R> D = zero;
+			for(int ww = 0; ww < WY; ww++) {
+				sD[ww * 32 + lane] = D;
+				D = sA[ww * 32 + lane] * D + sB[ww * 32 + lane];
+			}
+		}
+		__syncthreads();
+		cx<R> d = sD[w * 32 + lane];
+		cx<R> acc = zero;
+#pragma unroll
+		for(int k = 0; k < M; k++) {
+			int i = i0 + k;
+			if(col && i < n_unk) {
+				size_t q = (size_t)ix + (size_t)Nx * i;
+				d = Fc[F_A * plane + q] * d + v[k];
+				v[k] = d;
+				acc += Fc[F_W * plane + q] * d;
+				if(i == n_unk - 1) sL[lane] = d;
+			}
+		}
+		sP[w * 32 + lane] = acc;
+		__syncthreads();
+		if(w == 0) {
+			cx<R> tot = zero;
+			for(int ww = 0; ww < WY; ww++) tot += sP[ww * 32 + lane];
+			sF[lane] = cvt<R>((cvt<double>(tot) - r0 * cvt<double>(sL[lane])) * rden);
+		}
+		A = one; B = zero;
+#pragma unroll
+		for(int k = M - 1; k >= 0; k--) {
+			int i = i0 + k;
+			if(col && i < n_unk) {
+				cx<R> cc = Fc[F_C * plane + (size_t)ix + (size_t)Nx * i];
+				B = cc * B + v[k];
+				A = cc * A;
+			}
+		}
+		sA[w * 32 + lane] = A;
+		sB[w * 32 + lane] = B;
+		__syncthreads();
+		if(w == 0) {
+			cx<R> D = zero;
+			for(int ww = WY - 1; ww >= 0; ww--) {
+				sD[ww * 32 + lane] = D;
+				D = sA[ww * 32 + lane] * D + sB[ww * 32 + lane];
+			}
+		}
+		__syncthreads();
+		const cx<R> fr = sF[lane];
+		cx<R> dd = sD[w * 32 + lane];
+#pragma unroll
+		for(int k = M - 1; k >= 0; k--) {
+			int i = i0 + k;
+			if(col && i < n_unk) {
+				size_t q = (size_t)ix + (size_t)Nx * i;
+				dd = Fc[F_C * plane + q] * dd + v[k];
+				cx<R> x = dd - fr * Fc[F_COR * plane + q];
+				dst[off + q] = x;
+				if(acc_out) acc_out[off + q] = acc_in[off + q] + x;
+				if(i == 0) {
+					size_t qe = (size_t)ix + (size_t)Nx * (Ny - 1);
+					dst[off + qe] = x;
+					if(acc_out) acc_out[off + qe] = acc_in[off + qe] + x;
+				}
+			}
+		}
+		__syncthreads();
+	}
 }
 
 // Point-wise symmetric 2x2 phase operator (PhaseEvolutionOperator.cpp:14-32).

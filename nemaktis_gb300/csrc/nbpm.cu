@@ -70,6 +70,7 @@ struct SampleHost {
 	std::vector<GroupParams> gps;
 	std::vector<ShiftParams> shifts;
 	bool any_shift = false, any_zero_q = false;
+	int index = 0;
 	ScreenParams sp;
 	// device
 	DevBuf dir, dmask, dwts, F, E0, gpsd, shiftd, partial, wl, nout, qv;
@@ -190,6 +191,9 @@ struct Plan : PlanBase {
 	}
 	double last_slab_ms = 0;
 	size_t smem_limit = 0;
+	// line-solve configuration per sample (chunk sizes of the parallel kernels; 0 = sequential)
+	struct SolveCfg { int Mx = 0, My = 0, WY = 0; size_t plane_x = 0, plane_y = 0; };
+	std::vector<SolveCfg> scfg;
 
 	Plan(const nbpm_options& o) : opt(o) {
 		for(auto& e : ev) e = nullptr;
@@ -284,6 +288,7 @@ struct Plan : PlanBase {
 			sp.z_foc = zf;
 			for(int l = 0; l < 8; l++) sp.thick[l] = l < sp.n_iso ? s.iso_thick[l] : 0;
 			for(int l = 0; l < 9; l++) sp.index[l] = l < sp.n_iso ? s.iso_index[l] : 1;
+			h->index = (int)S.size();
 			S.push_back(std::move(h));
 		}
 		// Host-side validation is complete; only now touch the device.
@@ -295,7 +300,15 @@ struct Plan : PlanBase {
 		CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
 		smem_limit = (size_t)optin;
 		CK(cudaFuncSetAttribute(k_fft_lines<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit));
+		set_smem_attr<1>(); set_smem_attr<2>(); set_smem_attr<4>(); set_smem_attr<8>();
+		set_smem_attr<16>(); set_smem_attr<32>();
 		allocate();
+	}
+
+	template <int M>
+	void set_smem_attr() {
+		CK(cudaFuncSetAttribute(k_solve_xc<R, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit));
+		CK(cudaFuncSetAttribute(k_solve_yc<R, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit));
 	}
 
 	int gpp(const SampleHost& h) const {
@@ -309,11 +322,24 @@ struct Plan : PlanBase {
 			SampleHost& h = *hp;
 			size_t N = h.geom.N;
 			int ng = gpp(h);
+			SolveCfg sc;
+			int ux = h.s.Nx - 1, uy = h.s.Ny - 1;
+			if(h.s.Nx > 3) {
+				for(int M = 1; M <= 32; M *= 2) if(32 * M >= ux) { sc.Mx = M; break; }
+			}
+			if(h.s.Ny > 3) {
+				for(int M = 2; M <= 32; M *= 2) if((uy + M - 1) / M <= 16) { sc.My = M; break; }
+				if(!sc.My && (uy + 31) / 32 <= 32) sc.My = 32;
+				if(sc.My) sc.WY = (uy + sc.My - 1) / sc.My;
+			}
+			sc.plane_x = sc.Mx ? std::max(N, (size_t)h.s.Ny * 32 * sc.Mx) : N;
+			sc.plane_y = N;
+			scfg.push_back(sc);
 			maxT = std::max(maxT, (size_t)ng * h.spg * 2 * N);
 			maxQ = std::max(maxQ, (size_t)2 * ng * NQ * N);
 			maxC = std::max(maxC, (size_t)ng * NCOEF * N);
 			maxD = std::max(maxD, (size_t)ng * NDIAG * N);
-			maxFx = std::max(maxFx, (size_t)ng * 2 * NFAC * N);
+			maxFx = std::max(maxFx, (size_t)ng * 2 * NFAC * std::max(sc.plane_x, sc.plane_y));
 			maxL = std::max(maxL, (size_t)ng * 2 * std::max(h.s.Nx, h.s.Ny) * 2);
 			maxScr = std::max(maxScr, (size_t)ng * 2 * 2 * N);
 			if(sizeof(R) != sizeof(double)) maxStage = std::max(maxStage, (size_t)h.slots * 2 * N);
@@ -497,12 +523,13 @@ struct Plan : PlanBase {
 				});
 				int lx = ng * 2 * Ny, ly = ng * 2 * Nx;
 				const double fb = (double)N * ng * 2 * (3 * 16 + NFAC * sc + 4 * 16);
+				const SolveCfg& scf = scfg[h.index];
 				launch("factor_x", fb, [&] {
-					k_factor<R><<<(lx + 63) / 64, 64, 0, stream>>>(0, Gm, ng, Dg, facx.as<cx<R>>(),
+					k_factor<R><<<(lx + 63) / 64, 64, 0, stream>>>(0, Gm, ng, scf.Mx, Dg, facx.as<cx<R>>(), scf.plane_x,
 						lscx.as<cx<double>>(), scr.as<cx<double>>());
 				});
 				launch("factor_y", fb, [&] {
-					k_factor<R><<<(ly + 63) / 64, 64, 0, stream>>>(1, Gm, ng, Dg, facy.as<cx<R>>(),
+					k_factor<R><<<(ly + 63) / 64, 64, 0, stream>>>(1, Gm, ng, 0, Dg, facy.as<cx<R>>(), scf.plane_y,
 						lscy.as<cx<double>>(), scr.as<cx<double>>());
 				});
 				// shift -> phase -> ADI -> phase -> shift (BPMIteration.cpp:133-146)
@@ -552,21 +579,65 @@ struct Plan : PlanBase {
 		}
 	}
 
-	void rec_solve(int dirn, const Geom& Gm, int slot0, int nsl, int ng, const cx<R>* src, cx<R>* dst,
+	template <int M>
+	void launch_xc(const Geom& Gm, int slot0, int ng, const SolveCfg& sc, const cx<R>* src, cx<R>* dst,
+			const cx<R>* ai, cx<R>* ao) {
+		const int LT = 4;
+		size_t smem = (size_t)LT * 32 * (M + 1) * sizeof(cx<R>);
+		dim3 grid((unsigned)((Gm.Ny + LT - 1) / LT), (unsigned)(ng * 2));
+		k_solve_xc<R, M><<<grid, 32 * LT, smem, stream>>>(Gm, slot0, ng, facx.as<cx<R>>(), sc.plane_x,
+			lscx.as<cx<double>>(), src, dst, ai, ao);
+	}
+	template <int M>
+	void launch_yc(const Geom& Gm, int slot0, int ng, const SolveCfg& sc, const cx<R>* src, cx<R>* dst,
+			const cx<R>* ai, cx<R>* ao) {
+		size_t smem = (size_t)(5 * sc.WY * 32 + 2 * 32) * sizeof(cx<R>);
+		dim3 grid((unsigned)((Gm.Nx + 31) / 32), (unsigned)(ng * 2));
+		k_solve_yc<R, M><<<grid, dim3(32, sc.WY), smem, stream>>>(Gm, slot0, ng, facy.as<cx<R>>(), sc.plane_y,
+			lscy.as<cx<double>>(), src, dst, ai, ao);
+	}
+
+	void rec_solve(int dirn, SampleHost& h, const Geom& Gm, int slot0, int nsl, int ng, const cx<R>* src, cx<R>* dst,
 			const cx<R>* acc_in, cx<R>* acc_out) {
+		const SolveCfg& sc = scfg[h.index];
 		int nlines = dirn == 0 ? Gm.Ny : Gm.Nx;
 		int nt = nsl * 2 * nlines;
-		const double sc = sizeof(cx<R>);
-		double bytes = (double)Gm.N * nsl * 2 * sc * (acc_out ? 4 : 2) + (double)Gm.N * ng * 2 * NFAC * sc;
+		const double sz = sizeof(cx<R>);
+		double bytes = (double)Gm.N * nsl * 2 * sz * (acc_out ? 4 : 2) + (double)Gm.N * ng * 2 * NFAC * sz;
+		int M = dirn == 0 ? sc.Mx : sc.My;
+		if(M == 0) {
+			if(dirn == 0)
+				launch("solve_x", bytes, [&] {
+					k_solve<R, 0><<<(nt + 127) / 128, 128, 0, stream>>>(Gm, slot0, nsl, facx.as<cx<R>>(), sc.plane_x,
+						lscx.as<cx<double>>(), src, dst, acc_in, acc_out);
+				});
+			else
+				launch("solve_y", bytes, [&] {
+					k_solve<R, 1><<<(nt + 127) / 128, 128, 0, stream>>>(Gm, slot0, nsl, facy.as<cx<R>>(), sc.plane_y,
+						lscy.as<cx<double>>(), src, dst, acc_in, acc_out);
+				});
+			return;
+		}
 		if(dirn == 0)
 			launch("solve_x", bytes, [&] {
-				k_solve<R, 0><<<(nt + 127) / 128, 128, 0, stream>>>(Gm, slot0, nsl, facx.as<cx<R>>(),
-					lscx.as<cx<double>>(), src, dst, acc_in, acc_out);
+				switch(M) {
+					case 1: launch_xc<1>(Gm, slot0, ng, sc, src, dst, acc_in, acc_out); break;
+					case 2: launch_xc<2>(Gm, slot0, ng, sc, src, dst, acc_in, acc_out); break;
+					case 4: launch_xc<4>(Gm, slot0, ng, sc, src, dst, acc_in, acc_out); break;
+					case 8: launch_xc<8>(Gm, slot0, ng, sc, src, dst, acc_in, acc_out); break;
+					case 16: launch_xc<16>(Gm, slot0, ng, sc, src, dst, acc_in, acc_out); break;
+					default: launch_xc<32>(Gm, slot0, ng, sc, src, dst, acc_in, acc_out); break;
+				}
 			});
 		else
 			launch("solve_y", bytes, [&] {
-				k_solve<R, 1><<<(nt + 127) / 128, 128, 0, stream>>>(Gm, slot0, nsl, facy.as<cx<R>>(),
-					lscy.as<cx<double>>(), src, dst, acc_in, acc_out);
+				switch(M) {
+					case 2: launch_yc<2>(Gm, slot0, ng, sc, src, dst, acc_in, acc_out); break;
+					case 4: launch_yc<4>(Gm, slot0, ng, sc, src, dst, acc_in, acc_out); break;
+					case 8: launch_yc<8>(Gm, slot0, ng, sc, src, dst, acc_in, acc_out); break;
+					case 16: launch_yc<16>(Gm, slot0, ng, sc, src, dst, acc_in, acc_out); break;
+					default: launch_yc<32>(Gm, slot0, ng, sc, src, dst, acc_in, acc_out); break;
+				}
 			});
 	}
 
@@ -587,7 +658,7 @@ struct Plan : PlanBase {
 				launch("expl_x", fp * 4 * sc + (double)N * ng * 20 * sc, [&] {
 					k_stencil<R, ST_EXPL_X><<<gr, 256, 0, stream>>>(Gm, slot0, C, Fp, T2b);
 				});
-			rec_solve(dirn, Gm, slot0, nsl, ng, T2b, Tb, nullptr, nullptr);
+			rec_solve(dirn, h, Gm, slot0, nsl, ng, T2b, Tb, nullptr, nullptr);
 			cx<R>* cur = Tb;
 			cx<R>* oth = T2b;
 			if(Nw == 0) {
@@ -605,7 +676,7 @@ struct Plan : PlanBase {
 					launch("wood_y", fp * 4 * sc + (double)N * ng * 14 * sc, [&] {
 						k_stencil<R, ST_WOOD_Y><<<gr, 256, 0, stream>>>(Gm, slot0, C, cur, oth);
 					});
-				rec_solve(dirn, Gm, slot0, nsl, ng, oth, oth, it == 1 ? Tb : Fp, Fp);
+				rec_solve(dirn, h, Gm, slot0, nsl, ng, oth, oth, it == 1 ? Tb : Fp, Fp);
 				std::swap(cur, oth);
 			}
 		}
