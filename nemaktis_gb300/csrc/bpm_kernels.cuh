@@ -145,7 +145,8 @@ __global__ void k_neff_partial(const double* __restrict__ dir, int fd, const uin
 }
 
 // ---------------------------------------------------------------------------------------
-// Per-slab operator coefficients, FP64 arithmetic:
+// Per-slab operator coefficients (FP64 in FP64 mode; in FP32 mode the phase operator stays
+// FP64 and the stencil entries of mu*R are formed in FP32):
 //  * phase operator exp(i*a*d) (PhaseEvolutionOperator.cpp:34-63)
 //  * mu*R with R = i*W + (D*S^-1 + S^-1*D)/4, D = D0 + D1*K (ParaxialPrimaryEvolution-
 //    Operator.cpp:212-490), written per stencil entry: S^-1 and K at the column point for
@@ -153,51 +154,53 @@ __global__ void k_neff_partial(const double* __restrict__ dir, int fd, const uin
 //    and column points. D1 uses the reference's neighbour indices (ix==Nx-1 -> 1,
 //    ix==0 -> Nx-2) while the stencil columns wrap with period Nx-1.
 // ---------------------------------------------------------------------------------------
+template <typename T>
 struct CoefCtx {
 	const double* A;
 	const double* B;
 	int N, Nx;
-	double hmu, rxx, ryy, rxy, va0, va1;
-	__device__ __forceinline__ double avg(int q, int x, int y) const {
+	T hmu, rxx, ryy, rxy, va0, va1;
+	__device__ __forceinline__ T avg(int q, int x, int y) const {
 		int i = x + Nx * y;
-		return (A[q * N + i] + B[q * N + i]) / 2;
+		return (T)((A[q * N + i] + B[q * N + i]) / 2);
 	}
-	__device__ __forceinline__ double vsum(int a, int x, int y) const {
+	__device__ __forceinline__ T vsum(int a, int x, int y) const {
 		int i = x + Nx * y, q = a == 0 ? Q_VX : Q_VY;
-		return A[q * N + i] + B[q * N + i];
+		return (T)(A[q * N + i] + B[q * N + i]);
 	}
-	__device__ __forceinline__ void sinv(int x, int y, double& ixx, double& iyy, double& ixy) const {
-		double exx = avg(Q_XXS, x, y), eyy = avg(Q_YYS, x, y), exy = avg(Q_XYS, x, y);
-		double det = exx * eyy - exy * exy;
+	__device__ __forceinline__ void sinv(int x, int y, T& ixx, T& iyy, T& ixy) const {
+		T exx = avg(Q_XXS, x, y), eyy = avg(Q_YYS, x, y), exy = avg(Q_XYS, x, y);
+		T det = exx * eyy - exy * exy;
 		ixx = eyy / det; iyy = exx / det; ixy = -exy / det;
 	}
 	// One stencil entry of mu*R for the 4 blocks (00, 01, 10, 11). D is the real 2x2 entry
 	// of D at this (row, column) pair; dd is the first-derivative weight of the walk-off
 	// (0 for none) acting on component bT.
-	__device__ void entry(double D00, double D01, double D10, double D11, int cxp, int cyp,
-			double dd, int bT, cx<double> out[4]) const {
-		double re[4] = {0, 0, 0, 0}, im[4] = {0, 0, 0, 0};
+	__device__ void entry(T D00, T D01, T D10, T D11, int cxp, int cyp,
+			T dd, int bT, cx<T> out[4]) const {
+		T re[4] = {0, 0, 0, 0}, im[4] = {0, 0, 0, 0};
 		if(dd != 0) {
-			double vb0 = vsum(0, cxp, cyp), vb1 = vsum(1, cxp, cyp);
-			im[0 + bT] += dd * (0.25 * va0);
-			im[2 + bT] += dd * (0.25 * va1);
-			im[2 * bT + 0] += dd * (0.25 * vb0);
-			im[2 * bT + 1] += dd * (0.25 * vb1);
+			T vb0 = vsum(0, cxp, cyp), vb1 = vsum(1, cxp, cyp);
+			im[0 + bT] += dd * ((T)0.25 * va0);
+			im[2 + bT] += dd * ((T)0.25 * va1);
+			im[2 * bT + 0] += dd * ((T)0.25 * vb0);
+			im[2 * bT + 1] += dd * ((T)0.25 * vb1);
 		}
-		double cxx, cyy, cxy;
+		T cxx, cyy, cxy;
 		sinv(cxp, cyp, cxx, cyy, cxy);
-		double Dm[2][2] = {{D00, D01}, {D10, D11}};
+		T Dm[2][2] = {{D00, D01}, {D10, D11}};
+		const T q4 = (T)0.25;
 		for(int a = 0; a < 2; a++) {
-			re[2 * a] += 0.25 * Dm[a][0] * cxx;
-			re[2 * a] += 0.25 * Dm[a][1] * cxy;
-			re[2 * a + 1] += 0.25 * Dm[a][0] * cxy;
-			re[2 * a + 1] += 0.25 * Dm[a][1] * cyy;
+			re[2 * a] += q4 * Dm[a][0] * cxx;
+			re[2 * a] += q4 * Dm[a][1] * cxy;
+			re[2 * a + 1] += q4 * Dm[a][0] * cxy;
+			re[2 * a + 1] += q4 * Dm[a][1] * cyy;
 		}
 		for(int b = 0; b < 2; b++) {
-			re[b] += 0.25 * rxx * Dm[0][b];
-			re[b] += 0.25 * rxy * Dm[1][b];
-			re[2 + b] += 0.25 * rxy * Dm[0][b];
-			re[2 + b] += 0.25 * ryy * Dm[1][b];
+			re[b] += q4 * rxx * Dm[0][b];
+			re[b] += q4 * rxy * Dm[1][b];
+			re[2 + b] += q4 * rxy * Dm[0][b];
+			re[2 + b] += q4 * ryy * Dm[1][b];
 		}
 		for(int b = 0; b < 4; b++) out[b] = mk(-hmu * im[b], hmu * re[b]);  // i*hmu*(re+i*im)
 	}
@@ -206,7 +209,8 @@ struct CoefCtx {
 template <typename S>
 __global__ void k_coef(const double* __restrict__ QA, const double* __restrict__ QB,
 		const double* __restrict__ wts, int iz, Geom G, const GroupParams* __restrict__ gps,
-		cx<S>* __restrict__ coef, cx<double>* __restrict__ diag) {
+		cx<S>* __restrict__ coef, cx<S>* __restrict__ diag) {
+	typedef S T;  // arithmetic type of the R coefficients (the phase operator is always FP64)
 	int p = blockIdx.x * blockDim.x + threadIdx.x;
 	int g = blockIdx.y;
 	int N = G.N, Nx = G.Nx, Ny = G.Ny;
@@ -216,7 +220,7 @@ __global__ void k_coef(const double* __restrict__ QA, const double* __restrict__
 	const double* A = QA + (size_t)g * NQ * N;
 	const double* B = QB + (size_t)g * NQ * N;
 	cx<S>* C = coef + (size_t)g * NCOEF * N + p;
-	cx<double>* Dg = diag + (size_t)g * NDIAG * N + p;
+	cx<S>* Dg = diag + (size_t)g * NDIAG * N + p;
 
 	// Phase operator.
 	{
@@ -239,40 +243,40 @@ __global__ void k_coef(const double* __restrict__ QA, const double* __restrict__
 		C[(size_t)(C_PH + 2) * N] = cvt<S>(((e * mk(0.0, 1.0)) * dxy) * sinc);
 	}
 
-	CoefCtx X;
+	CoefCtx<T> X;
 	X.A = A; X.B = B; X.N = N; X.Nx = Nx;
-	X.hmu = gp.dZ / 2.;
+	X.hmu = (T)(gp.dZ / 2.);
 	X.sinv(ix, iy, X.rxx, X.ryy, X.rxy);
 	X.va0 = X.vsum(0, ix, iy);
 	X.va1 = X.vsum(1, ix, iy);
-	const double dX = gp.dX, dY = gp.dY;
-	auto ezz = [&](int x, int y) { int i = x + Nx * y; return (A[Q_IZZ * N + i] + B[Q_IZZ * N + i]) / 2; };
-	double e0 = ezz(ix, iy);
+	const T dX = (T)gp.dX, dY = (T)gp.dY;
+	auto ezz = [&](int x, int y) { int i = x + Nx * y; return (T)((A[Q_IZZ * N + i] + B[Q_IZZ * N + i]) / 2); };
+	T e0 = ezz(ix, iy);
 	int pxq = (ix == Nx - 1) ? 1 : ix + 1, mxq = (ix == 0) ? Nx - 2 : ix - 1;
 	int pyq = (iy == Ny - 1) ? 1 : iy + 1, myq = (iy == 0) ? Ny - 2 : iy - 1;
 	int pxs = (ix == Nx - 2) ? 0 : ix + 1, mxs = (ix == 0) ? Nx - 2 : ix - 1;
 	int pys = (iy == Ny - 2) ? 0 : iy + 1, mys = (iy == 0) ? Ny - 2 : iy - 1;
-	cx<double> r[4];
-	const cx<double> z = mk(0.0, 0.0);
+	cx<T> r[4];
+	const cx<T> z = mk<T>(0, 0);
 
 	// DX: rows ix < Nx-1 when Nx > 3; k = 0 mx, 1 centre, 2 px.
 	{
 		bool ok = Nx > 3 && ix < Nx - 1;
-		double cm = 0, cp = 0, c0 = 0;
+		T cm = 0, cp = 0, c0 = 0;
 		if(ok) {
-			cm = 0.5 * (ezz(mxq, iy) + e0) / (dX * dX);
-			cp = 0.5 * (ezz(pxq, iy) + e0) / (dX * dX);
+			cm = (T)0.5 * (ezz(mxq, iy) + e0) / (dX * dX);
+			cp = (T)0.5 * (ezz(pxq, iy) + e0) / (dX * dX);
 			c0 = -cm - cp;
 		}
 		const int cols[3] = {mxs, ix, pxs};
-		const double c1[3] = {cm, c0, cp};
-		const double L[3] = {1. / (dX * dX), -2. / (dX * dX), 1. / (dX * dX)};
-		const double dd[3] = {-0.5 / dX, 0, 0.5 / dX};
+		const T c1[3] = {cm, c0, cp};
+		const T L[3] = {(T)1 / (dX * dX), (T)-2 / (dX * dX), (T)1 / (dX * dX)};
+		const T dd[3] = {(T)-0.5 / dX, 0, (T)0.5 / dX};
 		for(int k = 0; k < 3; k++) {
 			if(ok) {
 				int cxp = cols[k];
-				double kxx = X.avg(Q_XXTR, cxp, iy), kxy = X.avg(Q_XYTR, cxp, iy);
-				X.entry(c1[k] * kxx, c1[k] * kxy, 0.0, L[k], cxp, iy, dd[k], 0, r);
+				T kxx = X.avg(Q_XXTR, cxp, iy), kxy = X.avg(Q_XYTR, cxp, iy);
+				X.entry(c1[k] * kxx, c1[k] * kxy, (T)0, L[k], cxp, iy, dd[k], 0, r);
 			}
 			else r[0] = r[1] = r[2] = r[3] = z;
 			for(int b = 0; b < 4; b++) C[(size_t)(C_DX + 3 * b + k) * N] = cvt<S>(r[b]);
@@ -283,21 +287,21 @@ __global__ void k_coef(const double* __restrict__ QA, const double* __restrict__
 	// DY: rows iy < Ny-1 when Ny > 3; k = 0 my, 1 centre, 2 py.
 	{
 		bool ok = Ny > 3 && iy < Ny - 1;
-		double cm = 0, cp = 0, c0 = 0;
+		T cm = 0, cp = 0, c0 = 0;
 		if(ok) {
-			cp = 0.5 * (ezz(ix, pyq) + e0) / (dY * dY);
-			cm = 0.5 * (ezz(ix, myq) + e0) / (dY * dY);
+			cp = (T)0.5 * (ezz(ix, pyq) + e0) / (dY * dY);
+			cm = (T)0.5 * (ezz(ix, myq) + e0) / (dY * dY);
 			c0 = -cm - cp;
 		}
 		const int rows[3] = {mys, iy, pys};
-		const double c1[3] = {cm, c0, cp};
-		const double L[3] = {1. / (dY * dY), -2. / (dY * dY), 1. / (dY * dY)};
-		const double dd[3] = {-0.5 / dY, 0, 0.5 / dY};
+		const T c1[3] = {cm, c0, cp};
+		const T L[3] = {(T)1 / (dY * dY), (T)-2 / (dY * dY), (T)1 / (dY * dY)};
+		const T dd[3] = {(T)-0.5 / dY, 0, (T)0.5 / dY};
 		for(int k = 0; k < 3; k++) {
 			if(ok) {
 				int cyp = rows[k];
-				double kyy = X.avg(Q_YYTR, ix, cyp), kxy = X.avg(Q_XYTR, ix, cyp);
-				X.entry(L[k], 0.0, c1[k] * kxy, c1[k] * kyy, ix, cyp, dd[k], 1, r);
+				T kyy = X.avg(Q_YYTR, ix, cyp), kxy = X.avg(Q_XYTR, ix, cyp);
+				X.entry(L[k], (T)0, c1[k] * kxy, c1[k] * kyy, ix, cyp, dd[k], 1, r);
 			}
 			else r[0] = r[1] = r[2] = r[3] = z;
 			for(int b = 0; b < 4; b++) C[(size_t)(C_DY + 3 * b + k) * N] = cvt<S>(r[b]);
@@ -308,22 +312,23 @@ __global__ void k_coef(const double* __restrict__ QA, const double* __restrict__
 	// DXDY: rows ix < Nx-1, iy < Ny-1 when Nx > 3 and Ny > 3; k = pxpy, mxpy, pxmy, mxmy.
 	{
 		bool ok = Nx > 3 && Ny > 3 && ix < Nx - 1 && iy < Ny - 1;
-		double a1 = 0, c1 = 0, a2 = 0, c2 = 0;
+		T a1 = 0, c1 = 0, a2 = 0, c2 = 0;
+		const T q4 = (T)0.25;
 		if(ok) {
-			a1 = 0.25 * ezz(pxq, iy) / (dX * dY); c1 = 0.25 * ezz(mxq, iy) / (dX * dY);
-			a2 = 0.25 * ezz(ix, pyq) / (dX * dY); c2 = 0.25 * ezz(ix, myq) / (dX * dY);
+			a1 = q4 * ezz(pxq, iy) / (dX * dY); c1 = q4 * ezz(mxq, iy) / (dX * dY);
+			a2 = q4 * ezz(ix, pyq) / (dX * dY); c2 = q4 * ezz(ix, myq) / (dX * dY);
 		}
-		const double g0[4] = {-0.25 / (dX * dY), 0.25 / (dX * dY), 0.25 / (dX * dY), -0.25 / (dX * dY)};
-		const double d01[4] = {a1, -c1, -a1, c1};
-		const double d10[4] = {a2, -a2, -c2, c2};
+		const T g0[4] = {-q4 / (dX * dY), q4 / (dX * dY), q4 / (dX * dY), -q4 / (dX * dY)};
+		const T d01[4] = {a1, -c1, -a1, c1};
+		const T d10[4] = {a2, -a2, -c2, c2};
 		const int cxs[4] = {pxs, mxs, pxs, mxs};
 		const int cys[4] = {pys, pys, mys, mys};
 		for(int k = 0; k < 4; k++) {
 			if(ok) {
-				double kxx = X.avg(Q_XXTR, cxs[k], cys[k]), kyy = X.avg(Q_YYTR, cxs[k], cys[k]);
-				double kxy = X.avg(Q_XYTR, cxs[k], cys[k]);
+				T kxx = X.avg(Q_XXTR, cxs[k], cys[k]), kyy = X.avg(Q_YYTR, cxs[k], cys[k]);
+				T kxy = X.avg(Q_XYTR, cxs[k], cys[k]);
 				X.entry(d01[k] * kxy, g0[k] + d01[k] * kyy, g0[k] + d10[k] * kxx, d10[k] * kxy,
-					cxs[k], cys[k], 0.0, 0, r);
+					cxs[k], cys[k], (T)0, 0, r);
 			}
 			else r[0] = r[1] = r[2] = r[3] = z;
 			for(int b = 0; b < 4; b++) C[(size_t)(C_DXDY + 4 * b + k) * N] = cvt<S>(r[b]);
@@ -333,7 +338,7 @@ __global__ void k_coef(const double* __restrict__ QA, const double* __restrict__
 
 // ---------------------------------------------------------------------------------------
 // Pre-factorisation of the periodic line solves (I - mu*R_cc) x = b, one thread per
-// (group, comp, line), FP64. Restates shifted_block_vmult_inv (BlockSparseMatrix.cpp:
+// (group, comp, line), in the plan's precision. Restates shifted_block_vmult_inv (BlockSparseMatrix.cpp:
 // 195-258 and 386-449): Thomas sweep with beta0 = 2*mid0 and the Sherman-Morrison corner
 // vector corr (corr0 = -1/2). Everything that does not depend on the right-hand side is
 // computed here once per (wavelength, slab) and shared by all (q, pol) slots:
@@ -345,11 +350,12 @@ __global__ void k_coef(const double* __restrict__ QA, const double* __restrict__
 // x_{i-1} = d_{i-1} - gamma_{i-1} x_i: both first-order affine recurrences whose
 // coefficients do not depend on b, which is what the chunked solves below exploit.
 // plus per line r0 = inf0/mid0 and rden = 1/(1 + corr0 - r0*corr_{L-2}) in FP64.
-// scr holds FP64 gamma and forward corr: [group][comp][2][N].
+// scr holds gamma and the forward corr: [group][comp][2][N].
 // ---------------------------------------------------------------------------------------
 template <typename S>
-__global__ void k_factor(int dirn, Geom G, int ngroups, int chunkM, const cx<double>* __restrict__ diag,
-		cx<S>* __restrict__ fac, size_t plane, cx<double>* __restrict__ lsc, cx<double>* __restrict__ scr) {
+__global__ void k_factor(int dirn, Geom G, int ngroups, int chunkM, const cx<S>* __restrict__ diag,
+		cx<S>* __restrict__ fac, size_t plane, cx<double>* __restrict__ lsc, cx<S>* __restrict__ scr) {
+	typedef S T;
 	int Nx = G.Nx, Ny = G.Ny, N = G.N;
 	int L = dirn == 0 ? Nx : Ny;
 	int nlines = dirn == 0 ? Ny : Nx;
@@ -358,10 +364,10 @@ __global__ void k_factor(int dirn, Geom G, int ngroups, int chunkM, const cx<dou
 	int line = t % nlines;
 	int c = (t / nlines) % 2;
 	int g = t / (2 * nlines);
-	const cx<double>* Dg = diag + (size_t)g * NDIAG * N + (size_t)(dirn * 6 + c * 3) * N;
+	const cx<T>* Dg = diag + (size_t)g * NDIAG * N + (size_t)(dirn * 6 + c * 3) * N;
 	cx<S>* Fc = fac + ((size_t)g * 2 + c) * NFAC * plane;
-	cx<double>* sG = scr + ((size_t)g * 2 + c) * 2 * N;
-	cx<double>* sC = sG + N;
+	cx<T>* sG = scr + ((size_t)g * 2 + c) * 2 * N;
+	cx<T>* sC = sG + N;
 	cx<double>* ls = lsc + (((size_t)g * 2 + c) * nlines + line) * 2;
 	const int stride = dirn == 0 ? 1 : Nx;
 	const int base = dirn == 0 ? Nx * line : line;
@@ -373,22 +379,22 @@ __global__ void k_factor(int dirn, Geom G, int ngroups, int chunkM, const cx<dou
 		if(chunkM <= 0) return (size_t)P(i);
 		return (size_t)line * 32 * chunkM + (size_t)(i % chunkM) * 32 + (i / chunkM);
 	};
-	const cx<double> one = mk(1.0, 0.0);
+	const cx<T> one = mk<T>(1, 0);
 	auto sup = [&](int i) { return -Dg[2 * (size_t)N + P(i)]; };
 	auto mid = [&](int i) { return one - Dg[1 * (size_t)N + P(i)]; };
 	auto inf = [&](int i) { return -Dg[P(i)]; };
 
-	cx<double> beta = 2.0 * mid(0);
-	cx<double> rb = crecip(beta);
+	cx<T> beta = (T)2 * mid(0);
+	cx<T> rb = crecip(beta);
 	Fc[F_RB * plane + Q(0)] = cvt<S>(rb);
 	Fc[F_A * plane + Q(0)] = mk<S>(0, 0);
-	cx<double> corr = mk(-0.5, 0.0);
+	cx<T> corr = mk<T>(-0.5, 0);
 	sC[P(0)] = corr;
 	for(int i = 1; i < L - 2; i++) {
-		cx<double> gam = sup(i - 1) * rb;
+		cx<T> gam = sup(i - 1) * rb;
 		sG[P(i - 1)] = gam;
 		Fc[F_C * plane + Q(i - 1)] = cvt<S>(-gam);
-		cx<double> in = inf(i);
+		cx<T> in = inf(i);
 		beta = mid(i) - in * gam;
 		rb = crecip(beta);
 		Fc[F_RB * plane + Q(i)] = cvt<S>(rb);
@@ -396,24 +402,24 @@ __global__ void k_factor(int dirn, Geom G, int ngroups, int chunkM, const cx<dou
 		corr = -(in * corr) * rb;
 		sC[P(i)] = corr;
 	}
-	cx<double> gl = sup(L - 3) * rb;
+	cx<T> gl = sup(L - 3) * rb;
 	sG[P(L - 3)] = gl;
 	Fc[F_C * plane + Q(L - 3)] = cvt<S>(-gl);
-	cx<double> inL = inf(L - 2);
+	cx<T> inL = inf(L - 2);
 	beta = mid(L - 2) + cdiv(sup(L - 2) * inf(0), mid(0)) - inL * gl;
 	rb = crecip(beta);
 	Fc[F_RB * plane + Q(L - 2)] = cvt<S>(rb);
 	Fc[F_A * plane + Q(L - 2)] = cvt<S>(-(inL * rb));
-	cx<double> corr_last = (sup(L - 2) - inL * corr) * rb;
+	cx<T> corr_last = (sup(L - 2) - inL * corr) * rb;
 	Fc[F_COR * plane + Q(L - 2)] = cvt<S>(corr_last);
 	Fc[F_C * plane + Q(L - 2)] = mk<S>(0, 0);
-	cx<double> cn = corr_last;
+	cx<T> cn = corr_last;
 	for(int i = L - 2; i > 0; i--) {
-		cx<double> cv = sC[P(i - 1)] - sG[P(i - 1)] * cn;
+		cx<T> cv = sC[P(i - 1)] - sG[P(i - 1)] * cn;
 		Fc[F_COR * plane + Q(i - 1)] = cvt<S>(cv);
 		cn = cv;
 	}
-	cx<double> w = one;
+	cx<T> w = one;
 	Fc[F_W * plane + Q(0)] = cvt<S>(w);
 	for(int i = 1; i < L - 1; i++) {
 		w = -(w * sG[P(i - 1)]);
@@ -429,9 +435,10 @@ __global__ void k_factor(int dirn, Geom G, int ngroups, int chunkM, const cx<dou
 			Fc[F_COR * plane + Q(i)] = mk<S>(0, 0);
 		}
 	}
-	cx<double> r0 = cdiv(inf(0), mid(0));
+	// Sherman-Morrison scalars in FP64
+	cx<double> r0 = cdiv(cvt<double>(inf(0)), cvt<double>(mid(0)));
 	ls[0] = r0;
-	ls[1] = crecip(one + cn - r0 * corr_last);
+	ls[1] = crecip(mk(1.0, 0.0) + cvt<double>(cn) - r0 * cvt<double>(corr_last));
 }
 
 // ---------------------------------------------------------------------------------------
@@ -469,6 +476,62 @@ struct Stencil {
 // with the duplicate-row/column fix-ups of BlockSparseMatrix.cpp folded in analytically).
 enum { ST_EXPL_Y = 0, ST_EXPL_X = 1, ST_WOOD_X = 2, ST_WOOD_Y = 3 };
 
+// One component of a composite stencil step at point (ix, iy). EXPL kinds return
+// f + mu*R f (explicit half-step), WOOD kinds return mu*R_offdiag t (Woodbury right-hand side).
+// (xx, yy) are the indices with the duplicate column / row folded onto column / row 0, which
+// is where the reference's fix-ups copy their values from.
+template <typename R, int KIND>
+__device__ __forceinline__ cx<R> composite(const Stencil<R>& st, int comp, int ix, int iy,
+		const cx<R>* f0, const cx<R>* f1) {
+	const int Nx = st.Nx, Ny = st.Ny;
+	const int xx = ix == Nx - 1 ? 0 : ix, yy = iy == Ny - 1 ? 0 : iy;
+	const bool ax = Nx > 3, ay = Ny > 3;
+	cx<R> T = mk<R>(0, 0);
+	if(KIND == ST_EXPL_Y) {
+		if(comp == 0) {
+			if(ay) T = st.dy(0, ix, yy, f0) + st.dy(1, ix, yy, f1);
+			return f0[ix + Nx * iy] + T;
+		}
+		if(ay) {
+			if(ax) T = st.dy(3, xx, yy, f1) + st.dxdy(3, xx, yy, f1) + st.dy(2, xx, yy, f0) + st.dxdy(2, xx, yy, f0);
+			else T = st.dy(3, ix, yy, f1) + st.dy(2, ix, yy, f0);
+		}
+		return f1[ix + Nx * iy] + T;
+	}
+	if(KIND == ST_EXPL_X) {
+		if(comp == 0) {
+			if(ax) {
+				if(ay) T = st.dx(0, xx, yy, f0) + st.dxdy(0, xx, yy, f0) + st.dx(1, xx, yy, f1) + st.dxdy(1, xx, yy, f1);
+				else T = st.dx(0, xx, iy, f0) + st.dx(1, xx, iy, f1);
+			}
+			return f0[ix + Nx * iy] + T;
+		}
+		if(ax) T = st.dx(3, xx, iy, f1) + st.dx(2, xx, iy, f0);
+		return f1[ix + Nx * iy] + T;
+	}
+	if(KIND == ST_WOOD_X) {
+		if(comp == 0) {
+			if(ax) {
+				if(ay) T = st.dx(1, xx, yy, f1) + st.dxdy(1, xx, yy, f1) + st.dxdy(0, xx, yy, f0);
+				else T = st.dx(1, xx, iy, f1);
+			}
+			return T;
+		}
+		if(ax) T = st.dx(2, xx, iy, f0);
+		return T;
+	}
+	// ST_WOOD_Y
+	if(comp == 0) {
+		if(ay) T = st.dy(1, ix, yy, f1);
+		return T;
+	}
+	if(ay) {
+		if(ax) T = st.dy(2, xx, yy, f0) + st.dxdy(2, xx, yy, f0) + st.dxdy(3, xx, yy, f1);
+		else T = st.dy(2, ix, yy, f0);
+	}
+	return T;
+}
+
 template <typename R, int KIND>
 __global__ void k_stencil(Geom G, int slot0, const cx<R>* __restrict__ coef, const cx<R>* __restrict__ src,
 		cx<R>* __restrict__ dst) {
@@ -481,45 +544,8 @@ __global__ void k_stencil(Geom G, int slot0, const cx<R>* __restrict__ coef, con
 	const cx<R>* f0 = src + (size_t)s * 2 * N;
 	const cx<R>* f1 = f0 + N;
 	int ix = p % Nx, iy = p / Nx;
-	int xx = ix == Nx - 1 ? 0 : ix, yy = iy == Ny - 1 ? 0 : iy;
-	bool ax = Nx > 3, ay = Ny > 3;
-	cx<R> T0 = mk<R>(0, 0), T1 = mk<R>(0, 0);
-	if(KIND == ST_EXPL_Y) {
-		if(ay) {
-			T0 = st.dy(0, ix, yy, f0) + st.dy(1, ix, yy, f1);
-			if(ax) T1 = st.dy(3, xx, yy, f1) + st.dxdy(3, xx, yy, f1) + st.dy(2, xx, yy, f0) + st.dxdy(2, xx, yy, f0);
-			else T1 = st.dy(3, ix, yy, f1) + st.dy(2, ix, yy, f0);
-		}
-		dst[(size_t)s * 2 * N + p] = f0[p] + T0;
-		dst[(size_t)s * 2 * N + N + p] = f1[p] + T1;
-	}
-	else if(KIND == ST_EXPL_X) {
-		if(ax) {
-			if(ay) T0 = st.dx(0, xx, yy, f0) + st.dxdy(0, xx, yy, f0) + st.dx(1, xx, yy, f1) + st.dxdy(1, xx, yy, f1);
-			else T0 = st.dx(0, xx, iy, f0) + st.dx(1, xx, iy, f1);
-			T1 = st.dx(3, xx, iy, f1) + st.dx(2, xx, iy, f0);
-		}
-		dst[(size_t)s * 2 * N + p] = f0[p] + T0;
-		dst[(size_t)s * 2 * N + N + p] = f1[p] + T1;
-	}
-	else if(KIND == ST_WOOD_X) {
-		if(ax) {
-			if(ay) T0 = st.dx(1, xx, yy, f1) + st.dxdy(1, xx, yy, f1) + st.dxdy(0, xx, yy, f0);
-			else T0 = st.dx(1, xx, iy, f1);
-			T1 = st.dx(2, xx, iy, f0);
-		}
-		dst[(size_t)s * 2 * N + p] = T0;
-		dst[(size_t)s * 2 * N + N + p] = T1;
-	}
-	else {
-		if(ay) {
-			T0 = st.dy(1, ix, yy, f1);
-			if(ax) T1 = st.dy(2, xx, yy, f0) + st.dxdy(2, xx, yy, f0) + st.dxdy(3, xx, yy, f1);
-			else T1 = st.dy(2, ix, yy, f0);
-		}
-		dst[(size_t)s * 2 * N + p] = T0;
-		dst[(size_t)s * 2 * N + N + p] = T1;
-	}
+	dst[(size_t)s * 2 * N + p] = composite<R, KIND>(st, 0, ix, iy, f0, f1);
+	dst[(size_t)s * 2 * N + N + p] = composite<R, KIND>(st, 1, ix, iy, f0, f1);
 }
 
 // Periodic line solve with the pre-factored Thomas/Sherman-Morrison data, sequential form:
@@ -600,23 +626,26 @@ __device__ __forceinline__ cx<R> shfl_xor_c(cx<R> v, int m) {
 	return mk<R>(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
 }
 
-// x-line solve, chunked parallel form: one warp per (line, group, comp); lane l owns the
+// x-line solve fused with the right-hand side that precedes it (KIND: explicit y half-step or
+// x Woodbury term), chunked parallel form: one warp per (line, slot, comp); lane l owns the
 // unknowns [l*M, l*M+M) of the line. The forward and backward recurrences are composed per
 // chunk, combined by warp-shuffle scans and replayed, so every sweep is parallel over
 // 32 lanes. The line is staged through shared memory for coalesced global accesses, the
-// factor planes are stored chunk-interleaved (element l*M+k at k*32+l). Each warp loops over
-// every (q, pol) slot of its wavelength group. Block = LT warps = LT consecutive lines.
-template <typename R, int M>
-__global__ void __launch_bounds__(128) k_solve_xc(Geom G, int slot0, int ng, const cx<R>* __restrict__ fac,
-		size_t plane, const cx<double>* __restrict__ lsc, const cx<R>* src, cx<R>* dst,
-		const cx<R>* acc_in, cx<R>* acc_out) {
+// factor planes are stored chunk-interleaved (element l*M+k at k*32+l) and shared through L2
+// by the (q, pol) slots of a wavelength. Block = LT warps = LT consecutive lines of one
+// (slot, comp).
+template <typename R, int M, int KIND>
+__global__ void __launch_bounds__(128) k_solve_xc(Geom G, int slot0, const cx<R>* __restrict__ coef,
+		const cx<R>* __restrict__ fac, size_t plane, const cx<double>* __restrict__ lsc,
+		const cx<R>* __restrict__ src, cx<R>* __restrict__ dst, const cx<R>* acc_in, cx<R>* acc_out) {
 	extern __shared__ unsigned char smem_raw[];
 	const int LT = blockDim.x / 32;
 	const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
 	const int Nx = G.Nx, Ny = G.Ny, N = G.N;
 	const int iy = blockIdx.x * LT + warp;
 	if(iy >= Ny) return;
-	const int g = blockIdx.y / 2, c = blockIdx.y % 2;
+	const int sl = blockIdx.y / 2, c = blockIdx.y % 2;
+	const int g = (slot0 + sl) / G.spg - slot0 / G.spg;
 	const int n_unk = Nx - 1;
 	cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw) + (size_t)warp * 32 * (M + 1);
 	const cx<R>* Fc = fac + ((size_t)g * 2 + c) * NFAC * plane + (size_t)iy * 32 * M;
@@ -625,9 +654,12 @@ __global__ void __launch_bounds__(128) k_solve_xc(Geom G, int slot0, int ng, con
 	const int i0 = lane * M;
 	const int last = n_unk - 1, lane_last = last / M, k_last = last % M;
 	const cx<R> one = mk<R>(1, 0), zero = mk<R>(0, 0);
-	for(int sl = 0; sl < G.spg; sl++) {
-		const size_t off = ((size_t)g * G.spg + sl) * 2 * N + (size_t)c * N + (size_t)iy * Nx;
-		for(int e = lane; e < n_unk; e += 32) buf[(e / M) * (M + 1) + e % M] = src[off + e];
+	{
+		const size_t off = (size_t)sl * 2 * N + (size_t)c * N + (size_t)iy * Nx;
+		const cx<R>* f0 = src + (size_t)sl * 2 * N;
+		const Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
+		for(int e = lane; e < n_unk; e += 32)
+			buf[(e / M) * (M + 1) + e % M] = composite<R, KIND>(st, c, e, iy, f0, f0 + N);
 		__syncwarp();
 		cx<R> v[M];
 		cx<R> A = one, B = zero;
@@ -690,27 +722,28 @@ __global__ void __launch_bounds__(128) k_solve_xc(Geom G, int slot0, int ng, con
 		for(int e = lane; e < Nx; e += 32) {
 			int ee = e == Nx - 1 ? 0 : e;
 			cx<R> x = buf[(ee / M) * (M + 1) + ee % M];
-			dst[off + e] = x;
+			if(dst) dst[off + e] = x;
 			if(acc_out) acc_out[off + e] = acc_in[off + e] + x;
 		}
-		__syncwarp();
 	}
 }
 
-// y-line solve, chunked parallel form: block = 32 adjacent columns (lanes, coalesced) x WY
+// y-line solve fused with its right-hand side (KIND: explicit x half-step or y Woodbury term),
+// chunked parallel form: block = 32 adjacent columns (lanes, coalesced) x WY
 // warps; warp w owns the rows [w*M, w*M+M) of the 32 lines. Chunk maps are combined across
-// warps through shared memory. Each block loops over the (q, pol) slots of its group.
-template <typename R, int M>
-__global__ void __launch_bounds__(1024) k_solve_yc(Geom G, int slot0, int ng, const cx<R>* __restrict__ fac,
-		size_t plane, const cx<double>* __restrict__ lsc, const cx<R>* src, cx<R>* dst,
-		const cx<R>* acc_in, cx<R>* acc_out) {
+// warps through shared memory. One block per (32-column tile, slot, comp).
+template <typename R, int M, int KIND>
+__global__ void __launch_bounds__(1024) k_solve_yc(Geom G, int slot0, const cx<R>* __restrict__ coef,
+		const cx<R>* __restrict__ fac, size_t plane, const cx<double>* __restrict__ lsc,
+		const cx<R>* __restrict__ src, cx<R>* __restrict__ dst, const cx<R>* acc_in, cx<R>* acc_out) {
 	extern __shared__ unsigned char smem_raw[];
 	const int WY = blockDim.y;
 	const int lane = threadIdx.x, w = threadIdx.y;
 	const int Nx = G.Nx, Ny = G.Ny, N = G.N;
 	const int ix = blockIdx.x * 32 + lane;
 	const bool col = ix < Nx;
-	const int g = blockIdx.y / 2, c = blockIdx.y % 2;
+	const int sl = blockIdx.y / 2, c = blockIdx.y % 2;
+	const int g = (slot0 + sl) / G.spg - slot0 / G.spg;
 	const int n_unk = Ny - 1;
 	cx<R>* sA = reinterpret_cast<cx<R>*>(smem_raw);
 	cx<R>* sB = sA + WY * 32;
@@ -726,8 +759,10 @@ __global__ void __launch_bounds__(1024) k_solve_yc(Geom G, int slot0, int ng, co
 		const cx<double>* ls = lsc + (((size_t)g * 2 + c) * Nx + ix) * 2;
 		r0 = ls[0]; rden = ls[1];
 	}
-	for(int sl = 0; sl < G.spg; sl++) {
-		const size_t off = ((size_t)g * G.spg + sl) * 2 * N + (size_t)c * N;
+	{
+		const size_t off = (size_t)sl * 2 * N + (size_t)c * N;
+		const cx<R>* f0 = src + (size_t)sl * 2 * N;
+		const Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
 		cx<R> v[M];
 		cx<R> A = one, B = zero;
 #pragma unroll
@@ -737,7 +772,7 @@ __global__ void __launch_bounds__(1024) k_solve_yc(Geom G, int slot0, int ng, co
 			if(col && i < n_unk) {
 				size_t q = (size_t)ix + (size_t)Nx * i;
 				cx<R> a = Fc[F_A * plane + q];
-				cx<R> b = src[off + q] * Fc[F_RB * plane + q];
+				cx<R> b = composite<R, KIND>(st, c, ix, i, f0, f0 + N) * Fc[F_RB * plane + q];
 				v[k] = b;
 				B = a * B + b;
 				A = a * A;
@@ -804,16 +839,15 @@ __global__ void __launch_bounds__(1024) k_solve_yc(Geom G, int slot0, int ng, co
 				size_t q = (size_t)ix + (size_t)Nx * i;
 				dd = Fc[F_C * plane + q] * dd + v[k];
 				cx<R> x = dd - fr * Fc[F_COR * plane + q];
-				dst[off + q] = x;
+				if(dst) dst[off + q] = x;
 				if(acc_out) acc_out[off + q] = acc_in[off + q] + x;
 				if(i == 0) {
 					size_t qe = (size_t)ix + (size_t)Nx * (Ny - 1);
-					dst[off + qe] = x;
+					if(dst) dst[off + qe] = x;
 					if(acc_out) acc_out[off + qe] = acc_in[off + qe] + x;
 				}
 			}
 		}
-		__syncthreads();
 	}
 }
 
@@ -842,84 +876,123 @@ __device__ __forceinline__ int ref_wrap(int i, int n) {
 }
 
 template <typename R>
-__global__ void k_shift_x(Geom G, int slot0, const ShiftParams* __restrict__ sp, const cx<R>* __restrict__ F,
-		cx<R>* __restrict__ T) {
+__device__ __forceinline__ void phase_apply(const cx<R>* C, size_t N, int p, cx<R>& a, cx<R>& b) {
+	cx<R> oxx = C[(C_PH + 0) * N + p], oyy = C[(C_PH + 1) * N + p], oxy = C[(C_PH + 2) * N + p];
+	cx<R> u = oxx * a + oxy * b, v = oxy * a + oyy * b;
+	a = u;
+	b = v;
+}
+
+// x pass of the shift operator for every slot (q = 0 slots included: their weights are
+// exactly 0/1/0/0 and the pass reduces to the duplicate-column copy), optionally preceded by
+// the phase operator of coefficient set CA applied at each tap: T = X(phase_A(F)).
+template <typename R>
+__global__ void k_shift_x(Geom G, int slot0, const ShiftParams* __restrict__ sp, const cx<R>* __restrict__ CA,
+		const cx<R>* __restrict__ F, cx<R>* __restrict__ T) {
 	int p = blockIdx.x * blockDim.x + threadIdx.x;
 	if(p >= G.N) return;
 	int s = blockIdx.y;
 	int gs = slot0 + s;
+	int g = gs / G.spg - slot0 / G.spg;
 	int gq = (gs / G.spg) * G.Nq + (gs / 2) % G.Nq;
 	const ShiftParams P = sp[gq];
-	if(!P.active) return;
-	int N = G.N, Nx = G.Nx;
+	const size_t N = G.N;
+	const int Nx = G.Nx;
 	int ix = p % Nx, iy = p / Nx;
-	for(int c = 0; c < 2; c++) {
-		const cx<R>* f = F + (size_t)s * 2 * N + (size_t)c * N;
-		cx<R> v;
-		if(Nx > 3) {
-			v = mk<R>(0, 0);
-			for(int k = 0; k < 4; k++)
-				v += (R)P.wx[k] * f[ref_wrap(ix + P.msx - 1 + k, Nx) + Nx * iy];
+	const cx<R>* f = F + (size_t)s * 2 * N;
+	const cx<R>* Cg = CA ? CA + (size_t)g * NCOEF * N : nullptr;
+	cx<R> v0, v1;
+	if(Nx > 3) {
+		v0 = mk<R>(0, 0);
+		v1 = mk<R>(0, 0);
+#pragma unroll
+		for(int k = 0; k < 4; k++) {
+			int q = ref_wrap(ix + P.msx - 1 + k, Nx) + Nx * iy;
+			cx<R> a = f[q], b = f[N + q];
+			if(Cg) phase_apply(Cg, N, q, a, b);
+			v0 += (R)P.wx[k] * a;
+			v1 += (R)P.wx[k] * b;
 		}
-		else v = f[p];
-		T[(size_t)s * 2 * N + (size_t)c * N + p] = v;
 	}
-}
-
-template <typename R>
-__global__ void k_shift_y(Geom G, int slot0, const ShiftParams* __restrict__ sp, const cx<R>* __restrict__ T,
-		cx<R>* __restrict__ F) {
-	int p = blockIdx.x * blockDim.x + threadIdx.x;
-	if(p >= G.N) return;
-	int s = blockIdx.y;
-	int gs = slot0 + s;
-	int gq = (gs / G.spg) * G.Nq + (gs / 2) % G.Nq;
-	const ShiftParams P = sp[gq];
-	if(!P.active) return;
-	int N = G.N, Nx = G.Nx, Ny = G.Ny;
-	int ix = p % Nx, iy = p / Nx;
-	cx<R> ph = mk<R>((R)P.ph_re, (R)P.ph_im);
-	for(int c = 0; c < 2; c++) {
-		const cx<R>* t = T + (size_t)s * 2 * N + (size_t)c * N;
-		cx<R> v;
-		if(Ny > 3) {
-			v = mk<R>(0, 0);
-			for(int k = 0; k < 4; k++)
-				v += (R)P.wy[k] * t[ix + Nx * ref_wrap(iy + P.msy - 1 + k, Ny)];
-		}
-		else v = t[p];
-		F[(size_t)s * 2 * N + (size_t)c * N + p] = v * ph;
-	}
-}
-
-// For q = 0 the shift operator reduces to its periodic wrap: the x pass copies column 0 onto
-// the duplicate column Nx-1, then the y pass copies row 0 onto row Ny-1 (the interpolation
-// weights are exactly 0/1/0/0 and the phase factor is exactly 1). This kernel writes those
-// border values directly; one thread per border point of a (slot, comp) plane.
-template <typename R>
-__global__ void k_sync_dup(Geom G, int slot0, const ShiftParams* __restrict__ sp, cx<R>* F) {
-	int Nx = G.Nx, Ny = G.Ny, N = G.N;
-	int t = blockIdx.x * blockDim.x + threadIdx.x;
-	int nb = (Ny - 1) + (Nx - 1) + 1;
-	if(t >= nb) return;
-	int s = blockIdx.y;
-	int gs = slot0 + s;
-	int gq = (gs / G.spg) * G.Nq + (gs / 2) % G.Nq;
-	if(sp[gq].active) return;
-	bool ax = Nx > 3, ay = Ny > 3;
-	int dst, src = -1;
-	if(t < Ny - 1) { dst = (Nx - 1) + Nx * t; if(ax) src = Nx * t; }
-	else if(t < Ny - 1 + Nx - 1) { int ix = t - (Ny - 1); dst = ix + Nx * (Ny - 1); if(ay) src = ix; }
 	else {
-		dst = (Nx - 1) + Nx * (Ny - 1);
-		if(ax && ay) src = 0;
-		else if(ay) src = Nx - 1;
-		else if(ax) src = Nx * (Ny - 1);
+		v0 = f[p];
+		v1 = f[N + p];
+		if(Cg) phase_apply(Cg, N, p, v0, v1);
 	}
-	if(src < 0 || src == dst) return;
+	T[(size_t)s * 2 * N + p] = v0;
+	T[(size_t)s * 2 * N + N + p] = v1;
+}
+
+// y pass and phase factor of the shift operator, optionally followed by the phase operator
+// of coefficient set CB: F = phase_B(ph * Y(T)).
+template <typename R>
+__global__ void k_shift_y(Geom G, int slot0, const ShiftParams* __restrict__ sp, const cx<R>* __restrict__ CB,
+		const cx<R>* __restrict__ T, cx<R>* __restrict__ F) {
+	int p = blockIdx.x * blockDim.x + threadIdx.x;
+	if(p >= G.N) return;
+	int s = blockIdx.y;
+	int gs = slot0 + s;
+	int g = gs / G.spg - slot0 / G.spg;
+	int gq = (gs / G.spg) * G.Nq + (gs / 2) % G.Nq;
+	const ShiftParams P = sp[gq];
+	const size_t N = G.N;
+	const int Nx = G.Nx, Ny = G.Ny;
+	int ix = p % Nx, iy = p / Nx;
+	const cx<R>* t = T + (size_t)s * 2 * N;
+	cx<R> ph = mk<R>((R)P.ph_re, (R)P.ph_im);
+	cx<R> v0, v1;
+	if(Ny > 3) {
+		v0 = mk<R>(0, 0);
+		v1 = mk<R>(0, 0);
+#pragma unroll
+		for(int k = 0; k < 4; k++) {
+			int q = ix + Nx * ref_wrap(iy + P.msy - 1 + k, Ny);
+			v0 += (R)P.wy[k] * t[q];
+			v1 += (R)P.wy[k] * t[N + q];
+		}
+	}
+	else {
+		v0 = t[p];
+		v1 = t[N + p];
+	}
+	v0 = v0 * ph;
+	v1 = v1 * ph;
+	if(CB) phase_apply(CB + (size_t)g * NCOEF * N, N, p, v0, v1);
+	F[(size_t)s * 2 * N + p] = v0;
+	F[(size_t)s * 2 * N + N + p] = v1;
+}
+
+// All slots at q = 0: phase_A, then the shift operator's duplicate-border copy (column 0 ->
+// column Nx-1, then row 0 -> row Ny-1), then phase_B, in one in-place pass. The thread of a
+// source point also writes the border points copied from it, so no thread reads a value
+// another thread writes.
+template <typename R>
+__global__ void k_phase_sync(Geom G, int slot0, const cx<R>* __restrict__ CA, const cx<R>* __restrict__ CB,
+		cx<R>* F) {
+	int p = blockIdx.x * blockDim.x + threadIdx.x;
+	if(p >= G.N) return;
+	int s = blockIdx.y;
+	int g = (slot0 + s) / G.spg - slot0 / G.spg;
+	const size_t N = G.N;
+	const int Nx = G.Nx, Ny = G.Ny;
+	const bool ax = Nx > 3, ay = Ny > 3;
+	int ix = p % Nx, iy = p / Nx;
+	if((ax && ix == Nx - 1) || (ay && iy == Ny - 1)) return;
 	cx<R>* f = F + (size_t)s * 2 * N;
-	f[dst] = f[src];
-	f[N + dst] = f[N + src];
+	const cx<R>* Ca = CA ? CA + (size_t)g * NCOEF * N : nullptr;
+	const cx<R>* Cb = CB ? CB + (size_t)g * NCOEF * N : nullptr;
+	cx<R> u0 = f[p], u1 = f[N + p];
+	if(Ca) phase_apply(Ca, N, p, u0, u1);
+	auto put = [&](int d) {
+		cx<R> a = u0, b = u1;
+		if(Cb) phase_apply(Cb, N, d, a, b);
+		f[d] = a;
+		f[N + d] = b;
+	};
+	put(p);
+	if(ax && ix == 0) put((Nx - 1) + Nx * iy);
+	if(ay && iy == 0) put(ix + Nx * (Ny - 1));
+	if(ax && ay && ix == 0 && iy == 0) put((Nx - 1) + Nx * (Ny - 1));
 }
 
 // Entrance field: beam profile with polarisation angle pi/2*pol (BPMIteration.cpp:87-109,

@@ -300,15 +300,17 @@ struct Plan : PlanBase {
 		CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
 		smem_limit = (size_t)optin;
 		CK(cudaFuncSetAttribute(k_fft_lines<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit));
-		set_smem_attr<1>(); set_smem_attr<2>(); set_smem_attr<4>(); set_smem_attr<8>();
+		set_smem_attr<2>(); set_smem_attr<4>(); set_smem_attr<8>();
 		set_smem_attr<16>(); set_smem_attr<32>();
 		allocate();
 	}
 
 	template <int M>
 	void set_smem_attr() {
-		CK(cudaFuncSetAttribute(k_solve_xc<R, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit));
-		CK(cudaFuncSetAttribute(k_solve_yc<R, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit));
+		CK(cudaFuncSetAttribute(k_solve_xc<R, M, ST_EXPL_Y>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit));
+		CK(cudaFuncSetAttribute(k_solve_xc<R, M, ST_WOOD_X>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit));
+		CK(cudaFuncSetAttribute(k_solve_yc<R, M, ST_EXPL_X>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit));
+		CK(cudaFuncSetAttribute(k_solve_yc<R, M, ST_WOOD_Y>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit));
 	}
 
 	int gpp(const SampleHost& h) const {
@@ -325,7 +327,7 @@ struct Plan : PlanBase {
 			SolveCfg sc;
 			int ux = h.s.Nx - 1, uy = h.s.Ny - 1;
 			if(h.s.Nx > 3) {
-				for(int M = 1; M <= 32; M *= 2) if(32 * M >= ux) { sc.Mx = M; break; }
+				for(int M = 2; M <= 32; M *= 2) if(32 * M >= ux) { sc.Mx = M; break; }
 			}
 			if(h.s.Ny > 3) {
 				for(int M = 2; M <= 32; M *= 2) if((uy + M - 1) / M <= 16) { sc.My = M; break; }
@@ -337,7 +339,7 @@ struct Plan : PlanBase {
 			scfg.push_back(sc);
 			maxT = std::max(maxT, (size_t)ng * h.spg * 2 * N);
 			maxQ = std::max(maxQ, (size_t)2 * ng * NQ * N);
-			maxC = std::max(maxC, (size_t)ng * NCOEF * N);
+			maxC = std::max(maxC, (size_t)2 * ng * NCOEF * N);  // two slabs (transition kernels)
 			maxD = std::max(maxD, (size_t)ng * NDIAG * N);
 			maxFx = std::max(maxFx, (size_t)ng * 2 * NFAC * std::max(sc.plane_x, sc.plane_y));
 			maxL = std::max(maxL, (size_t)ng * 2 * std::max(h.s.Nx, h.s.Ny) * 2);
@@ -363,12 +365,12 @@ struct Plan : PlanBase {
 		T2.alloc(sizeof(cx<R>) * maxT);
 		Qring.alloc(sizeof(double) * maxQ);
 		coef.alloc(sizeof(cx<R>) * maxC);
-		diag.alloc(sizeof(cx<double>) * maxD);
+		diag.alloc(sizeof(cx<R>) * maxD);
 		facx.alloc(sizeof(cx<R>) * maxFx);
 		facy.alloc(sizeof(cx<R>) * maxFx);
 		lscx.alloc(sizeof(cx<double>) * maxL);
 		lscy.alloc(sizeof(cx<double>) * maxL);
-		scr.alloc(sizeof(cx<double>) * maxScr);
+		scr.alloc(sizeof(cx<R>) * maxScr);
 		stage.alloc(sizeof(cx<double>) * maxStage);
 		dev_bytes += T.bytes + T2.bytes + Qring.bytes + coef.bytes + diag.bytes + facx.bytes + facy.bytes +
 			lscx.bytes + lscy.bytes + scr.bytes + stage.bytes;
@@ -492,8 +494,8 @@ struct Plan : PlanBase {
 			double* Q0 = Qring.as<double>();
 			double* Q1 = Q0 + (size_t)ng * NQ * N;
 			double* Qr[2] = {Q0, Q1};
-			cx<R>* C = coef.as<cx<R>>();
-			cx<double>* Dg = diag.as<cx<double>>();
+			cx<R>* Cring[2] = {coef.as<cx<R>>(), coef.as<cx<R>>() + (size_t)ng * NCOEF * N};
+			cx<R>* Dg = diag.as<cx<R>>();
 			const double eps_bytes = (double)N * ng * (h.fd * 8 + (mk_ ? 1 : 0) + NQ * 8);
 			const double field_pts = (double)N * nsl;
 
@@ -512,37 +514,34 @@ struct Plan : PlanBase {
 					k_copy<R><<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, h.E0.as<cx<R>>() + (size_t)slot0 * 2 * N, Fp);
 				});
 			}
+			const cx<R>* Cprev = nullptr;
 			for(int iz = 0; iz < Nz - 1; iz++) {
 				double* QA = Qr[iz & 1];
 				double* QB = Qr[(iz + 1) & 1];
+				cx<R>* C = Cring[iz & 1];
 				launch("eps_plane", eps_bytes, [&] {
 					k_eps_plane<<<pgrid(N, ng), 256, 0, stream>>>(h.dir.as<double>(), h.fd, mk_, N, iz + 1, gps, QB);
 				});
-				launch("coef", (double)N * ng * (2 * NQ * 8 + NCOEF * sc + NDIAG * 16 + (wts ? 16 : 0)), [&] {
+				launch("coef", (double)N * ng * (2 * NQ * 8 + NCOEF * sc + NDIAG * sc + (wts ? 16 : 0)), [&] {
 					k_coef<R><<<pgrid(N, ng, 128), 128, 0, stream>>>(QA, QB, wts, iz, Gm, gps, C, Dg);
 				});
 				int lx = ng * 2 * Ny, ly = ng * 2 * Nx;
-				const double fb = (double)N * ng * 2 * (3 * 16 + NFAC * sc + 4 * 16);
+				const double fb = (double)N * ng * 2 * (3 * sc + NFAC * sc + 4 * sc);
 				const SolveCfg& scf = scfg[h.index];
 				launch("factor_x", fb, [&] {
 					k_factor<R><<<(lx + 63) / 64, 64, 0, stream>>>(0, Gm, ng, scf.Mx, Dg, facx.as<cx<R>>(), scf.plane_x,
-						lscx.as<cx<double>>(), scr.as<cx<double>>());
+						lscx.as<cx<double>>(), scr.as<cx<R>>());
 				});
 				launch("factor_y", fb, [&] {
 					k_factor<R><<<(ly + 63) / 64, 64, 0, stream>>>(1, Gm, ng, 0, Dg, facy.as<cx<R>>(), scf.plane_y,
-						lscy.as<cx<double>>(), scr.as<cx<double>>());
+						lscy.as<cx<double>>(), scr.as<cx<R>>());
 				});
-				// shift -> phase -> ADI -> phase -> shift (BPMIteration.cpp:133-146)
-				rec_shift(h, slot0, nsl, Fp, T2b);
-				launch("phase", field_pts * 4 * sc + (double)N * ng * 3 * sc, [&] {
-					k_phase<R><<<pgrid(N, nsl), 256, 0, stream>>>(Gm, slot0, C, Fp);
-				});
+				// [phase(iz-1)] shift(iz-1) | shift(iz) phase(iz)   (BPMIteration.cpp:133-146)
+				rec_transition(h, slot0, nsl, Cprev, C, Fp, Tb, T2b, iz > 0);
 				rec_adi(h, Gm, slot0, nsl, ng, Nw, C, Fp, Tb, T2b);
-				launch("phase", field_pts * 4 * sc + (double)N * ng * 3 * sc, [&] {
-					k_phase<R><<<pgrid(N, nsl), 256, 0, stream>>>(Gm, slot0, C, Fp);
-				});
-				rec_shift(h, slot0, nsl, Fp, T2b);
+				Cprev = C;
 			}
+			if(Nz > 1) rec_transition(h, slot0, nsl, Cprev, nullptr, Fp, Tb, T2b, false);
 			launch("fresnel_out", field_pts * 4 * sc + (double)N * ng * 3 * 8, [&] {
 				k_fresnel_out<R><<<pgrid(N, nsl), 256, 0, stream>>>(Gm, slot0, gps, Qr[(Nz - 1) & 1], Fp);
 			});
@@ -557,87 +556,115 @@ struct Plan : PlanBase {
 		fft2(h, F, nplanes, +1);
 	}
 
-	// SimpleShiftOperator::apply for every slot: interpolation kernels for tilted slots, the
-	// duplicate-border copy for q = 0 slots.
-	void rec_shift(SampleHost& h, int slot0, int nsl, cx<R>* Fp, cx<R>* T2b) {
+	// Between the Strang half-steps of consecutive slabs: phase(CA) -> shift -> [shift] ->
+	// phase(CB), with CA / CB the coefficient sets of the previous / current slab (null: no
+	// phase) and two_shifts selecting shift(iz-1) followed by shift(iz). If every slot is at
+	// q = 0 the shifts reduce to the duplicate-border copy and the whole transition is one pass.
+	void rec_transition(SampleHost& h, int slot0, int nsl, const cx<R>* CA, const cx<R>* CB, cx<R>* Fp,
+			cx<R>* Tb, cx<R>* T2b, bool two_shifts) {
 		const Geom Gm = h.geom;
 		const double sc = sizeof(cx<R>);
-		if(h.any_shift) {
-			launch("shift_x", (double)Gm.N * nsl * 4 * sc, [&] {
-				k_shift_x<R><<<pgrid(Gm.N, nsl), 256, 0, stream>>>(Gm, slot0, h.shiftd.as<ShiftParams>(), Fp, T2b);
+		const double fpb = (double)Gm.N * nsl * 4 * sc;
+		const ShiftParams* sp = h.shiftd.as<ShiftParams>();
+		if(!h.any_shift) {
+			launch("phase_sync", fpb, [&] {
+				k_phase_sync<R><<<pgrid(Gm.N, nsl), 256, 0, stream>>>(Gm, slot0, CA, CB, Fp);
 			});
-			launch("shift_y", (double)Gm.N * nsl * 4 * sc, [&] {
-				k_shift_y<R><<<pgrid(Gm.N, nsl), 256, 0, stream>>>(Gm, slot0, h.shiftd.as<ShiftParams>(), T2b, Fp);
+			return;
+		}
+		launch("shift_x", fpb, [&] {
+			k_shift_x<R><<<pgrid(Gm.N, nsl), 256, 0, stream>>>(Gm, slot0, sp, CA, Fp, T2b);
+		});
+		if(two_shifts) {
+			launch("shift_y", fpb, [&] {
+				k_shift_y<R><<<pgrid(Gm.N, nsl), 256, 0, stream>>>(Gm, slot0, sp, nullptr, T2b, Tb);
+			});
+			launch("shift_x", fpb, [&] {
+				k_shift_x<R><<<pgrid(Gm.N, nsl), 256, 0, stream>>>(Gm, slot0, sp, nullptr, Tb, T2b);
 			});
 		}
-		if(h.any_zero_q) {
-			int nb = Gm.Nx + Gm.Ny - 1;
-			launch("sync_dup", (double)nb * nsl * 4 * sc, [&] {
-				k_sync_dup<R><<<dim3((unsigned)((nb + 127) / 128), (unsigned)nsl), 128, 0, stream>>>(Gm, slot0,
-					h.shiftd.as<ShiftParams>(), Fp);
-			});
-		}
+		launch("shift_y", fpb, [&] {
+			k_shift_y<R><<<pgrid(Gm.N, nsl), 256, 0, stream>>>(Gm, slot0, sp, CB, T2b, Fp);
+		});
 	}
 
-	template <int M>
-	void launch_xc(const Geom& Gm, int slot0, int ng, const SolveCfg& sc, const cx<R>* src, cx<R>* dst,
-			const cx<R>* ai, cx<R>* ao) {
+	template <int M, int KIND>
+	void launch_xc(const Geom& Gm, int slot0, int nsl, const SolveCfg& sc, const cx<R>* C, const cx<R>* src,
+			cx<R>* dst, const cx<R>* ai, cx<R>* ao) {
 		const int LT = 4;
 		size_t smem = (size_t)LT * 32 * (M + 1) * sizeof(cx<R>);
-		dim3 grid((unsigned)((Gm.Ny + LT - 1) / LT), (unsigned)(ng * 2));
-		k_solve_xc<R, M><<<grid, 32 * LT, smem, stream>>>(Gm, slot0, ng, facx.as<cx<R>>(), sc.plane_x,
+		dim3 grid((unsigned)((Gm.Ny + LT - 1) / LT), (unsigned)(nsl * 2));
+		k_solve_xc<R, M, KIND><<<grid, 32 * LT, smem, stream>>>(Gm, slot0, C, facx.as<cx<R>>(), sc.plane_x,
 			lscx.as<cx<double>>(), src, dst, ai, ao);
 	}
-	template <int M>
-	void launch_yc(const Geom& Gm, int slot0, int ng, const SolveCfg& sc, const cx<R>* src, cx<R>* dst,
-			const cx<R>* ai, cx<R>* ao) {
+	template <int M, int KIND>
+	void launch_yc(const Geom& Gm, int slot0, int nsl, const SolveCfg& sc, const cx<R>* C, const cx<R>* src,
+			cx<R>* dst, const cx<R>* ai, cx<R>* ao) {
 		size_t smem = (size_t)(5 * sc.WY * 32 + 2 * 32) * sizeof(cx<R>);
-		dim3 grid((unsigned)((Gm.Nx + 31) / 32), (unsigned)(ng * 2));
-		k_solve_yc<R, M><<<grid, dim3(32, sc.WY), smem, stream>>>(Gm, slot0, ng, facy.as<cx<R>>(), sc.plane_y,
+		dim3 grid((unsigned)((Gm.Nx + 31) / 32), (unsigned)(nsl * 2));
+		k_solve_yc<R, M, KIND><<<grid, dim3(32, sc.WY), smem, stream>>>(Gm, slot0, C, facy.as<cx<R>>(), sc.plane_y,
 			lscy.as<cx<double>>(), src, dst, ai, ao);
 	}
+	template <int KIND>
+	void dispatch_xc(int M, const Geom& Gm, int slot0, int nsl, const SolveCfg& sc, const cx<R>* C,
+			const cx<R>* src, cx<R>* dst, const cx<R>* ai, cx<R>* ao) {
+		switch(M) {
+			case 2: launch_xc<2, KIND>(Gm, slot0, nsl, sc, C, src, dst, ai, ao); break;
+			case 4: launch_xc<4, KIND>(Gm, slot0, nsl, sc, C, src, dst, ai, ao); break;
+			case 8: launch_xc<8, KIND>(Gm, slot0, nsl, sc, C, src, dst, ai, ao); break;
+			case 16: launch_xc<16, KIND>(Gm, slot0, nsl, sc, C, src, dst, ai, ao); break;
+			default: launch_xc<32, KIND>(Gm, slot0, nsl, sc, C, src, dst, ai, ao); break;
+		}
+	}
+	template <int KIND>
+	void dispatch_yc(int M, const Geom& Gm, int slot0, int nsl, const SolveCfg& sc, const cx<R>* C,
+			const cx<R>* src, cx<R>* dst, const cx<R>* ai, cx<R>* ao) {
+		switch(M) {
+			case 2: launch_yc<2, KIND>(Gm, slot0, nsl, sc, C, src, dst, ai, ao); break;
+			case 4: launch_yc<4, KIND>(Gm, slot0, nsl, sc, C, src, dst, ai, ao); break;
+			case 8: launch_yc<8, KIND>(Gm, slot0, nsl, sc, C, src, dst, ai, ao); break;
+			case 16: launch_yc<16, KIND>(Gm, slot0, nsl, sc, C, src, dst, ai, ao); break;
+			default: launch_yc<32, KIND>(Gm, slot0, nsl, sc, C, src, dst, ai, ao); break;
+		}
+	}
 
-	void rec_solve(int dirn, SampleHost& h, const Geom& Gm, int slot0, int nsl, int ng, const cx<R>* src, cx<R>* dst,
-			const cx<R>* acc_in, cx<R>* acc_out) {
+	// Sequential line solve (lines too long for the chunked kernels).
+	void rec_solve_seq(int dirn, SampleHost& h, const Geom& Gm, int slot0, int nsl, int ng, const cx<R>* src,
+			cx<R>* dst, const cx<R>* acc_in, cx<R>* acc_out) {
 		const SolveCfg& sc = scfg[h.index];
 		int nlines = dirn == 0 ? Gm.Ny : Gm.Nx;
 		int nt = nsl * 2 * nlines;
 		const double sz = sizeof(cx<R>);
 		double bytes = (double)Gm.N * nsl * 2 * sz * (acc_out ? 4 : 2) + (double)Gm.N * ng * 2 * NFAC * sz;
-		int M = dirn == 0 ? sc.Mx : sc.My;
-		if(M == 0) {
-			if(dirn == 0)
-				launch("solve_x", bytes, [&] {
-					k_solve<R, 0><<<(nt + 127) / 128, 128, 0, stream>>>(Gm, slot0, nsl, facx.as<cx<R>>(), sc.plane_x,
-						lscx.as<cx<double>>(), src, dst, acc_in, acc_out);
-				});
-			else
-				launch("solve_y", bytes, [&] {
-					k_solve<R, 1><<<(nt + 127) / 128, 128, 0, stream>>>(Gm, slot0, nsl, facy.as<cx<R>>(), sc.plane_y,
-						lscy.as<cx<double>>(), src, dst, acc_in, acc_out);
-				});
-			return;
-		}
 		if(dirn == 0)
 			launch("solve_x", bytes, [&] {
-				switch(M) {
-					case 1: launch_xc<1>(Gm, slot0, ng, sc, src, dst, acc_in, acc_out); break;
-					case 2: launch_xc<2>(Gm, slot0, ng, sc, src, dst, acc_in, acc_out); break;
-					case 4: launch_xc<4>(Gm, slot0, ng, sc, src, dst, acc_in, acc_out); break;
-					case 8: launch_xc<8>(Gm, slot0, ng, sc, src, dst, acc_in, acc_out); break;
-					case 16: launch_xc<16>(Gm, slot0, ng, sc, src, dst, acc_in, acc_out); break;
-					default: launch_xc<32>(Gm, slot0, ng, sc, src, dst, acc_in, acc_out); break;
-				}
+				k_solve<R, 0><<<(nt + 127) / 128, 128, 0, stream>>>(Gm, slot0, nsl, facx.as<cx<R>>(), sc.plane_x,
+					lscx.as<cx<double>>(), src, dst, acc_in, acc_out);
 			});
 		else
 			launch("solve_y", bytes, [&] {
-				switch(M) {
-					case 2: launch_yc<2>(Gm, slot0, ng, sc, src, dst, acc_in, acc_out); break;
-					case 4: launch_yc<4>(Gm, slot0, ng, sc, src, dst, acc_in, acc_out); break;
-					case 8: launch_yc<8>(Gm, slot0, ng, sc, src, dst, acc_in, acc_out); break;
-					case 16: launch_yc<16>(Gm, slot0, ng, sc, src, dst, acc_in, acc_out); break;
-					default: launch_yc<32>(Gm, slot0, ng, sc, src, dst, acc_in, acc_out); break;
-				}
+				k_solve<R, 1><<<(nt + 127) / 128, 128, 0, stream>>>(Gm, slot0, nsl, facy.as<cx<R>>(), sc.plane_y,
+					lscy.as<cx<double>>(), src, dst, acc_in, acc_out);
+			});
+	}
+
+	// Fused right-hand side + chunked line solve. wood = false: explicit half-step of the other
+	// direction; wood = true: Woodbury term. dst may be null (t not needed afterwards).
+	void rec_solve_fused(int dirn, bool wood, SampleHost& h, const Geom& Gm, int slot0, int nsl, int ng,
+			const cx<R>* C, const cx<R>* src, cx<R>* dst, const cx<R>* acc_in, cx<R>* acc_out) {
+		const SolveCfg& sc = scfg[h.index];
+		const double sz = sizeof(cx<R>);
+		double fp = (double)Gm.N * nsl * 2 * sz;
+		double bytes = fp * (1 + (dst ? 1 : 0) + (acc_out ? 2 : 0)) + (double)Gm.N * ng * (2 * NFAC + (wood ? 14 : 20)) * sz;
+		if(dirn == 0)
+			launch(wood ? "wood_solve_x" : "expl_solve_x", bytes, [&] {
+				if(wood) dispatch_xc<ST_WOOD_X>(sc.Mx, Gm, slot0, nsl, sc, C, src, dst, acc_in, acc_out);
+				else dispatch_xc<ST_EXPL_Y>(sc.Mx, Gm, slot0, nsl, sc, C, src, dst, acc_in, acc_out);
+			});
+		else
+			launch(wood ? "wood_solve_y" : "expl_solve_y", bytes, [&] {
+				if(wood) dispatch_yc<ST_WOOD_Y>(sc.My, Gm, slot0, nsl, sc, C, src, dst, acc_in, acc_out);
+				else dispatch_yc<ST_EXPL_X>(sc.My, Gm, slot0, nsl, sc, C, src, dst, acc_in, acc_out);
 			});
 	}
 
@@ -648,17 +675,25 @@ struct Plan : PlanBase {
 		const double sc = sizeof(cx<R>);
 		dim3 gr = pgrid(N, nsl);
 		const double fp = (double)N * nsl;
+		const SolveCfg& cfg = scfg[h.index];
 		for(int dirn = 0; dirn < 2; dirn++) {
-			// explicit half-step in the other direction, then implicit solve + Woodbury
-			if(dirn == 0)
-				launch("expl_y", fp * 4 * sc + (double)N * ng * 20 * sc, [&] {
-					k_stencil<R, ST_EXPL_Y><<<gr, 256, 0, stream>>>(Gm, slot0, C, Fp, T2b);
-				});
-			else
-				launch("expl_x", fp * 4 * sc + (double)N * ng * 20 * sc, [&] {
-					k_stencil<R, ST_EXPL_X><<<gr, 256, 0, stream>>>(Gm, slot0, C, Fp, T2b);
-				});
-			rec_solve(dirn, h, Gm, slot0, nsl, ng, T2b, Tb, nullptr, nullptr);
+			bool fused = (dirn == 0 ? cfg.Mx : cfg.My) > 0;
+			if(fused) {
+				// t0 = solve(f + mu R f) written to T; Woodbury: t_k = solve(mu R' t_{k-1}),
+				// F = t0 + t1 + ... accumulated by the solves (the last t_k is not stored).
+				rec_solve_fused(dirn, false, h, Gm, slot0, nsl, ng, C, Fp, Tb, nullptr, nullptr);
+			}
+			else {
+				if(dirn == 0)
+					launch("expl_y", fp * 4 * sc + (double)N * ng * 20 * sc, [&] {
+						k_stencil<R, ST_EXPL_Y><<<gr, 256, 0, stream>>>(Gm, slot0, C, Fp, T2b);
+					});
+				else
+					launch("expl_x", fp * 4 * sc + (double)N * ng * 20 * sc, [&] {
+						k_stencil<R, ST_EXPL_X><<<gr, 256, 0, stream>>>(Gm, slot0, C, Fp, T2b);
+					});
+				rec_solve_seq(dirn, h, Gm, slot0, nsl, ng, T2b, Tb, nullptr, nullptr);
+			}
 			cx<R>* cur = Tb;
 			cx<R>* oth = T2b;
 			if(Nw == 0) {
@@ -668,19 +703,24 @@ struct Plan : PlanBase {
 				});
 			}
 			for(int it = 1; it <= Nw; it++) {
-				if(dirn == 0)
-					launch("wood_x", fp * 4 * sc + (double)N * ng * 14 * sc, [&] {
-						k_stencil<R, ST_WOOD_X><<<gr, 256, 0, stream>>>(Gm, slot0, C, cur, oth);
-					});
-				else
-					launch("wood_y", fp * 4 * sc + (double)N * ng * 14 * sc, [&] {
-						k_stencil<R, ST_WOOD_Y><<<gr, 256, 0, stream>>>(Gm, slot0, C, cur, oth);
-					});
-				rec_solve(dirn, h, Gm, slot0, nsl, ng, oth, oth, it == 1 ? Tb : Fp, Fp);
+				const cx<R>* ai = it == 1 ? Tb : Fp;
+				if(fused) {
+					rec_solve_fused(dirn, true, h, Gm, slot0, nsl, ng, C, cur, it == Nw ? nullptr : oth, ai, Fp);
+				}
+				else {
+					if(dirn == 0)
+						launch("wood_x", fp * 4 * sc + (double)N * ng * 14 * sc, [&] {
+							k_stencil<R, ST_WOOD_X><<<gr, 256, 0, stream>>>(Gm, slot0, C, cur, oth);
+						});
+					else
+						launch("wood_y", fp * 4 * sc + (double)N * ng * 14 * sc, [&] {
+							k_stencil<R, ST_WOOD_Y><<<gr, 256, 0, stream>>>(Gm, slot0, C, cur, oth);
+						});
+					rec_solve_seq(dirn, h, Gm, slot0, nsl, ng, oth, oth, ai, Fp);
+				}
 				std::swap(cur, oth);
 			}
 		}
-		(void)h;
 	}
 
 	// One eager execution with events around every launch; per-kernel totals.
