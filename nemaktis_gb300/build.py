@@ -11,8 +11,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libnbpm.so")
-SOURCES = ["nbpm.cu"]
-HEADERS = ["bpm_kernels.cuh", "fft_kernels.cuh", "cplx.cuh", "host_settings.h", "host_expr.h", "host_json.h"]
+SOURCES = ["nbpm.cu", "solve_x_f32.cu", "solve_x_f64.cu", "solve_y_f32.cu", "solve_y_f64.cu"]
+HEADERS = ["bpm_kernels.cuh", "fft_kernels.cuh", "cplx.cuh", "host_settings.h", "host_expr.h", "host_json.h",
+           "solve_dispatch.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -33,16 +34,26 @@ def _stale():
 
 
 def build(force=False, verbose=False, extra=()):
-    """Build libnbpm.so if it is missing or older than its sources; returns its path."""
+    """Build libnbpm.so if it is missing or older than its sources; returns its path.
+
+    The translation units compile in parallel (one nvcc process each), then link."""
     if not force and not _stale():
         return LIB
     os.makedirs(BUILD, exist_ok=True)
+    flags = ["-O3", "-std=c++17", *ARCH, "-lineinfo", "-Xcompiler", "-fPIC,-fopenmp", *extra]
+    procs, objs = [], []
+    for f in SOURCES:
+        obj = os.path.join(BUILD, f.replace(".cu", ".o"))
+        cmd = [nvcc(), *flags, "-c", "-o", obj, os.path.join(CSRC, f)]
+        if verbose:
+            print(" ".join(cmd))
+        procs.append((f, subprocess.Popen(cmd)))
+        objs.append(obj)
+    bad = [f for f, p in procs if p.wait() != 0]
+    if bad:
+        raise RuntimeError("nvcc failed for " + ", ".join(bad))
     tmp = LIB + ".tmp%d" % os.getpid()
-    cmd = [nvcc(), "-O3", "-std=c++17", *ARCH, "-lineinfo", "-Xcompiler", "-fPIC,-fopenmp",
-           "-shared", "-o", tmp, *[os.path.join(CSRC, f) for f in SOURCES], "-lgomp", *extra]
-    if verbose:
-        print(" ".join(cmd))
-    subprocess.run(cmd, check=True)
+    subprocess.run([nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lgomp"], check=True)
     os.replace(tmp, LIB)
     return LIB
 

@@ -94,7 +94,7 @@ __device__ __forceinline__ double neff_of(double xxtr, double yytr, double xytr)
 }
 
 // One transverse plane of derived quantities for every group of the pass.
-__global__ void k_eps_plane(const double* __restrict__ dir, int fd, const uint8_t* __restrict__ mask,
+static __global__ void k_eps_plane(const double* __restrict__ dir, int fd, const uint8_t* __restrict__ mask,
 		int N, int iz, const GroupParams* __restrict__ gps, double* __restrict__ out) {
 	int p = blockIdx.x * blockDim.x + threadIdx.x;
 	int g = blockIdx.y;
@@ -121,7 +121,7 @@ __global__ void k_eps_plane(const double* __restrict__ dir, int fd, const uint8_
 
 // Partial sums of neff over the volume for nref (PermittivityTensorField.cpp:183-211),
 // in a fixed block order so the reduction is deterministic.
-__global__ void k_neff_partial(const double* __restrict__ dir, int fd, const uint8_t* __restrict__ mask,
+static __global__ void k_neff_partial(const double* __restrict__ dir, int fd, const uint8_t* __restrict__ mask,
 		size_t nvox, const GroupParams* __restrict__ gps, double* __restrict__ partial) {
 	__shared__ double sh[256];
 	int g = blockIdx.y;
@@ -470,6 +470,45 @@ struct Stencil {
 		return c(base, p) * s[px + Nx * py] + c(base + 1, p) * s[mx + Nx * py] +
 			c(base + 2, p) * s[px + Nx * my] + c(base + 3, p) * s[mx + Nx * my];
 	}
+	// Multi-slot forms: the same stencil coefficients applied to KS fields (slot planes
+	// ss apart), accumulated into out[].
+	template <int KS>
+	__device__ __forceinline__ void dx_m(int b, int x, int y, const cx<R>* s, size_t ss, cx<R>* out) const {
+		int p = x + Nx * y;
+		int mx = x == 0 ? Nx - 2 : x - 1, px = x == Nx - 2 ? 0 : x + 1;
+		int base = C_DX + 3 * b;
+		cx<R> c0 = c(base, p), c1 = c(base + 1, p), c2 = c(base + 2, p);
+#pragma unroll
+		for(int j = 0; j < KS; j++) {
+			const cx<R>* f = s + j * ss;
+			out[j] += c0 * f[mx + Nx * y] + c1 * f[p] + c2 * f[px + Nx * y];
+		}
+	}
+	template <int KS>
+	__device__ __forceinline__ void dy_m(int b, int x, int y, const cx<R>* s, size_t ss, cx<R>* out) const {
+		int p = x + Nx * y;
+		int my = y == 0 ? Ny - 2 : y - 1, py = y == Ny - 2 ? 0 : y + 1;
+		int base = C_DY + 3 * b;
+		cx<R> c0 = c(base, p), c1 = c(base + 1, p), c2 = c(base + 2, p);
+#pragma unroll
+		for(int j = 0; j < KS; j++) {
+			const cx<R>* f = s + j * ss;
+			out[j] += c0 * f[x + Nx * my] + c1 * f[p] + c2 * f[x + Nx * py];
+		}
+	}
+	template <int KS>
+	__device__ __forceinline__ void dxdy_m(int b, int x, int y, const cx<R>* s, size_t ss, cx<R>* out) const {
+		int p = x + Nx * y;
+		int mx = x == 0 ? Nx - 2 : x - 1, px = x == Nx - 2 ? 0 : x + 1;
+		int my = y == 0 ? Ny - 2 : y - 1, py = y == Ny - 2 ? 0 : y + 1;
+		int base = C_DXDY + 4 * b;
+		cx<R> c0 = c(base, p), c1 = c(base + 1, p), c2 = c(base + 2, p), c3 = c(base + 3, p);
+#pragma unroll
+		for(int j = 0; j < KS; j++) {
+			const cx<R>* f = s + j * ss;
+			out[j] += c0 * f[px + Nx * py] + c1 * f[mx + Nx * py] + c2 * f[px + Nx * my] + c3 * f[mx + Nx * my];
+		}
+	}
 };
 
 // Step kinds of the composite stencil kernel (ParaxialPrimaryEvolutionOperator.cpp:153-207
@@ -530,6 +569,82 @@ __device__ __forceinline__ cx<R> composite(const Stencil<R>& st, int comp, int i
 		else T = st.dy(2, ix, yy, f0);
 	}
 	return T;
+}
+
+// composite() for KS consecutive slots at once (f0: comp-0 plane of the first slot, slot
+// planes 2N apart, comp-1 plane at +N); every stencil coefficient is loaded once.
+template <typename R, int KIND, int KS>
+__device__ __forceinline__ void composite_m(const Stencil<R>& st, int comp, int ix, int iy, const cx<R>* f0,
+		cx<R>* out) {
+	const int Nx = st.Nx, Ny = st.Ny;
+	const size_t N = st.N, ss = 2 * N;
+	const cx<R>* f1 = f0 + N;
+	const int xx = ix == Nx - 1 ? 0 : ix, yy = iy == Ny - 1 ? 0 : iy;
+	const bool ax = Nx > 3, ay = Ny > 3;
+	const int p = ix + Nx * iy;
+#pragma unroll
+	for(int j = 0; j < KS; j++) out[j] = mk<R>(0, 0);
+	if(KIND == ST_EXPL_Y) {
+		if(comp == 0) {
+			if(ay) { st.template dy_m<KS>(0, ix, yy, f0, ss, out); st.template dy_m<KS>(1, ix, yy, f1, ss, out); }
+#pragma unroll
+			for(int j = 0; j < KS; j++) out[j] += f0[j * ss + p];
+			return;
+		}
+		if(ay) {
+			if(ax) {
+				st.template dy_m<KS>(3, xx, yy, f1, ss, out); st.template dxdy_m<KS>(3, xx, yy, f1, ss, out);
+				st.template dy_m<KS>(2, xx, yy, f0, ss, out); st.template dxdy_m<KS>(2, xx, yy, f0, ss, out);
+			}
+			else { st.template dy_m<KS>(3, ix, yy, f1, ss, out); st.template dy_m<KS>(2, ix, yy, f0, ss, out); }
+		}
+#pragma unroll
+		for(int j = 0; j < KS; j++) out[j] += f1[j * ss + p];
+		return;
+	}
+	if(KIND == ST_EXPL_X) {
+		if(comp == 0) {
+			if(ax) {
+				if(ay) {
+					st.template dx_m<KS>(0, xx, yy, f0, ss, out); st.template dxdy_m<KS>(0, xx, yy, f0, ss, out);
+					st.template dx_m<KS>(1, xx, yy, f1, ss, out); st.template dxdy_m<KS>(1, xx, yy, f1, ss, out);
+				}
+				else { st.template dx_m<KS>(0, xx, iy, f0, ss, out); st.template dx_m<KS>(1, xx, iy, f1, ss, out); }
+			}
+#pragma unroll
+			for(int j = 0; j < KS; j++) out[j] += f0[j * ss + p];
+			return;
+		}
+		if(ax) { st.template dx_m<KS>(3, xx, iy, f1, ss, out); st.template dx_m<KS>(2, xx, iy, f0, ss, out); }
+#pragma unroll
+		for(int j = 0; j < KS; j++) out[j] += f1[j * ss + p];
+		return;
+	}
+	if(KIND == ST_WOOD_X) {
+		if(comp == 0) {
+			if(ax) {
+				if(ay) {
+					st.template dx_m<KS>(1, xx, yy, f1, ss, out); st.template dxdy_m<KS>(1, xx, yy, f1, ss, out);
+					st.template dxdy_m<KS>(0, xx, yy, f0, ss, out);
+				}
+				else st.template dx_m<KS>(1, xx, iy, f1, ss, out);
+			}
+			return;
+		}
+		if(ax) st.template dx_m<KS>(2, xx, iy, f0, ss, out);
+		return;
+	}
+	if(comp == 0) {
+		if(ay) st.template dy_m<KS>(1, ix, yy, f1, ss, out);
+		return;
+	}
+	if(ay) {
+		if(ax) {
+			st.template dy_m<KS>(2, xx, yy, f0, ss, out); st.template dxdy_m<KS>(2, xx, yy, f0, ss, out);
+			st.template dxdy_m<KS>(3, xx, yy, f1, ss, out);
+		}
+		else st.template dy_m<KS>(2, ix, yy, f0, ss, out);
+	}
 }
 
 template <typename R, int KIND>
@@ -627,15 +742,15 @@ __device__ __forceinline__ cx<R> shfl_xor_c(cx<R> v, int m) {
 }
 
 // x-line solve fused with the right-hand side that precedes it (KIND: explicit y half-step or
-// x Woodbury term), chunked parallel form: one warp per (line, slot, comp); lane l owns the
-// unknowns [l*M, l*M+M) of the line. The forward and backward recurrences are composed per
-// chunk, combined by warp-shuffle scans and replayed, so every sweep is parallel over
-// 32 lanes. The line is staged through shared memory for coalesced global accesses, the
-// factor planes are stored chunk-interleaved (element l*M+k at k*32+l) and shared through L2
-// by the (q, pol) slots of a wavelength. Block = LT warps = LT consecutive lines of one
-// (slot, comp).
-template <typename R, int M, int KIND>
-__global__ void __launch_bounds__(128) k_solve_xc(Geom G, int slot0, const cx<R>* __restrict__ coef,
+// x Woodbury term), chunked parallel form: one warp per (line, comp, KS slots of one
+// wavelength); lane l owns the unknowns [l*M, l*M+M) of the line. The forward and backward
+// recurrences are composed per chunk, combined by warp-shuffle scans and replayed, so every
+// sweep is parallel over 32 lanes. The right-hand side is formed with each stencil
+// coefficient loaded once for the KS slots and staged through shared memory so that global
+// accesses stay coalesced; the factor planes are stored chunk-interleaved (element l*M+k at
+// k*32+l) and are also loaded once for the KS slots. Block = LT warps = LT lines.
+template <typename R, int M, int KIND, int KS>
+__global__ void __launch_bounds__(128) k_solve_xc(Geom G, int slot0, int nch, const cx<R>* __restrict__ coef,
 		const cx<R>* __restrict__ fac, size_t plane, const cx<double>* __restrict__ lsc,
 		const cx<R>* __restrict__ src, cx<R>* __restrict__ dst, const cx<R>* acc_in, cx<R>* acc_out) {
 	extern __shared__ unsigned char smem_raw[];
@@ -644,84 +759,127 @@ __global__ void __launch_bounds__(128) k_solve_xc(Geom G, int slot0, const cx<R>
 	const int Nx = G.Nx, Ny = G.Ny, N = G.N;
 	const int iy = blockIdx.x * LT + warp;
 	if(iy >= Ny) return;
-	const int sl = blockIdx.y / 2, c = blockIdx.y % 2;
-	const int g = (slot0 + sl) / G.spg - slot0 / G.spg;
+	const int c = blockIdx.y % 2, bc = blockIdx.y / 2;
+	const int g = bc / nch, ch = bc % nch;
+	const int s0 = g * G.spg + ch * KS;  // first slot (pass-relative)
 	const int n_unk = Nx - 1;
-	cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw) + (size_t)warp * 32 * (M + 1);
+	const int PITCH = 32 * (M + 1);
+	cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw) + (size_t)warp * KS * PITCH;
 	const cx<R>* Fc = fac + ((size_t)g * 2 + c) * NFAC * plane + (size_t)iy * 32 * M;
 	const cx<double>* ls = lsc + (((size_t)g * 2 + c) * Ny + iy) * 2;
 	const cx<double> r0 = ls[0], rden = ls[1];
 	const int i0 = lane * M;
 	const int last = n_unk - 1, lane_last = last / M, k_last = last % M;
 	const cx<R> one = mk<R>(1, 0), zero = mk<R>(0, 0);
-	{
-		const size_t off = (size_t)sl * 2 * N + (size_t)c * N + (size_t)iy * Nx;
-		const cx<R>* f0 = src + (size_t)sl * 2 * N;
-		const Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
-		for(int e = lane; e < n_unk; e += 32)
-			buf[(e / M) * (M + 1) + e % M] = composite<R, KIND>(st, c, e, iy, f0, f0 + N);
-		__syncwarp();
-		cx<R> v[M];
-		cx<R> A = one, B = zero;
+	const Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
+	const cx<R>* f0 = src + (size_t)s0 * 2 * N;
+	for(int e = lane; e < n_unk; e += 32) {
+		cx<R> r[KS];
+		composite_m<R, KIND, KS>(st, c, e, iy, f0, r);
 #pragma unroll
-		for(int k = 0; k < M; k++) {
-			v[k] = zero;
-			if(i0 + k < n_unk) {
-				cx<R> a = Fc[F_A * plane + k * 32 + lane];
-				cx<R> b = buf[lane * (M + 1) + k] * Fc[F_RB * plane + k * 32 + lane];
-				v[k] = b;
-				B = a * B + b;
-				A = a * A;
+		for(int j = 0; j < KS; j++) buf[j * PITCH + (e / M) * (M + 1) + e % M] = r[j];
+	}
+	__syncwarp();
+	cx<R> v[KS][M];
+	cx<R> A[KS], B[KS];
+#pragma unroll
+	for(int j = 0; j < KS; j++) { A[j] = one; B[j] = zero; }
+#pragma unroll
+	for(int k = 0; k < M; k++) {
+		bool ok = i0 + k < n_unk;
+		cx<R> a = zero, rb = zero;
+		if(ok) { a = Fc[F_A * plane + k * 32 + lane]; rb = Fc[F_RB * plane + k * 32 + lane]; }
+#pragma unroll
+		for(int j = 0; j < KS; j++) {
+			v[j][k] = zero;
+			if(ok) {
+				cx<R> b = buf[j * PITCH + lane * (M + 1) + k] * rb;
+				v[j][k] = b;
+				B[j] = a * B[j] + b;
+				A[j] = a * A[j];
 			}
 		}
+	}
 #pragma unroll
-		for(int o = 1; o < 32; o <<= 1) {
-			cx<R> Ap = shfl_up_c(A, o), Bp = shfl_up_c(B, o);
-			if(lane >= o) { B = A * Bp + B; A = A * Ap; }
+	for(int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+		for(int j = 0; j < KS; j++) {
+			cx<R> Ap = shfl_up_c(A[j], o), Bp = shfl_up_c(B[j], o);
+			if(lane >= o) { B[j] = A[j] * Bp + B[j]; A[j] = A[j] * Ap; }
 		}
-		cx<R> d = shfl_up_c(B, 1);
-		if(lane == 0) d = zero;
-		cx<R> acc = zero, dl = zero;
+	}
+	cx<R> d[KS], acc[KS], dl[KS];
 #pragma unroll
-		for(int k = 0; k < M; k++) {
-			if(i0 + k < n_unk) {
-				d = Fc[F_A * plane + k * 32 + lane] * d + v[k];
-				v[k] = d;
-				acc += Fc[F_W * plane + k * 32 + lane] * d;
-			}
-			if(k == k_last) dl = d;
-		}
+	for(int j = 0; j < KS; j++) {
+		d[j] = shfl_up_c(B[j], 1);
+		if(lane == 0) d[j] = zero;
+		acc[j] = zero;
+		dl[j] = zero;
+	}
 #pragma unroll
-		for(int o = 16; o > 0; o >>= 1) acc += shfl_xor_c(acc, o);
-		dl = shfl_idx_c(dl, lane_last);
-		const cx<R> fr = cvt<R>((cvt<double>(acc) - r0 * cvt<double>(dl)) * rden);
-		A = one; B = zero;
+	for(int k = 0; k < M; k++) {
+		if(i0 + k < n_unk) {
+			cx<R> a = Fc[F_A * plane + k * 32 + lane], w = Fc[F_W * plane + k * 32 + lane];
 #pragma unroll
-		for(int k = M - 1; k >= 0; k--) {
-			if(i0 + k < n_unk) {
-				cx<R> cc = Fc[F_C * plane + k * 32 + lane];
-				B = cc * B + v[k];
-				A = cc * A;
+			for(int j = 0; j < KS; j++) {
+				d[j] = a * d[j] + v[j][k];
+				v[j][k] = d[j];
+				acc[j] += w * d[j];
 			}
 		}
+		if(k == k_last) {
 #pragma unroll
-		for(int o = 1; o < 32; o <<= 1) {
-			cx<R> An = shfl_down_c(A, o), Bn = shfl_down_c(B, o);
-			if(lane + o < 32) { B = A * Bn + B; A = A * An; }
+			for(int j = 0; j < KS; j++) dl[j] = d[j];
 		}
-		cx<R> dd = shfl_down_c(B, 1);
-		if(lane == 31) dd = zero;
+	}
+	cx<R> fr[KS];
 #pragma unroll
-		for(int k = M - 1; k >= 0; k--) {
-			if(i0 + k < n_unk) {
-				dd = Fc[F_C * plane + k * 32 + lane] * dd + v[k];
-				buf[lane * (M + 1) + k] = dd - fr * Fc[F_COR * plane + k * 32 + lane];
+	for(int j = 0; j < KS; j++) {
+#pragma unroll
+		for(int o = 16; o > 0; o >>= 1) acc[j] += shfl_xor_c(acc[j], o);
+		dl[j] = shfl_idx_c(dl[j], lane_last);
+		fr[j] = cvt<R>((cvt<double>(acc[j]) - r0 * cvt<double>(dl[j])) * rden);
+		A[j] = one;
+		B[j] = zero;
+	}
+#pragma unroll
+	for(int k = M - 1; k >= 0; k--) {
+		if(i0 + k < n_unk) {
+			cx<R> cc = Fc[F_C * plane + k * 32 + lane];
+#pragma unroll
+			for(int j = 0; j < KS; j++) { B[j] = cc * B[j] + v[j][k]; A[j] = cc * A[j]; }
+		}
+	}
+#pragma unroll
+	for(int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+		for(int j = 0; j < KS; j++) {
+			cx<R> An = shfl_down_c(A[j], o), Bn = shfl_down_c(B[j], o);
+			if(lane + o < 32) { B[j] = A[j] * Bn + B[j]; A[j] = A[j] * An; }
+		}
+	}
+#pragma unroll
+	for(int j = 0; j < KS; j++) {
+		d[j] = shfl_down_c(B[j], 1);
+		if(lane == 31) d[j] = zero;
+	}
+#pragma unroll
+	for(int k = M - 1; k >= 0; k--) {
+		if(i0 + k < n_unk) {
+			cx<R> cc = Fc[F_C * plane + k * 32 + lane], cr = Fc[F_COR * plane + k * 32 + lane];
+#pragma unroll
+			for(int j = 0; j < KS; j++) {
+				d[j] = cc * d[j] + v[j][k];
+				buf[j * PITCH + lane * (M + 1) + k] = d[j] - fr[j] * cr;
 			}
 		}
-		__syncwarp();
+	}
+	__syncwarp();
+	for(int j = 0; j < KS; j++) {
+		const size_t off = (size_t)(s0 + j) * 2 * N + (size_t)c * N + (size_t)iy * Nx;
 		for(int e = lane; e < Nx; e += 32) {
 			int ee = e == Nx - 1 ? 0 : e;
-			cx<R> x = buf[(ee / M) * (M + 1) + ee % M];
+			cx<R> x = buf[j * PITCH + (ee / M) * (M + 1) + ee % M];
 			if(dst) dst[off + e] = x;
 			if(acc_out) acc_out[off + e] = acc_in[off + e] + x;
 		}
@@ -729,11 +887,11 @@ __global__ void __launch_bounds__(128) k_solve_xc(Geom G, int slot0, const cx<R>
 }
 
 // y-line solve fused with its right-hand side (KIND: explicit x half-step or y Woodbury term),
-// chunked parallel form: block = 32 adjacent columns (lanes, coalesced) x WY
-// warps; warp w owns the rows [w*M, w*M+M) of the 32 lines. Chunk maps are combined across
-// warps through shared memory. One block per (32-column tile, slot, comp).
-template <typename R, int M, int KIND>
-__global__ void __launch_bounds__(1024) k_solve_yc(Geom G, int slot0, const cx<R>* __restrict__ coef,
+// chunked parallel form: block = 32 adjacent columns (lanes, coalesced) x WY warps for KS
+// slots of one wavelength; warp w owns the rows [w*M, w*M+M) of the 32 lines for all KS
+// slots. Chunk maps are combined across warps through shared memory.
+template <typename R, int M, int KIND, int KS>
+__global__ void __launch_bounds__(512) k_solve_yc(Geom G, int slot0, int nch, const cx<R>* __restrict__ coef,
 		const cx<R>* __restrict__ fac, size_t plane, const cx<double>* __restrict__ lsc,
 		const cx<R>* __restrict__ src, cx<R>* __restrict__ dst, const cx<R>* acc_in, cx<R>* acc_out) {
 	extern __shared__ unsigned char smem_raw[];
@@ -742,103 +900,131 @@ __global__ void __launch_bounds__(1024) k_solve_yc(Geom G, int slot0, const cx<R
 	const int Nx = G.Nx, Ny = G.Ny, N = G.N;
 	const int ix = blockIdx.x * 32 + lane;
 	const bool col = ix < Nx;
-	const int sl = blockIdx.y / 2, c = blockIdx.y % 2;
-	const int g = (slot0 + sl) / G.spg - slot0 / G.spg;
+	const int c = blockIdx.y % 2, bc = blockIdx.y / 2;
+	const int g = bc / nch, ch = bc % nch;
+	const int s0 = g * G.spg + ch * KS;
 	const int n_unk = Ny - 1;
-	cx<R>* sA = reinterpret_cast<cx<R>*>(smem_raw);
-	cx<R>* sB = sA + WY * 32;
-	cx<R>* sD = sB + WY * 32;
-	cx<R>* sP = sD + WY * 32;
-	cx<R>* sL = sP + WY * 32;
-	cx<R>* sF = sL + 32;
+	const int SZ = WY * 32;
+	cx<R>* sA = reinterpret_cast<cx<R>*>(smem_raw);  // [KS][WY][32]
+	cx<R>* sB = sA + KS * SZ;
+	cx<R>* sD = sB + KS * SZ;
+	cx<R>* sP = sD + KS * SZ;
+	cx<R>* sL = sP + KS * SZ;                         // [KS][32]
+	cx<R>* sF = sL + KS * 32;                         // [KS][32]
 	const cx<R>* Fc = fac + ((size_t)g * 2 + c) * NFAC * plane;
 	const int i0 = w * M;
 	const cx<R> one = mk<R>(1, 0), zero = mk<R>(0, 0);
 	cx<double> r0 = mk(0.0, 0.0), rden = mk(0.0, 0.0);
 	if(col) {
 		const cx<double>* ls = lsc + (((size_t)g * 2 + c) * Nx + ix) * 2;
-		r0 = ls[0]; rden = ls[1];
+		r0 = ls[0];
+		rden = ls[1];
 	}
-	{
-		const size_t off = (size_t)sl * 2 * N + (size_t)c * N;
-		const cx<R>* f0 = src + (size_t)sl * 2 * N;
-		const Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
-		cx<R> v[M];
-		cx<R> A = one, B = zero;
+	const Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
+	const cx<R>* f0 = src + (size_t)s0 * 2 * N;
+	cx<R> v[KS][M];
+	cx<R> A[KS], B[KS];
 #pragma unroll
-		for(int k = 0; k < M; k++) {
-			v[k] = zero;
-			int i = i0 + k;
-			if(col && i < n_unk) {
-				size_t q = (size_t)ix + (size_t)Nx * i;
-				cx<R> a = Fc[F_A * plane + q];
-				cx<R> b = composite<R, KIND>(st, c, ix, i, f0, f0 + N) * Fc[F_RB * plane + q];
-				v[k] = b;
-				B = a * B + b;
-				A = a * A;
+	for(int j = 0; j < KS; j++) { A[j] = one; B[j] = zero; }
+#pragma unroll
+	for(int k = 0; k < M; k++) {
+		int i = i0 + k;
+		bool ok = col && i < n_unk;
+#pragma unroll
+		for(int j = 0; j < KS; j++) v[j][k] = zero;
+		if(ok) {
+			size_t q = (size_t)ix + (size_t)Nx * i;
+			cx<R> a = Fc[F_A * plane + q], rb = Fc[F_RB * plane + q];
+			cx<R> r[KS];
+			composite_m<R, KIND, KS>(st, c, ix, i, f0, r);
+#pragma unroll
+			for(int j = 0; j < KS; j++) {
+				cx<R> b = r[j] * rb;
+				v[j][k] = b;
+				B[j] = a * B[j] + b;
+				A[j] = a * A[j];
 			}
 		}
-		sA[w * 32 + lane] = A;
-		sB[w * 32 + lane] = B;
-		__syncthreads();
-		if(w == 0) {
+	}
+#pragma unroll
+	for(int j = 0; j < KS; j++) { sA[j * SZ + w * 32 + lane] = A[j]; sB[j * SZ + w * 32 + lane] = B[j]; }
+	__syncthreads();
+	if(w == 0) {
+		for(int j = 0; j < KS; j++) {
 			cx<R> D = zero;
 			for(int ww = 0; ww < WY; ww++) {
-				sD[ww * 32 + lane] = D;
-				D = sA[ww * 32 + lane] * D + sB[ww * 32 + lane];
+				sD[j * SZ + ww * 32 + lane] = D;
+				D = sA[j * SZ + ww * 32 + lane] * D + sB[j * SZ + ww * 32 + lane];
 			}
 		}
-		__syncthreads();
-		cx<R> d = sD[w * 32 + lane];
-		cx<R> acc = zero;
+	}
+	__syncthreads();
+	cx<R> d[KS], acc[KS];
 #pragma unroll
-		for(int k = 0; k < M; k++) {
-			int i = i0 + k;
-			if(col && i < n_unk) {
-				size_t q = (size_t)ix + (size_t)Nx * i;
-				d = Fc[F_A * plane + q] * d + v[k];
-				v[k] = d;
-				acc += Fc[F_W * plane + q] * d;
-				if(i == n_unk - 1) sL[lane] = d;
+	for(int j = 0; j < KS; j++) { d[j] = sD[j * SZ + w * 32 + lane]; acc[j] = zero; }
+#pragma unroll
+	for(int k = 0; k < M; k++) {
+		int i = i0 + k;
+		if(col && i < n_unk) {
+			size_t q = (size_t)ix + (size_t)Nx * i;
+			cx<R> a = Fc[F_A * plane + q], wv = Fc[F_W * plane + q];
+#pragma unroll
+			for(int j = 0; j < KS; j++) {
+				d[j] = a * d[j] + v[j][k];
+				v[j][k] = d[j];
+				acc[j] += wv * d[j];
+				if(i == n_unk - 1) sL[j * 32 + lane] = d[j];
 			}
 		}
-		sP[w * 32 + lane] = acc;
-		__syncthreads();
-		if(w == 0) {
+	}
+#pragma unroll
+	for(int j = 0; j < KS; j++) sP[j * SZ + w * 32 + lane] = acc[j];
+	__syncthreads();
+	if(w == 0) {
+		for(int j = 0; j < KS; j++) {
 			cx<R> tot = zero;
-			for(int ww = 0; ww < WY; ww++) tot += sP[ww * 32 + lane];
-			sF[lane] = cvt<R>((cvt<double>(tot) - r0 * cvt<double>(sL[lane])) * rden);
+			for(int ww = 0; ww < WY; ww++) tot += sP[j * SZ + ww * 32 + lane];
+			sF[j * 32 + lane] = cvt<R>((cvt<double>(tot) - r0 * cvt<double>(sL[j * 32 + lane])) * rden);
 		}
-		A = one; B = zero;
+	}
 #pragma unroll
-		for(int k = M - 1; k >= 0; k--) {
-			int i = i0 + k;
-			if(col && i < n_unk) {
-				cx<R> cc = Fc[F_C * plane + (size_t)ix + (size_t)Nx * i];
-				B = cc * B + v[k];
-				A = cc * A;
-			}
+	for(int j = 0; j < KS; j++) { A[j] = one; B[j] = zero; }
+#pragma unroll
+	for(int k = M - 1; k >= 0; k--) {
+		int i = i0 + k;
+		if(col && i < n_unk) {
+			cx<R> cc = Fc[F_C * plane + (size_t)ix + (size_t)Nx * i];
+#pragma unroll
+			for(int j = 0; j < KS; j++) { B[j] = cc * B[j] + v[j][k]; A[j] = cc * A[j]; }
 		}
-		sA[w * 32 + lane] = A;
-		sB[w * 32 + lane] = B;
-		__syncthreads();
-		if(w == 0) {
+	}
+#pragma unroll
+	for(int j = 0; j < KS; j++) { sA[j * SZ + w * 32 + lane] = A[j]; sB[j * SZ + w * 32 + lane] = B[j]; }
+	__syncthreads();
+	if(w == 0) {
+		for(int j = 0; j < KS; j++) {
 			cx<R> D = zero;
 			for(int ww = WY - 1; ww >= 0; ww--) {
-				sD[ww * 32 + lane] = D;
-				D = sA[ww * 32 + lane] * D + sB[ww * 32 + lane];
+				sD[j * SZ + ww * 32 + lane] = D;
+				D = sA[j * SZ + ww * 32 + lane] * D + sB[j * SZ + ww * 32 + lane];
 			}
 		}
-		__syncthreads();
-		const cx<R> fr = sF[lane];
-		cx<R> dd = sD[w * 32 + lane];
+	}
+	__syncthreads();
+	cx<R> fr[KS];
 #pragma unroll
-		for(int k = M - 1; k >= 0; k--) {
-			int i = i0 + k;
-			if(col && i < n_unk) {
-				size_t q = (size_t)ix + (size_t)Nx * i;
-				dd = Fc[F_C * plane + q] * dd + v[k];
-				cx<R> x = dd - fr * Fc[F_COR * plane + q];
+	for(int j = 0; j < KS; j++) { fr[j] = sF[j * 32 + lane]; d[j] = sD[j * SZ + w * 32 + lane]; }
+#pragma unroll
+	for(int k = M - 1; k >= 0; k--) {
+		int i = i0 + k;
+		if(col && i < n_unk) {
+			size_t q = (size_t)ix + (size_t)Nx * i;
+			cx<R> cc = Fc[F_C * plane + q], cr = Fc[F_COR * plane + q];
+#pragma unroll
+			for(int j = 0; j < KS; j++) {
+				d[j] = cc * d[j] + v[j][k];
+				cx<R> x = d[j] - fr[j] * cr;
+				size_t off = (size_t)(s0 + j) * 2 * N + (size_t)c * N;
 				if(dst) dst[off + q] = x;
 				if(acc_out) acc_out[off + q] = acc_in[off + q] + x;
 				if(i == 0) {

@@ -23,6 +23,7 @@
 #include "bpm_kernels.cuh"
 #include "fft_kernels.cuh"
 #include "host_settings.h"
+#include "solve_dispatch.cuh"
 
 namespace nbpm {
 
@@ -192,7 +193,7 @@ struct Plan : PlanBase {
 	double last_slab_ms = 0;
 	size_t smem_limit = 0;
 	// line-solve configuration per sample (chunk sizes of the parallel kernels; 0 = sequential)
-	struct SolveCfg { int Mx = 0, My = 0, WY = 0; size_t plane_x = 0, plane_y = 0; };
+	struct SolveCfg { int Mx = 0, My = 0, WY = 0, KSx = 1, KSy = 1; size_t plane_x = 0, plane_y = 0; };
 	std::vector<SolveCfg> scfg;
 
 	Plan(const nbpm_options& o) : opt(o) {
@@ -300,17 +301,10 @@ struct Plan : PlanBase {
 		CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
 		smem_limit = (size_t)optin;
 		CK(cudaFuncSetAttribute(k_fft_lines<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit));
-		set_smem_attr<2>(); set_smem_attr<4>(); set_smem_attr<8>();
-		set_smem_attr<16>(); set_smem_attr<32>();
+		if(sizeof(R) == sizeof(float)) { set_solve_smem_x_f32((int)smem_limit); set_solve_smem_y_f32((int)smem_limit); }
+		else { set_solve_smem_x_f64((int)smem_limit); set_solve_smem_y_f64((int)smem_limit); }
+		CK(cudaGetLastError());
 		allocate();
-	}
-
-	template <int M>
-	void set_smem_attr() {
-		CK(cudaFuncSetAttribute(k_solve_xc<R, M, ST_EXPL_Y>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit));
-		CK(cudaFuncSetAttribute(k_solve_xc<R, M, ST_WOOD_X>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit));
-		CK(cudaFuncSetAttribute(k_solve_yc<R, M, ST_EXPL_X>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit));
-		CK(cudaFuncSetAttribute(k_solve_yc<R, M, ST_WOOD_Y>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit));
 	}
 
 	int gpp(const SampleHost& h) const {
@@ -330,10 +324,22 @@ struct Plan : PlanBase {
 				for(int M = 2; M <= 32; M *= 2) if(32 * M >= ux) { sc.Mx = M; break; }
 			}
 			if(h.s.Ny > 3) {
+				// block of 32 columns x WY <= 16 warps (<= 512 threads, <= 128 registers)
 				for(int M = 2; M <= 32; M *= 2) if((uy + M - 1) / M <= 16) { sc.My = M; break; }
-				if(!sc.My && (uy + 31) / 32 <= 32) sc.My = 32;
 				if(sc.My) sc.WY = (uy + sc.My - 1) / sc.My;
 			}
+			// slots per thread: largest KS dividing 2*Nq with a compiled (M, KS) instance
+			// per-thread chunk values (M*KS complex) kept within 32 FP32 / 16 FP64 complex registers
+			const int cap = sizeof(R) == sizeof(float) ? 32 : 16;
+			auto pick_ks = [&](int M) {
+				for(int ks : {4, 2, 1})
+					if(h.spg % ks == 0 && solve_pair_ok(M, ks) && (M * ks <= cap || ks == 1)) return ks;
+				return 0;
+			};
+			if(sc.Mx) { sc.KSx = pick_ks(sc.Mx); if(!sc.KSx) sc.Mx = 0; }
+			if(sc.My) { sc.KSy = pick_ks(sc.My); if(!sc.KSy) { sc.My = 0; sc.WY = 0; } }
+			if(opt.verbose)
+				std::printf("line solves: x M=%d KS=%d, y M=%d WY=%d KS=%d\n", sc.Mx, sc.KSx, sc.My, sc.WY, sc.KSy);
 			sc.plane_x = sc.Mx ? std::max(N, (size_t)h.s.Ny * 32 * sc.Mx) : N;
 			sc.plane_y = N;
 			scfg.push_back(sc);
@@ -588,46 +594,6 @@ struct Plan : PlanBase {
 		});
 	}
 
-	template <int M, int KIND>
-	void launch_xc(const Geom& Gm, int slot0, int nsl, const SolveCfg& sc, const cx<R>* C, const cx<R>* src,
-			cx<R>* dst, const cx<R>* ai, cx<R>* ao) {
-		const int LT = 4;
-		size_t smem = (size_t)LT * 32 * (M + 1) * sizeof(cx<R>);
-		dim3 grid((unsigned)((Gm.Ny + LT - 1) / LT), (unsigned)(nsl * 2));
-		k_solve_xc<R, M, KIND><<<grid, 32 * LT, smem, stream>>>(Gm, slot0, C, facx.as<cx<R>>(), sc.plane_x,
-			lscx.as<cx<double>>(), src, dst, ai, ao);
-	}
-	template <int M, int KIND>
-	void launch_yc(const Geom& Gm, int slot0, int nsl, const SolveCfg& sc, const cx<R>* C, const cx<R>* src,
-			cx<R>* dst, const cx<R>* ai, cx<R>* ao) {
-		size_t smem = (size_t)(5 * sc.WY * 32 + 2 * 32) * sizeof(cx<R>);
-		dim3 grid((unsigned)((Gm.Nx + 31) / 32), (unsigned)(nsl * 2));
-		k_solve_yc<R, M, KIND><<<grid, dim3(32, sc.WY), smem, stream>>>(Gm, slot0, C, facy.as<cx<R>>(), sc.plane_y,
-			lscy.as<cx<double>>(), src, dst, ai, ao);
-	}
-	template <int KIND>
-	void dispatch_xc(int M, const Geom& Gm, int slot0, int nsl, const SolveCfg& sc, const cx<R>* C,
-			const cx<R>* src, cx<R>* dst, const cx<R>* ai, cx<R>* ao) {
-		switch(M) {
-			case 2: launch_xc<2, KIND>(Gm, slot0, nsl, sc, C, src, dst, ai, ao); break;
-			case 4: launch_xc<4, KIND>(Gm, slot0, nsl, sc, C, src, dst, ai, ao); break;
-			case 8: launch_xc<8, KIND>(Gm, slot0, nsl, sc, C, src, dst, ai, ao); break;
-			case 16: launch_xc<16, KIND>(Gm, slot0, nsl, sc, C, src, dst, ai, ao); break;
-			default: launch_xc<32, KIND>(Gm, slot0, nsl, sc, C, src, dst, ai, ao); break;
-		}
-	}
-	template <int KIND>
-	void dispatch_yc(int M, const Geom& Gm, int slot0, int nsl, const SolveCfg& sc, const cx<R>* C,
-			const cx<R>* src, cx<R>* dst, const cx<R>* ai, cx<R>* ao) {
-		switch(M) {
-			case 2: launch_yc<2, KIND>(Gm, slot0, nsl, sc, C, src, dst, ai, ao); break;
-			case 4: launch_yc<4, KIND>(Gm, slot0, nsl, sc, C, src, dst, ai, ao); break;
-			case 8: launch_yc<8, KIND>(Gm, slot0, nsl, sc, C, src, dst, ai, ao); break;
-			case 16: launch_yc<16, KIND>(Gm, slot0, nsl, sc, C, src, dst, ai, ao); break;
-			default: launch_yc<32, KIND>(Gm, slot0, nsl, sc, C, src, dst, ai, ao); break;
-		}
-	}
-
 	// Sequential line solve (lines too long for the chunked kernels).
 	void rec_solve_seq(int dirn, SampleHost& h, const Geom& Gm, int slot0, int nsl, int ng, const cx<R>* src,
 			cx<R>* dst, const cx<R>* acc_in, cx<R>* acc_out) {
@@ -656,16 +622,33 @@ struct Plan : PlanBase {
 		const double sz = sizeof(cx<R>);
 		double fp = (double)Gm.N * nsl * 2 * sz;
 		double bytes = fp * (1 + (dst ? 1 : 0) + (acc_out ? 2 : 0)) + (double)Gm.N * ng * (2 * NFAC + (wood ? 14 : 20)) * sz;
-		if(dirn == 0)
+		SolveLaunch L;
+		L.stream = stream;
+		if(dirn == 0) {
+			const int LT = 4;
+			L.M = sc.Mx; L.KS = sc.KSx; L.kind = wood ? ST_WOOD_X : ST_EXPL_Y;
+			int nch = h.spg / L.KS;
+			L.grid = dim3((unsigned)((Gm.Ny + LT - 1) / LT), (unsigned)(ng * nch * 2));
+			L.block = dim3(32 * LT);
+			L.smem = (size_t)LT * L.KS * 32 * (L.M + 1) * sizeof(cx<R>);
 			launch(wood ? "wood_solve_x" : "expl_solve_x", bytes, [&] {
-				if(wood) dispatch_xc<ST_WOOD_X>(sc.Mx, Gm, slot0, nsl, sc, C, src, dst, acc_in, acc_out);
-				else dispatch_xc<ST_EXPL_Y>(sc.Mx, Gm, slot0, nsl, sc, C, src, dst, acc_in, acc_out);
+				if(!launch_solve_xc<R>(L, Gm, slot0, nch, C, facx.as<cx<R>>(), sc.plane_x, lscx.as<cx<double>>(), src,
+						dst, acc_in, acc_out))
+					throw BackendError(E_INTERNAL, "no x-solve instance");
 			});
-		else
+		}
+		else {
+			L.M = sc.My; L.KS = sc.KSy; L.kind = wood ? ST_WOOD_Y : ST_EXPL_X;
+			int nch = h.spg / L.KS;
+			L.grid = dim3((unsigned)((Gm.Nx + 31) / 32), (unsigned)(ng * nch * 2));
+			L.block = dim3(32, sc.WY);
+			L.smem = (size_t)(4 * L.KS * sc.WY * 32 + 2 * L.KS * 32) * sizeof(cx<R>);
 			launch(wood ? "wood_solve_y" : "expl_solve_y", bytes, [&] {
-				if(wood) dispatch_yc<ST_WOOD_Y>(sc.My, Gm, slot0, nsl, sc, C, src, dst, acc_in, acc_out);
-				else dispatch_yc<ST_EXPL_X>(sc.My, Gm, slot0, nsl, sc, C, src, dst, acc_in, acc_out);
+				if(!launch_solve_yc<R>(L, Gm, slot0, nch, C, facy.as<cx<R>>(), sc.plane_y, lscy.as<cx<double>>(), src,
+						dst, acc_in, acc_out))
+					throw BackendError(E_INTERNAL, "no y-solve instance");
 			});
+		}
 	}
 
 	// ParaxialPrimaryEvolutionOperator::apply (ParaxialPrimaryEvolutionOperator.cpp:153-209).

@@ -1,0 +1,41 @@
+// Launchers of the chunked line-solve kernels, one translation unit per (direction,
+// precision) so the many template instances compile in parallel.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "bpm_kernels.cuh"
+
+namespace nbpm {
+
+struct SolveLaunch {
+	int M, KS, kind;           // chunk length, slots per thread, stencil kind (ST_*)
+	dim3 grid, block;
+	size_t smem;
+	cudaStream_t stream;
+};
+
+// Returns false if (M, KS) has no compiled instance.
+template <typename R>
+bool launch_solve_xc(const SolveLaunch& L, Geom G, int slot0, int nch, const cx<R>* coef, const cx<R>* fac,
+	size_t plane, const cx<double>* lsc, const cx<R>* src, cx<R>* dst, const cx<R>* ai, cx<R>* ao);
+template <typename R>
+bool launch_solve_yc(const SolveLaunch& L, Geom G, int slot0, int nch, const cx<R>* coef, const cx<R>* fac,
+	size_t plane, const cx<double>* lsc, const cx<R>* src, cx<R>* dst, const cx<R>* ai, cx<R>* ao);
+void set_solve_smem_x_f32(int bytes);
+void set_solve_smem_x_f64(int bytes);
+void set_solve_smem_y_f32(int bytes);
+void set_solve_smem_y_f64(int bytes);
+
+// (M, KS) pairs with compiled instances.
+inline bool solve_pair_ok(int M, int KS) {
+	switch(M) {
+		case 2: case 4: return KS == 2 || KS == 4;
+		case 8: return KS == 1 || KS == 2 || KS == 4;
+		case 16: return KS == 1 || KS == 2;
+		case 32: return KS == 1;
+	}
+	return false;
+}
+
+}  // namespace nbpm

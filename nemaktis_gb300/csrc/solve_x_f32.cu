@@ -1,0 +1,36 @@
+// Instances of the chunked x-line solve kernels, float precision.
+#include "solve_dispatch.cuh"
+
+namespace nbpm {
+
+#define NBPM_XC(MM, KK, KD) \
+	if(L.M == MM && L.KS == KK && L.kind == KD) { \
+		k_solve_xc<float, MM, KD, KK><<<L.grid, L.block, L.smem, L.stream>>>(G, slot0, nch, coef, fac, plane, lsc, \
+			src, dst, ai, ao); \
+		return true; \
+	}
+#define NBPM_XC_PAIRS(KIND) \
+	NBPM_XC(2, 2, KIND) NBPM_XC(2, 4, KIND) NBPM_XC(4, 2, KIND) NBPM_XC(4, 4, KIND) \
+	NBPM_XC(8, 1, KIND) NBPM_XC(8, 2, KIND) NBPM_XC(8, 4, KIND) NBPM_XC(16, 1, KIND) NBPM_XC(16, 2, KIND) NBPM_XC(32, 1, KIND)
+
+template <>
+bool launch_solve_xc<float>(const SolveLaunch& L, Geom G, int slot0, int nch, const cx<float>* coef,
+		const cx<float>* fac, size_t plane, const cx<double>* lsc, const cx<float>* src, cx<float>* dst,
+		const cx<float>* ai, cx<float>* ao) {
+	NBPM_XC_PAIRS(ST_EXPL_Y)
+	NBPM_XC_PAIRS(ST_WOOD_X)
+	return false;
+}
+
+#define NBPM_XA(MM, KK, KD) \
+	cudaFuncSetAttribute(k_solve_xc<float, MM, KD, KK>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+#define NBPM_XA_PAIRS(KIND) \
+	NBPM_XA(2, 2, KIND) NBPM_XA(2, 4, KIND) NBPM_XA(4, 2, KIND) NBPM_XA(4, 4, KIND) \
+	NBPM_XA(8, 1, KIND) NBPM_XA(8, 2, KIND) NBPM_XA(8, 4, KIND) NBPM_XA(16, 1, KIND) NBPM_XA(16, 2, KIND) NBPM_XA(32, 1, KIND)
+
+void set_solve_smem_x_f32(int bytes) {
+	NBPM_XA_PAIRS(ST_EXPL_Y)
+	NBPM_XA_PAIRS(ST_WOOD_X)
+}
+
+}  // namespace nbpm

@@ -1,0 +1,36 @@
+// Instances of the chunked y-line solve kernels, float precision.
+#include "solve_dispatch.cuh"
+
+namespace nbpm {
+
+#define NBPM_YC(MM, KK, KD) \
+	if(L.M == MM && L.KS == KK && L.kind == KD) { \
+		k_solve_yc<float, MM, KD, KK><<<L.grid, L.block, L.smem, L.stream>>>(G, slot0, nch, coef, fac, plane, lsc, \
+			src, dst, ai, ao); \
+		return true; \
+	}
+#define NBPM_YC_PAIRS(KIND) \
+	NBPM_YC(2, 2, KIND) NBPM_YC(2, 4, KIND) NBPM_YC(4, 2, KIND) NBPM_YC(4, 4, KIND) \
+	NBPM_YC(8, 1, KIND) NBPM_YC(8, 2, KIND) NBPM_YC(8, 4, KIND) NBPM_YC(16, 1, KIND) NBPM_YC(16, 2, KIND) NBPM_YC(32, 1, KIND)
+
+template <>
+bool launch_solve_yc<float>(const SolveLaunch& L, Geom G, int slot0, int nch, const cx<float>* coef,
+		const cx<float>* fac, size_t plane, const cx<double>* lsc, const cx<float>* src, cx<float>* dst,
+		const cx<float>* ai, cx<float>* ao) {
+	NBPM_YC_PAIRS(ST_EXPL_X)
+	NBPM_YC_PAIRS(ST_WOOD_Y)
+	return false;
+}
+
+#define NBPM_YA(MM, KK, KD) \
+	cudaFuncSetAttribute(k_solve_yc<float, MM, KD, KK>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+#define NBPM_YA_PAIRS(KIND) \
+	NBPM_YA(2, 2, KIND) NBPM_YA(2, 4, KIND) NBPM_YA(4, 2, KIND) NBPM_YA(4, 4, KIND) \
+	NBPM_YA(8, 1, KIND) NBPM_YA(8, 2, KIND) NBPM_YA(8, 4, KIND) NBPM_YA(16, 1, KIND) NBPM_YA(16, 2, KIND) NBPM_YA(32, 1, KIND)
+
+void set_solve_smem_y_f32(int bytes) {
+	NBPM_YA_PAIRS(ST_EXPL_X)
+	NBPM_YA_PAIRS(ST_WOOD_Y)
+}
+
+}  // namespace nbpm
