@@ -119,6 +119,18 @@ int nbpm_eval_index(const char* expr, double lambda, double* out);
 int nbpm_mask_weights(const char* json_str, const char* mask_formula, const double* mask_vals, int n_mask_vals,
 		unsigned char* mask_out, double* weights_out);
 
+/* Batched periodic tridiagonal solves on the device, complex FP64 (interleaved re, im).
+ * Replaces BlockSparseMatrixDX/DY::shifted_block_vmult_inv (BeamPropagationSolver/src/
+ * BeamPropagationLib/BlockSparseMatrix.cpp:195-258, 386-449) as a standalone primitive: each
+ * of the nlines lines has L points, the last duplicating the first (period L-1), and row i
+ * reads inf[i]*x[i-1] + mid[i]*x[i] + sup[i]*x[i+1] = rhs[i] with indices modulo L-1.
+ * inf, mid, sup, rhs and x are device arrays of nlines*L complex values (line-major; entry
+ * L-1 of inf/mid/sup/rhs is ignored, x[L-1] receives x[0]). Requires L >= 4. stream is a
+ * cudaStream_t (NULL: default stream); the call returns after the solve completed. Allocates
+ * its factorisation scratch (5*nlines*(L-1) + 2*nlines complex) stream-ordered. */
+int nbpm_periodic_tridiag_solve(int L, int nlines, const double* inf, const double* mid, const double* sup,
+		const double* rhs, double* x, void* stream);
+
 /* Message of the last failure on this thread ("" if none). */
 const char* nbpm_last_error(void);
 

@@ -55,6 +55,7 @@ EXPORTS = {
     "nbpm_plan_profile": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, ctypes.POINTER(c_int)]),
     "nbpm_eval_index": (c_int, [c_char_p, c_double, ctypes.POINTER(c_double)]),
     "nbpm_mask_weights": (c_int, [c_char_p, c_char_p, c_void_p, c_int, c_void_p, c_void_p]),
+    "nbpm_periodic_tridiag_solve": (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "nbpm_last_error": (c_char_p, []),
     "nbpm_version": (c_char_p, []),
 }

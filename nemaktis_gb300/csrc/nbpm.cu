@@ -29,6 +29,9 @@ namespace nbpm {
 
 static thread_local std::string g_last_error;
 
+// Shared with the other translation units of the library.
+void set_last_error(const std::string& m) { g_last_error = m; }
+
 #define CK(call)                                                                                   \
 	do {                                                                                           \
 		cudaError_t e_ = (call);                                                                   \
