@@ -131,6 +131,19 @@ int nbpm_mask_weights(const char* json_str, const char* mask_formula, const doub
 int nbpm_periodic_tridiag_solve(int L, int nlines, const double* inf, const double* mid, const double* sup,
 		const double* rhs, double* x, void* stream);
 
+/* Same solve as nbpm_periodic_tridiag_solve for callers that cannot allocate device memory:
+ * code recording inside a CUDA stream capture (a cudaMalloc there breaks the capture),
+ * real-time loops that must avoid the allocator and its implicit synchronisation, and hosts
+ * that give the whole device memory to their own pool. It allocates nothing: its scratch is a
+ * fixed 32 MiB device array (2 Mi complex FP64 values) that every device loading the library
+ * holds until the process exits, so sizes with 5*nlines*(L-1) + 2*nlines above 2*1024*1024
+ * are rejected with NBPM_ERR_SIZE. The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress); make that first call before any stream capture. All calls
+ * share the array: calls that overlap on the GPU (other streams, other host threads) race on
+ * it and must be serialised by the caller. No counterpart in the reference. */
+int nbpm_periodic_tridiag_solve_noalloc(int L, int nlines, const double* inf, const double* mid,
+		const double* sup, const double* rhs, double* x, void* stream);
+
 /* Message of the last failure on this thread ("" if none). */
 const char* nbpm_last_error(void);
 

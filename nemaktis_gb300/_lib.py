@@ -56,6 +56,8 @@ EXPORTS = {
     "nbpm_eval_index": (c_int, [c_char_p, c_double, ctypes.POINTER(c_double)]),
     "nbpm_mask_weights": (c_int, [c_char_p, c_char_p, c_void_p, c_int, c_void_p, c_void_p]),
     "nbpm_periodic_tridiag_solve": (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "nbpm_periodic_tridiag_solve_noalloc": (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                                    c_void_p]),
     "nbpm_last_error": (c_char_p, []),
     "nbpm_version": (c_char_p, []),
 }
