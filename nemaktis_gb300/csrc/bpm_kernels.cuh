@@ -352,14 +352,25 @@ __global__ void k_coef(const double* __restrict__ QA, const double* __restrict__
 // plus per line r0 = inf0/mid0 and rden = 1/(1 + corr0 - r0*corr_{L-2}) in FP64.
 // scr holds gamma and the forward corr: [group][comp][2][N].
 // ---------------------------------------------------------------------------------------
+// One launch covers the x factorisations (threads [0, ngroups*2*Ny)) and the y ones (the
+// following ngroups*2*Nx threads); scratch halves are separate.
 template <typename S>
-__global__ void k_factor(int dirn, Geom G, int ngroups, int chunkM, const cx<S>* __restrict__ diag,
-		cx<S>* __restrict__ fac, size_t plane, cx<double>* __restrict__ lsc, cx<S>* __restrict__ scr) {
+__global__ void k_factor(Geom G, int ngroups, int chunkMx, const cx<S>* __restrict__ diag,
+		cx<S>* __restrict__ facx, size_t planex, cx<double>* __restrict__ lscx,
+		cx<S>* __restrict__ facy, size_t planey, cx<double>* __restrict__ lscy, cx<S>* __restrict__ scr_all) {
 	typedef S T;
 	int Nx = G.Nx, Ny = G.Ny, N = G.N;
+	int t = blockIdx.x * blockDim.x + threadIdx.x;
+	const int nx_threads = ngroups * 2 * Ny;
+	const int dirn = t < nx_threads ? 0 : 1;
+	if(dirn == 1) t -= nx_threads;
+	const int chunkM = dirn == 0 ? chunkMx : 0;
+	cx<S>* fac = dirn == 0 ? facx : facy;
+	const size_t plane = dirn == 0 ? planex : planey;
+	cx<double>* lsc = dirn == 0 ? lscx : lscy;
+	cx<S>* scr = scr_all + (size_t)dirn * ngroups * 2 * 2 * N;
 	int L = dirn == 0 ? Nx : Ny;
 	int nlines = dirn == 0 ? Ny : Nx;
-	int t = blockIdx.x * blockDim.x + threadIdx.x;
 	if(t >= ngroups * 2 * nlines || L <= 3) return;
 	int line = t % nlines;
 	int c = (t / nlines) % 2;

@@ -156,7 +156,16 @@ template <typename R>
 struct Plan : PlanBase {
 	nbpm_options opt;
 	std::vector<std::unique_ptr<SampleHost>> S;
-	cudaStream_t stream = nullptr;
+	cudaStream_t stream = nullptr;   // main stream (right-hand-side work, copies)
+	cudaStream_t streamB = nullptr;  // per-slab setup (eps planes, coefficients, factorisations)
+	cudaStream_t cs = nullptr;       // stream the next launch goes to
+	cudaEvent_t eFork = nullptr, eJoin = nullptr, eCoef = nullptr, eFac = nullptr, eTrans = nullptr, eAdi[2] = {nullptr, nullptr};
+	// double-buffered factor planes / line scalars: slab iz uses half iz & 1
+	size_t facx_half = 0, facy_half = 0, lsc_half = 0;
+	cx<R>* fx_cur = nullptr;
+	cx<R>* fy_cur = nullptr;
+	cx<double>* lx_cur = nullptr;
+	cx<double>* ly_cur = nullptr;
 	cudaGraphExec_t gexec = nullptr;
 	cudaEvent_t ev[6];
 	// workspace (shared by passes, sized for the largest)
@@ -184,9 +193,9 @@ struct Plan : PlanBase {
 	void launch(const char* name, double bytes, F&& fn) {
 		if(profiling) {
 			ProfRec r{name, bytes, pool_event(), pool_event()};
-			CK(cudaEventRecord(r.a, stream));
+			CK(cudaEventRecord(r.a, cs));
 			fn();
-			CK(cudaEventRecord(r.b, stream));
+			CK(cudaEventRecord(r.b, cs));
 			prof.push_back(r);
 		}
 		else fn();
@@ -206,6 +215,8 @@ struct Plan : PlanBase {
 		for(auto e : evpool) cudaEventDestroy(e);
 		if(gexec) cudaGraphExecDestroy(gexec);
 		for(auto& e : ev) if(e) cudaEventDestroy(e);
+		for(cudaEvent_t e : {eFork, eJoin, eCoef, eFac, eTrans, eAdi[0], eAdi[1]}) if(e) cudaEventDestroy(e);
+		if(streamB) cudaStreamDestroy(streamB);
 		if(stream) cudaStreamDestroy(stream);
 	}
 
@@ -298,6 +309,10 @@ struct Plan : PlanBase {
 		// Host-side validation is complete; only now touch the device.
 		CK(cudaSetDevice(opt.device));
 		CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+		CK(cudaStreamCreateWithFlags(&streamB, cudaStreamNonBlocking));
+		for(cudaEvent_t* e : {&eFork, &eJoin, &eCoef, &eFac, &eTrans, &eAdi[0], &eAdi[1]})
+			CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+		cs = stream;
 		for(auto& e : ev) CK(cudaEventCreate(&e));
 		int dev = opt.device;
 		int optin = 0;
@@ -352,7 +367,7 @@ struct Plan : PlanBase {
 			maxD = std::max(maxD, (size_t)ng * NDIAG * N);
 			maxFx = std::max(maxFx, (size_t)ng * 2 * NFAC * std::max(sc.plane_x, sc.plane_y));
 			maxL = std::max(maxL, (size_t)ng * 2 * std::max(h.s.Nx, h.s.Ny) * 2);
-			maxScr = std::max(maxScr, (size_t)ng * 2 * 2 * N);
+			maxScr = std::max(maxScr, (size_t)2 * ng * 2 * 2 * N);  // x and y halves
 			if(sizeof(R) != sizeof(double)) maxStage = std::max(maxStage, (size_t)h.slots * 2 * N);
 			// per-sample buffers
 			h.dir.alloc(sizeof(double) * h.nvox * h.fd);
@@ -375,10 +390,12 @@ struct Plan : PlanBase {
 		Qring.alloc(sizeof(double) * maxQ);
 		coef.alloc(sizeof(cx<R>) * maxC);
 		diag.alloc(sizeof(cx<R>) * maxD);
-		facx.alloc(sizeof(cx<R>) * maxFx);
-		facy.alloc(sizeof(cx<R>) * maxFx);
-		lscx.alloc(sizeof(cx<double>) * maxL);
-		lscy.alloc(sizeof(cx<double>) * maxL);
+		facx_half = facy_half = maxFx;
+		lsc_half = maxL;
+		facx.alloc(sizeof(cx<R>) * maxFx * 2);
+		facy.alloc(sizeof(cx<R>) * maxFx * 2);
+		lscx.alloc(sizeof(cx<double>) * maxL * 2);
+		lscy.alloc(sizeof(cx<double>) * maxL * 2);
 		scr.alloc(sizeof(cx<R>) * maxScr);
 		stage.alloc(sizeof(cx<double>) * maxStage);
 		dev_bytes += T.bytes + T2.bytes + Qring.bytes + coef.bytes + diag.bytes + facx.bytes + facy.bytes +
@@ -458,13 +475,14 @@ struct Plan : PlanBase {
 			cx<R>* tw = twiddles(n);
 			double bytes = 2.0 * sizeof(cx<R>) * (double)nplanes * Nx * Ny;
 			launch(pass == 0 ? "fft_rows" : "fft_cols", bytes, [&] {
-				k_fft_lines<R><<<blocks, threads, smem, stream>>>(F, P, nlines, lpp, ps, ls, es, lpb, tw, sign);
+				k_fft_lines<R><<<blocks, threads, smem, cs>>>(F, P, nlines, lpp, ps, ls, es, lpb, tw, sign);
 			});
 		}
 	}
 
 	void record() {
 		launches = 0;
+		cs = stream;
 		for(auto& hp : S) record_sample(*hp);
 	}
 
@@ -480,15 +498,15 @@ struct Plan : PlanBase {
 		{
 			int nb = (int)std::min<size_t>(1024, (h.nvox + 255) / 256);
 			launch("neff_partial", (double)h.nvox * h.fd * 8 * h.G, [&] {
-				k_neff_partial<<<dim3(nb, h.G), 256, 0, stream>>>(h.dir.as<double>(), h.fd, mk_, h.nvox,
+				k_neff_partial<<<dim3(nb, h.G), 256, 0, cs>>>(h.dir.as<double>(), h.fd, mk_, h.nvox,
 					h.gpsd.as<GroupParams>(), h.partial.as<double>());
 			});
 			launch("nref_final", 8.0 * nb * h.G, [&] {
-				k_nref_final<<<(h.G + 63) / 64, 64, 0, stream>>>(h.G, nb, h.nvox, h.partial.as<double>(),
+				k_nref_final<<<(h.G + 63) / 64, 64, 0, cs>>>(h.G, nb, h.nvox, h.partial.as<double>(),
 					h.gpsd.as<GroupParams>());
 			});
 			launch("shift_params", sizeof(ShiftParams) * h.G * h.Nq, [&] {
-				k_shift_params<<<(h.G * h.Nq + 63) / 64, 64, 0, stream>>>(h.G, h.Nq, Nx, Ny, h.gpsd.as<GroupParams>(),
+				k_shift_params<<<(h.G * h.Nq + 63) / 64, 64, 0, cs>>>(h.G, h.Nq, Nx, Ny, h.gpsd.as<GroupParams>(),
 					h.qv.as<double>(), h.shiftd.as<ShiftParams>());
 			});
 		}
@@ -509,57 +527,79 @@ struct Plan : PlanBase {
 			const double field_pts = (double)N * nsl;
 
 			launch("eps_plane", eps_bytes, [&] {
-				k_eps_plane<<<pgrid(N, ng), 256, 0, stream>>>(h.dir.as<double>(), h.fd, mk_, N, 0, gps, Qr[0]);
+				k_eps_plane<<<pgrid(N, ng), 256, 0, cs>>>(h.dir.as<double>(), h.fd, mk_, N, 0, gps, Qr[0]);
 			});
 			if(h.s.beam_type != 2) {
 				launch("init_fields", field_pts * 2 * sc + (double)N * ng * 3 * 8, [&] {
-					k_init_fields<R><<<pgrid(N, nsl), 256, 0, stream>>>(Gm, slot0, gps, Qr[0], h.s.beam_type,
+					k_init_fields<R><<<pgrid(N, nsl), 256, 0, cs>>>(Gm, slot0, gps, Qr[0], h.s.beam_type,
 						h.s.waist, h.s.dx, h.s.dy, Fp);
 				});
 			}
 			else {
 				size_t n = (size_t)nsl * 2 * N;
 				launch("copy_fields", 2.0 * n * sc, [&] {
-					k_copy<R><<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, h.E0.as<cx<R>>() + (size_t)slot0 * 2 * N, Fp);
+					k_copy<R><<<(unsigned)((n + 255) / 256), 256, 0, cs>>>(n, h.E0.as<cx<R>>() + (size_t)slot0 * 2 * N, Fp);
 				});
 			}
 			const cx<R>* Cprev = nullptr;
+			// Setup of slab iz (eps plane iz+1, coefficients, factorisations) runs on streamB and
+			// overlaps the right-hand-side work of slab iz-1 on the main stream.
+			CK(cudaEventRecord(eFork, stream));
+			CK(cudaStreamWaitEvent(streamB, eFork, 0));
 			for(int iz = 0; iz < Nz - 1; iz++) {
 				double* QA = Qr[iz & 1];
 				double* QB = Qr[(iz + 1) & 1];
 				cx<R>* C = Cring[iz & 1];
-				launch("eps_plane", eps_bytes, [&] {
-					k_eps_plane<<<pgrid(N, ng), 256, 0, stream>>>(h.dir.as<double>(), h.fd, mk_, N, iz + 1, gps, QB);
-				});
-				launch("coef", (double)N * ng * (2 * NQ * 8 + NCOEF * sc + NDIAG * sc + (wts ? 16 : 0)), [&] {
-					k_coef<R><<<pgrid(N, ng, 128), 128, 0, stream>>>(QA, QB, wts, iz, Gm, gps, C, Dg);
-				});
-				int lx = ng * 2 * Ny, ly = ng * 2 * Nx;
-				const double fb = (double)N * ng * 2 * (3 * sc + NFAC * sc + 4 * sc);
 				const SolveCfg& scf = scfg[h.index];
-				launch("factor_x", fb, [&] {
-					k_factor<R><<<(lx + 63) / 64, 64, 0, stream>>>(0, Gm, ng, scf.Mx, Dg, facx.as<cx<R>>(), scf.plane_x,
-						lscx.as<cx<double>>(), scr.as<cx<R>>());
+				cx<R>* fx = facx.as<cx<R>>() + (size_t)(iz & 1) * facx_half;
+				cx<R>* fy = facy.as<cx<R>>() + (size_t)(iz & 1) * facy_half;
+				cx<double>* lx = lscx.as<cx<double>>() + (size_t)(iz & 1) * lsc_half;
+				cx<double>* ly = lscy.as<cx<double>>() + (size_t)(iz & 1) * lsc_half;
+				// ---- setup stream ----
+				cs = streamB;
+				launch("eps_plane", eps_bytes, [&] {
+					k_eps_plane<<<pgrid(N, ng), 256, 0, cs>>>(h.dir.as<double>(), h.fd, mk_, N, iz + 1, gps, QB);
 				});
-				launch("factor_y", fb, [&] {
-					k_factor<R><<<(ly + 63) / 64, 64, 0, stream>>>(1, Gm, ng, 0, Dg, facy.as<cx<R>>(), scf.plane_y,
-						lscy.as<cx<double>>(), scr.as<cx<R>>());
+				// coef(iz) overwrites the set the transition of slab iz-1 read (slab iz-2)
+				if(iz >= 1) CK(cudaStreamWaitEvent(streamB, eTrans, 0));
+				launch("coef", (double)N * ng * (2 * NQ * 8 + NCOEF * sc + NDIAG * sc + (wts ? 16 : 0)), [&] {
+					k_coef<R><<<pgrid(N, ng, 128), 128, 0, cs>>>(QA, QB, wts, iz, Gm, gps, C, Dg);
 				});
+				CK(cudaEventRecord(eCoef, streamB));
+				// factor(iz) overwrites the half the line solves of slab iz-2 used
+				if(iz >= 2) CK(cudaStreamWaitEvent(streamB, eAdi[iz & 1], 0));
+				int lx_n = ng * 2 * Ny, ly_n = ng * 2 * Nx;
+				const double fb = (double)N * ng * 2 * (3 * sc + NFAC * sc + 4 * sc);
+				launch("factor", 2 * fb, [&] {
+					k_factor<R><<<(lx_n + ly_n + 63) / 64, 64, 0, cs>>>(Gm, ng, scf.Mx, Dg, fx, scf.plane_x, lx, fy,
+						scf.plane_y, ly, scr.as<cx<R>>());
+				});
+				CK(cudaEventRecord(eFac, streamB));
+				// ---- main stream ----
+				cs = stream;
+				CK(cudaStreamWaitEvent(stream, eCoef, 0));
 				// [phase(iz-1)] shift(iz-1) | shift(iz) phase(iz)   (BPMIteration.cpp:133-146)
 				rec_transition(h, slot0, nsl, Cprev, C, Fp, Tb, T2b, iz > 0);
+				CK(cudaEventRecord(eTrans, stream));
+				CK(cudaStreamWaitEvent(stream, eFac, 0));
+				fx_cur = fx; fy_cur = fy; lx_cur = lx; ly_cur = ly;
 				rec_adi(h, Gm, slot0, nsl, ng, Nw, C, Fp, Tb, T2b);
+				CK(cudaEventRecord(eAdi[iz & 1], stream));
 				Cprev = C;
 			}
+			CK(cudaEventRecord(eJoin, streamB));
+			CK(cudaStreamWaitEvent(stream, eJoin, 0));
+			cs = stream;
 			if(Nz > 1) rec_transition(h, slot0, nsl, Cprev, nullptr, Fp, Tb, T2b, false);
 			launch("fresnel_out", field_pts * 4 * sc + (double)N * ng * 3 * 8, [&] {
-				k_fresnel_out<R><<<pgrid(N, nsl), 256, 0, stream>>>(Gm, slot0, gps, Qr[(Nz - 1) & 1], Fp);
+				k_fresnel_out<R><<<pgrid(N, nsl), 256, 0, cs>>>(Gm, slot0, gps, Qr[(Nz - 1) & 1], Fp);
 			});
 		}
 		// Screen filter over every plane of the sample (ScreenOutput.cpp:184-224).
 		int nplanes = h.slots * 2;
 		fft2(h, F, nplanes, -1);
 		launch("screen_filter", (double)N * h.slots * 4 * sc, [&] {
-			k_screen_filter<R><<<pgrid(N, h.G * h.Nq, 128), 128, 0, stream>>>(F, h.sp, 0, h.wl.as<double>(),
+			k_screen_filter<R><<<pgrid(N, h.G * h.Nq, 128), 128, 0, cs>>>(F, h.sp, 0, h.wl.as<double>(),
 				h.nout.as<double>(), h.qv.as<double>());
 		});
 		fft2(h, F, nplanes, +1);
@@ -577,23 +617,23 @@ struct Plan : PlanBase {
 		const ShiftParams* sp = h.shiftd.as<ShiftParams>();
 		if(!h.any_shift) {
 			launch("phase_sync", fpb, [&] {
-				k_phase_sync<R><<<pgrid(Gm.N, nsl), 256, 0, stream>>>(Gm, slot0, CA, CB, Fp);
+				k_phase_sync<R><<<pgrid(Gm.N, nsl), 256, 0, cs>>>(Gm, slot0, CA, CB, Fp);
 			});
 			return;
 		}
 		launch("shift_x", fpb, [&] {
-			k_shift_x<R><<<pgrid(Gm.N, nsl), 256, 0, stream>>>(Gm, slot0, sp, CA, Fp, T2b);
+			k_shift_x<R><<<pgrid(Gm.N, nsl), 256, 0, cs>>>(Gm, slot0, sp, CA, Fp, T2b);
 		});
 		if(two_shifts) {
 			launch("shift_y", fpb, [&] {
-				k_shift_y<R><<<pgrid(Gm.N, nsl), 256, 0, stream>>>(Gm, slot0, sp, nullptr, T2b, Tb);
+				k_shift_y<R><<<pgrid(Gm.N, nsl), 256, 0, cs>>>(Gm, slot0, sp, nullptr, T2b, Tb);
 			});
 			launch("shift_x", fpb, [&] {
-				k_shift_x<R><<<pgrid(Gm.N, nsl), 256, 0, stream>>>(Gm, slot0, sp, nullptr, Tb, T2b);
+				k_shift_x<R><<<pgrid(Gm.N, nsl), 256, 0, cs>>>(Gm, slot0, sp, nullptr, Tb, T2b);
 			});
 		}
 		launch("shift_y", fpb, [&] {
-			k_shift_y<R><<<pgrid(Gm.N, nsl), 256, 0, stream>>>(Gm, slot0, sp, CB, T2b, Fp);
+			k_shift_y<R><<<pgrid(Gm.N, nsl), 256, 0, cs>>>(Gm, slot0, sp, CB, T2b, Fp);
 		});
 	}
 
@@ -607,12 +647,12 @@ struct Plan : PlanBase {
 		double bytes = (double)Gm.N * nsl * 2 * sz * (acc_out ? 4 : 2) + (double)Gm.N * ng * 2 * NFAC * sz;
 		if(dirn == 0)
 			launch("solve_x", bytes, [&] {
-				k_solve<R, 0><<<(nt + 127) / 128, 128, 0, stream>>>(Gm, slot0, nsl, facx.as<cx<R>>(), sc.plane_x,
+				k_solve<R, 0><<<(nt + 127) / 128, 128, 0, cs>>>(Gm, slot0, nsl, facx.as<cx<R>>(), sc.plane_x,
 					lscx.as<cx<double>>(), src, dst, acc_in, acc_out);
 			});
 		else
 			launch("solve_y", bytes, [&] {
-				k_solve<R, 1><<<(nt + 127) / 128, 128, 0, stream>>>(Gm, slot0, nsl, facy.as<cx<R>>(), sc.plane_y,
+				k_solve<R, 1><<<(nt + 127) / 128, 128, 0, cs>>>(Gm, slot0, nsl, facy.as<cx<R>>(), sc.plane_y,
 					lscy.as<cx<double>>(), src, dst, acc_in, acc_out);
 			});
 	}
@@ -626,7 +666,7 @@ struct Plan : PlanBase {
 		double fp = (double)Gm.N * nsl * 2 * sz;
 		double bytes = fp * (1 + (dst ? 1 : 0) + (acc_out ? 2 : 0)) + (double)Gm.N * ng * (2 * NFAC + (wood ? 14 : 20)) * sz;
 		SolveLaunch L;
-		L.stream = stream;
+		L.stream = cs;
 		if(dirn == 0) {
 			const int LT = 4;
 			L.M = sc.Mx; L.KS = sc.KSx; L.kind = wood ? ST_WOOD_X : ST_EXPL_Y;
@@ -635,7 +675,7 @@ struct Plan : PlanBase {
 			L.block = dim3(32 * LT);
 			L.smem = (size_t)LT * L.KS * 32 * (L.M + 1) * sizeof(cx<R>);
 			launch(wood ? "wood_solve_x" : "expl_solve_x", bytes, [&] {
-				if(!launch_solve_xc<R>(L, Gm, slot0, nch, C, facx.as<cx<R>>(), sc.plane_x, lscx.as<cx<double>>(), src,
+				if(!launch_solve_xc<R>(L, Gm, slot0, nch, C, fx_cur, sc.plane_x, lx_cur, src,
 						dst, acc_in, acc_out))
 					throw BackendError(E_INTERNAL, "no x-solve instance");
 			});
@@ -647,7 +687,7 @@ struct Plan : PlanBase {
 			L.block = dim3(32, sc.WY);
 			L.smem = (size_t)(4 * L.KS * sc.WY * 32 + 2 * L.KS * 32) * sizeof(cx<R>);
 			launch(wood ? "wood_solve_y" : "expl_solve_y", bytes, [&] {
-				if(!launch_solve_yc<R>(L, Gm, slot0, nch, C, facy.as<cx<R>>(), sc.plane_y, lscy.as<cx<double>>(), src,
+				if(!launch_solve_yc<R>(L, Gm, slot0, nch, C, fy_cur, sc.plane_y, ly_cur, src,
 						dst, acc_in, acc_out))
 					throw BackendError(E_INTERNAL, "no y-solve instance");
 			});
@@ -672,11 +712,11 @@ struct Plan : PlanBase {
 			else {
 				if(dirn == 0)
 					launch("expl_y", fp * 4 * sc + (double)N * ng * 20 * sc, [&] {
-						k_stencil<R, ST_EXPL_Y><<<gr, 256, 0, stream>>>(Gm, slot0, C, Fp, T2b);
+						k_stencil<R, ST_EXPL_Y><<<gr, 256, 0, cs>>>(Gm, slot0, C, Fp, T2b);
 					});
 				else
 					launch("expl_x", fp * 4 * sc + (double)N * ng * 20 * sc, [&] {
-						k_stencil<R, ST_EXPL_X><<<gr, 256, 0, stream>>>(Gm, slot0, C, Fp, T2b);
+						k_stencil<R, ST_EXPL_X><<<gr, 256, 0, cs>>>(Gm, slot0, C, Fp, T2b);
 					});
 				rec_solve_seq(dirn, h, Gm, slot0, nsl, ng, T2b, Tb, nullptr, nullptr);
 			}
@@ -685,7 +725,7 @@ struct Plan : PlanBase {
 			if(Nw == 0) {
 				size_t n = (size_t)nsl * 2 * N;
 				launch("copy_fields", 2.0 * n * sc, [&] {
-					k_copy<R><<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, Tb, Fp);
+					k_copy<R><<<(unsigned)((n + 255) / 256), 256, 0, cs>>>(n, Tb, Fp);
 				});
 			}
 			for(int it = 1; it <= Nw; it++) {
@@ -696,11 +736,11 @@ struct Plan : PlanBase {
 				else {
 					if(dirn == 0)
 						launch("wood_x", fp * 4 * sc + (double)N * ng * 14 * sc, [&] {
-							k_stencil<R, ST_WOOD_X><<<gr, 256, 0, stream>>>(Gm, slot0, C, cur, oth);
+							k_stencil<R, ST_WOOD_X><<<gr, 256, 0, cs>>>(Gm, slot0, C, cur, oth);
 						});
 					else
 						launch("wood_y", fp * 4 * sc + (double)N * ng * 14 * sc, [&] {
-							k_stencil<R, ST_WOOD_Y><<<gr, 256, 0, stream>>>(Gm, slot0, C, cur, oth);
+							k_stencil<R, ST_WOOD_Y><<<gr, 256, 0, cs>>>(Gm, slot0, C, cur, oth);
 						});
 					rec_solve_seq(dirn, h, Gm, slot0, nsl, ng, oth, oth, ai, Fp);
 				}
@@ -720,6 +760,7 @@ struct Plan : PlanBase {
 		catch(...) { profiling = false; throw; }
 		profiling = false;
 		CK(cudaStreamSynchronize(stream));
+		CK(cudaStreamSynchronize(streamB));
 		for(auto& r : prof) {
 			float t = 0;
 			CK(cudaEventElapsedTime(&t, r.a, r.b));
