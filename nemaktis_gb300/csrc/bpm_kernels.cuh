@@ -524,7 +524,7 @@ struct Stencil {
 
 // Step kinds of the composite stencil kernel (ParaxialPrimaryEvolutionOperator.cpp:153-207
 // with the duplicate-row/column fix-ups of BlockSparseMatrix.cpp folded in analytically).
-enum { ST_EXPL_Y = 0, ST_EXPL_X = 1, ST_WOOD_X = 2, ST_WOOD_Y = 3 };
+enum { ST_EXPL_Y = 0, ST_EXPL_X = 1, ST_WOOD_X = 2, ST_WOOD_Y = 3, ST_GIVEN = 4 };
 
 // One component of a composite stencil step at point (ix, iy). EXPL kinds return
 // f + mu*R f (explicit half-step), WOOD kinds return mu*R_offdiag t (Woodbury right-hand side).
@@ -593,6 +593,12 @@ __device__ __forceinline__ void composite_m(const Stencil<R>& st, int comp, int 
 	const int xx = ix == Nx - 1 ? 0 : ix, yy = iy == Ny - 1 ? 0 : iy;
 	const bool ax = Nx > 3, ay = Ny > 3;
 	const int p = ix + Nx * iy;
+	if(KIND == ST_GIVEN) {
+		const cx<R>* fc = comp == 0 ? f0 : f1;
+#pragma unroll
+		for(int j = 0; j < KS; j++) out[j] = fc[j * ss + p];
+		return;
+	}
 #pragma unroll
 	for(int j = 0; j < KS; j++) out[j] = mk<R>(0, 0);
 	if(KIND == ST_EXPL_Y) {
@@ -655,6 +661,222 @@ __device__ __forceinline__ void composite_m(const Stencil<R>& st, int comp, int 
 			st.template dxdy_m<KS>(3, xx, yy, f1, ss, out);
 		}
 		else st.template dy_m<KS>(2, ix, yy, f0, ss, out);
+	}
+}
+
+// Stencil terms of one composite step at one point, gathered once so that they can be applied
+// to every slot of a wavelength group: value = [f_comp(p)] + sum_t coef_t * f_{src_t}(tap_t).
+template <typename R>
+struct Terms {
+	int n;
+	cx<R> c[14];
+	int tap[14];
+	unsigned char src[14];
+	__device__ __forceinline__ void add(cx<R> cv, int t, int s) { c[n] = cv; tap[n] = t; src[n] = (unsigned char)s; n++; }
+	__device__ __forceinline__ void dx(const Stencil<R>& st, int b, int x, int y, int s) {
+		int p = x + st.Nx * y, Nx = st.Nx;
+		int mx = x == 0 ? Nx - 2 : x - 1, px = x == Nx - 2 ? 0 : x + 1;
+		int base = C_DX + 3 * b;
+		add(st.c(base, p), mx + Nx * y, s); add(st.c(base + 1, p), p, s); add(st.c(base + 2, p), px + Nx * y, s);
+	}
+	__device__ __forceinline__ void dy(const Stencil<R>& st, int b, int x, int y, int s) {
+		int p = x + st.Nx * y, Nx = st.Nx, Ny = st.Ny;
+		int my = y == 0 ? Ny - 2 : y - 1, py = y == Ny - 2 ? 0 : y + 1;
+		int base = C_DY + 3 * b;
+		add(st.c(base, p), x + Nx * my, s); add(st.c(base + 1, p), p, s); add(st.c(base + 2, p), x + Nx * py, s);
+	}
+	__device__ __forceinline__ void dxdy(const Stencil<R>& st, int b, int x, int y, int s) {
+		int p = x + st.Nx * y, Nx = st.Nx, Ny = st.Ny;
+		int mx = x == 0 ? Nx - 2 : x - 1, px = x == Nx - 2 ? 0 : x + 1;
+		int my = y == 0 ? Ny - 2 : y - 1, py = y == Ny - 2 ? 0 : y + 1;
+		int base = C_DXDY + 4 * b;
+		add(st.c(base, p), px + Nx * py, s); add(st.c(base + 1, p), mx + Nx * py, s);
+		add(st.c(base + 2, p), px + Nx * my, s); add(st.c(base + 3, p), mx + Nx * my, s);
+	}
+};
+
+// The terms of composite<KIND>(comp) at (ix, iy), same folding of the duplicate row/column.
+// Returns whether the f_comp(p) identity term is present (explicit half-steps).
+template <typename R, int KIND>
+__device__ __forceinline__ bool gather_terms(const Stencil<R>& st, int comp, int ix, int iy, Terms<R>& T) {
+	const int Nx = st.Nx, Ny = st.Ny;
+	const int xx = ix == Nx - 1 ? 0 : ix, yy = iy == Ny - 1 ? 0 : iy;
+	const bool ax = Nx > 3, ay = Ny > 3;
+	T.n = 0;
+	if(KIND == ST_EXPL_Y) {
+		if(comp == 0) { if(ay) { T.dy(st, 0, ix, yy, 0); T.dy(st, 1, ix, yy, 1); } }
+		else if(ay) {
+			if(ax) { T.dy(st, 3, xx, yy, 1); T.dxdy(st, 3, xx, yy, 1); T.dy(st, 2, xx, yy, 0); T.dxdy(st, 2, xx, yy, 0); }
+			else { T.dy(st, 3, ix, yy, 1); T.dy(st, 2, ix, yy, 0); }
+		}
+		return true;
+	}
+	if(KIND == ST_EXPL_X) {
+		if(comp == 0) {
+			if(ax) {
+				if(ay) { T.dx(st, 0, xx, yy, 0); T.dxdy(st, 0, xx, yy, 0); T.dx(st, 1, xx, yy, 1); T.dxdy(st, 1, xx, yy, 1); }
+				else { T.dx(st, 0, xx, iy, 0); T.dx(st, 1, xx, iy, 1); }
+			}
+		}
+		else if(ax) { T.dx(st, 3, xx, iy, 1); T.dx(st, 2, xx, iy, 0); }
+		return true;
+	}
+	if(KIND == ST_WOOD_X) {
+		if(comp == 0) {
+			if(ax) {
+				if(ay) { T.dx(st, 1, xx, yy, 1); T.dxdy(st, 1, xx, yy, 1); T.dxdy(st, 0, xx, yy, 0); }
+				else T.dx(st, 1, xx, iy, 1);
+			}
+		}
+		else if(ax) T.dx(st, 2, xx, iy, 0);
+		return false;
+	}
+	if(comp == 0) { if(ay) T.dy(st, 1, ix, yy, 1); }
+	else if(ay) {
+		if(ax) { T.dy(st, 2, xx, yy, 0); T.dxdy(st, 2, xx, yy, 0); T.dxdy(st, 3, xx, yy, 1); }
+		else T.dy(st, 2, ix, yy, 0);
+	}
+	return false;
+}
+
+// Right-hand sides of one composite step for every slot of a wavelength group: one thread per
+// (point, comp, group); the stencil terms are gathered once and applied to all 2*Nq slots.
+template <typename R, int KIND>
+__global__ void __launch_bounds__(256) k_rhs(Geom G, int slot0, const cx<R>* __restrict__ coef,
+		const cx<R>* __restrict__ src, cx<R>* __restrict__ dst) {
+	int p = blockIdx.x * blockDim.x + threadIdx.x;
+	const int N = G.N, Nx = G.Nx, Ny = G.Ny;
+	if(p >= N) return;
+	const int c = blockIdx.y % 2, g = blockIdx.y / 2;
+	const Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
+	Terms<R> T;
+	bool ident = gather_terms<R, KIND>(st, c, p % Nx, p / Nx, T);
+	const size_t ss = 2 * (size_t)N;
+	const cx<R>* f = src + (size_t)g * G.spg * ss;
+	cx<R>* o = dst + (size_t)g * G.spg * ss + (size_t)c * N + p;
+	for(int sl = 0; sl < G.spg; sl++) {
+		const cx<R>* fs = f + sl * ss;
+		cx<R> v = ident ? fs[(size_t)c * N + p] : mk<R>(0, 0);
+		for(int t = 0; t < T.n; t++) v += T.c[t] * fs[(size_t)T.src[t] * N + T.tap[t]];
+		o[sl * ss] = v;
+	}
+}
+
+// x-line solve, group-cooperative form: one block per (line, comp, wavelength group) owns the
+// line for every (q, pol) slot of the group. The right-hand sides are formed with the stencil
+// terms gathered once per point and applied to all slots, the factor planes of the line are
+// loaded once into shared memory, and the block's warps solve the slots (one slot per warp at a
+// time) with the chunked scan of k_solve_xc.
+template <typename R, int M, int KIND>
+__global__ void __launch_bounds__(256) k_solve_xg(Geom G, int slot0, const cx<R>* __restrict__ coef,
+		const cx<R>* __restrict__ fac, size_t plane, const cx<double>* __restrict__ lsc,
+		const cx<R>* __restrict__ src, cx<R>* __restrict__ dst, const cx<R>* acc_in, cx<R>* acc_out) {
+	extern __shared__ unsigned char smem_raw[];
+	const int NWp = blockDim.x / 32;
+	const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+	const int Nx = G.Nx, Ny = G.Ny, N = G.N, spg = G.spg;
+	const int iy = blockIdx.x;
+	const int c = blockIdx.y % 2, g = blockIdx.y / 2;
+	const int n_unk = Nx - 1;
+	const int PITCH = 32 * (M + 1);
+	cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw);        // [spg][PITCH]
+	cx<R>* sf = buf + (size_t)spg * PITCH;                    // [NFAC][32*M]
+	const cx<R>* Fc = fac + ((size_t)g * 2 + c) * NFAC * plane + (size_t)iy * 32 * M;
+	for(int e = threadIdx.x; e < NFAC * 32 * M; e += blockDim.x) {
+		int f = e / (32 * M), i = e % (32 * M);
+		sf[e] = Fc[f * plane + i];
+	}
+	const Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
+	const size_t ss = 2 * (size_t)N;
+	const cx<R>* f0 = src + (size_t)g * spg * ss;
+	for(int e = threadIdx.x; e < n_unk; e += blockDim.x) {
+		Terms<R> T;
+		bool ident = gather_terms<R, KIND>(st, c, e, iy, T);
+		const int p = e + Nx * iy;
+		const int bi = (e / M) * (M + 1) + e % M;
+		for(int sl = 0; sl < spg; sl++) {
+			const cx<R>* fs = f0 + sl * ss;
+			cx<R> v = ident ? fs[(size_t)c * N + p] : mk<R>(0, 0);
+			for(int t = 0; t < T.n; t++) v += T.c[t] * fs[(size_t)T.src[t] * N + T.tap[t]];
+			buf[sl * PITCH + bi] = v;
+		}
+	}
+	__syncthreads();
+	const cx<double>* ls = lsc + (((size_t)g * 2 + c) * Ny + iy) * 2;
+	const cx<double> r0 = ls[0], rden = ls[1];
+	const int i0 = lane * M;
+	const int last = n_unk - 1, lane_last = last / M, k_last = last % M;
+	const cx<R> one = mk<R>(1, 0), zero = mk<R>(0, 0);
+	for(int sl = warp; sl < spg; sl += NWp) {
+		cx<R>* b = buf + sl * PITCH + lane * (M + 1);
+		cx<R> v[M];
+		cx<R> A = one, B = zero;
+#pragma unroll
+		for(int k = 0; k < M; k++) {
+			v[k] = zero;
+			if(i0 + k < n_unk) {
+				cx<R> a = sf[F_A * 32 * M + k * 32 + lane];
+				cx<R> bb = b[k] * sf[F_RB * 32 * M + k * 32 + lane];
+				v[k] = bb;
+				B = a * B + bb;
+				A = a * A;
+			}
+		}
+#pragma unroll
+		for(int o = 1; o < 32; o <<= 1) {
+			cx<R> Ap = shfl_up_c(A, o), Bp = shfl_up_c(B, o);
+			if(lane >= o) { B = A * Bp + B; A = A * Ap; }
+		}
+		cx<R> d = shfl_up_c(B, 1);
+		if(lane == 0) d = zero;
+		cx<R> acc = zero, dl = zero;
+#pragma unroll
+		for(int k = 0; k < M; k++) {
+			if(i0 + k < n_unk) {
+				d = sf[F_A * 32 * M + k * 32 + lane] * d + v[k];
+				v[k] = d;
+				acc += sf[F_W * 32 * M + k * 32 + lane] * d;
+			}
+			if(k == k_last) dl = d;
+		}
+#pragma unroll
+		for(int o = 16; o > 0; o >>= 1) acc += shfl_xor_c(acc, o);
+		dl = shfl_idx_c(dl, lane_last);
+		const cx<R> fr = cvt<R>((cvt<double>(acc) - r0 * cvt<double>(dl)) * rden);
+		A = one;
+		B = zero;
+#pragma unroll
+		for(int k = M - 1; k >= 0; k--) {
+			if(i0 + k < n_unk) {
+				cx<R> cc = sf[F_C * 32 * M + k * 32 + lane];
+				B = cc * B + v[k];
+				A = cc * A;
+			}
+		}
+#pragma unroll
+		for(int o = 1; o < 32; o <<= 1) {
+			cx<R> An = shfl_down_c(A, o), Bn = shfl_down_c(B, o);
+			if(lane + o < 32) { B = A * Bn + B; A = A * An; }
+		}
+		d = shfl_down_c(B, 1);
+		if(lane == 31) d = zero;
+#pragma unroll
+		for(int k = M - 1; k >= 0; k--) {
+			if(i0 + k < n_unk) {
+				d = sf[F_C * 32 * M + k * 32 + lane] * d + v[k];
+				b[k] = d - fr * sf[F_COR * 32 * M + k * 32 + lane];
+			}
+		}
+	}
+	__syncthreads();
+	for(int sl = 0; sl < spg; sl++) {
+		const size_t off = (size_t)(g * spg + sl) * ss + (size_t)c * N + (size_t)iy * Nx;
+		for(int e = threadIdx.x; e < Nx; e += blockDim.x) {
+			int ee = e == Nx - 1 ? 0 : e;
+			cx<R> x = buf[sl * PITCH + (ee / M) * (M + 1) + ee % M];
+			if(dst) dst[off + e] = x;
+			if(acc_out) acc_out[off + e] = acc_in[off + e] + x;
+		}
 	}
 }
 

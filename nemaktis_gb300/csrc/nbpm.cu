@@ -13,6 +13,7 @@
 #include <cmath>
 #include <complex>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <stdexcept>
@@ -205,7 +206,17 @@ struct Plan : PlanBase {
 	double last_slab_ms = 0;
 	size_t smem_limit = 0;
 	// line-solve configuration per sample (chunk sizes of the parallel kernels; 0 = sequential)
-	struct SolveCfg { int Mx = 0, My = 0, WY = 0, KSx = 1, KSy = 1; size_t plane_x = 0, plane_y = 0; };
+	// x: k_solve_xc with KSx slots per warp, or (NBPM_XMODE=1) the group-cooperative k_solve_xg
+	// (all slots of a wavelength per block) when its shared memory fits. y: ymode 0 = fused
+	// right-hand side (k_solve_yc with KSy slots per thread), 1 (NBPM_YMODE=1) = group-
+	// cooperative k_rhs + k_solve_yc(GIVEN). Defaults measured fastest on GB300.
+	struct SolveCfg {
+		int Mx = 0, My = 0, WY = 0, KSx = 1, KSy = 1;
+		bool xg = false;
+		int ymode = 0;
+		size_t plane_x = 0, plane_y = 0, smem_xg = 0;
+	};
+	DevBuf T3;
 	std::vector<SolveCfg> scfg;
 
 	Plan(const nbpm_options& o) : opt(o) {
@@ -319,8 +330,12 @@ struct Plan : PlanBase {
 		CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
 		smem_limit = (size_t)optin;
 		CK(cudaFuncSetAttribute(k_fft_lines<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit));
-		if(sizeof(R) == sizeof(float)) { set_solve_smem_x_f32((int)smem_limit); set_solve_smem_y_f32((int)smem_limit); }
-		else { set_solve_smem_x_f64((int)smem_limit); set_solve_smem_y_f64((int)smem_limit); }
+		if(sizeof(R) == sizeof(float)) {
+			set_solve_smem_x_f32((int)smem_limit); set_solve_smem_y_f32((int)smem_limit); set_solve_smem_xg_f32((int)smem_limit);
+		}
+		else {
+			set_solve_smem_x_f64((int)smem_limit); set_solve_smem_y_f64((int)smem_limit); set_solve_smem_xg_f64((int)smem_limit);
+		}
 		CK(cudaGetLastError());
 		allocate();
 	}
@@ -359,6 +374,12 @@ struct Plan : PlanBase {
 			if(opt.verbose)
 				std::printf("line solves: x M=%d KS=%d, y M=%d WY=%d KS=%d\n", sc.Mx, sc.KSx, sc.My, sc.WY, sc.KSy);
 			sc.plane_x = sc.Mx ? std::max(N, (size_t)h.s.Ny * 32 * sc.Mx) : N;
+			if(sc.Mx) {
+				sc.smem_xg = ((size_t)h.spg * 32 * (sc.Mx + 1) + (size_t)NFAC * 32 * sc.Mx) * sizeof(cx<R>);
+				sc.xg = false;  // measured slower than k_solve_xc on the 256x256 batched workload
+			}
+			if(const char* e = std::getenv("NBPM_XMODE")) sc.xg = sc.Mx && sc.smem_xg <= smem_limit && std::atoi(e) == 1;
+			if(const char* e = std::getenv("NBPM_YMODE")) sc.ymode = std::atoi(e);
 			sc.plane_y = N;
 			scfg.push_back(sc);
 			maxT = std::max(maxT, (size_t)ng * h.spg * 2 * N);
@@ -387,6 +408,9 @@ struct Plan : PlanBase {
 		}
 		T.alloc(sizeof(cx<R>) * maxT);
 		T2.alloc(sizeof(cx<R>) * maxT);
+		bool need_t3 = false;
+		for(auto& c : scfg) need_t3 |= (c.My > 0 && c.ymode == 1);
+		if(need_t3) T3.alloc(sizeof(cx<R>) * maxT);
 		Qring.alloc(sizeof(double) * maxQ);
 		coef.alloc(sizeof(cx<R>) * maxC);
 		diag.alloc(sizeof(cx<R>) * maxD);
@@ -399,7 +423,7 @@ struct Plan : PlanBase {
 		scr.alloc(sizeof(cx<R>) * maxScr);
 		stage.alloc(sizeof(cx<double>) * maxStage);
 		dev_bytes += T.bytes + T2.bytes + Qring.bytes + coef.bytes + diag.bytes + facx.bytes + facy.bytes +
-			lscx.bytes + lscy.bytes + scr.bytes + stage.bytes;
+			lscx.bytes + lscy.bytes + scr.bytes + stage.bytes + T3.bytes;
 	}
 
 	void upload() override {
@@ -668,8 +692,20 @@ struct Plan : PlanBase {
 		SolveLaunch L;
 		L.stream = cs;
 		if(dirn == 0) {
+			L.M = sc.Mx; L.kind = wood ? ST_WOOD_X : ST_EXPL_Y;
+			if(sc.xg) {
+				L.KS = 0;
+				L.grid = dim3((unsigned)Gm.Ny, (unsigned)(ng * 2));
+				L.block = dim3(256);
+				L.smem = sc.smem_xg;
+				launch(wood ? "wood_solve_x" : "expl_solve_x", bytes, [&] {
+					if(!launch_solve_xg<R>(L, Gm, slot0, C, fx_cur, sc.plane_x, lx_cur, src, dst, acc_in, acc_out))
+						throw BackendError(E_INTERNAL, "no x-solve instance");
+				});
+				return;
+			}
 			const int LT = 4;
-			L.M = sc.Mx; L.KS = sc.KSx; L.kind = wood ? ST_WOOD_X : ST_EXPL_Y;
+			L.KS = sc.KSx;
 			int nch = h.spg / L.KS;
 			L.grid = dim3((unsigned)((Gm.Ny + LT - 1) / LT), (unsigned)(ng * nch * 2));
 			L.block = dim3(32 * LT);
@@ -681,13 +717,24 @@ struct Plan : PlanBase {
 			});
 		}
 		else {
-			L.M = sc.My; L.KS = sc.KSy; L.kind = wood ? ST_WOOD_Y : ST_EXPL_X;
+			const cx<R>* rsrc = src;
+			if(sc.ymode == 1) {
+				// right-hand sides for all slots of each group, then a plain chunked solve
+				cx<R>* R3 = T3.as<cx<R>>();
+				launch(wood ? "wood_rhs_y" : "expl_rhs_y", fp * 2 + (double)Gm.N * ng * (wood ? 14 : 20) * sz, [&] {
+					dim3 gr((unsigned)((Gm.N + 255) / 256), (unsigned)(ng * 2));
+					if(wood) k_rhs<R, ST_WOOD_Y><<<gr, 256, 0, cs>>>(Gm, slot0, C, src, R3);
+					else k_rhs<R, ST_EXPL_X><<<gr, 256, 0, cs>>>(Gm, slot0, C, src, R3);
+				});
+				rsrc = R3;
+			}
+			L.M = sc.My; L.KS = sc.KSy; L.kind = sc.ymode == 1 ? ST_GIVEN : (wood ? ST_WOOD_Y : ST_EXPL_X);
 			int nch = h.spg / L.KS;
 			L.grid = dim3((unsigned)((Gm.Nx + 31) / 32), (unsigned)(ng * nch * 2));
 			L.block = dim3(32, sc.WY);
 			L.smem = (size_t)(4 * L.KS * sc.WY * 32 + 2 * L.KS * 32) * sizeof(cx<R>);
 			launch(wood ? "wood_solve_y" : "expl_solve_y", bytes, [&] {
-				if(!launch_solve_yc<R>(L, Gm, slot0, nch, C, fy_cur, sc.plane_y, ly_cur, src,
+				if(!launch_solve_yc<R>(L, Gm, slot0, nch, C, fy_cur, sc.plane_y, ly_cur, rsrc,
 						dst, acc_in, acc_out))
 					throw BackendError(E_INTERNAL, "no y-solve instance");
 			});

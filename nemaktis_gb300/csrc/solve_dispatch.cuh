@@ -22,6 +22,11 @@ bool launch_solve_xc(const SolveLaunch& L, Geom G, int slot0, int nch, const cx<
 template <typename R>
 bool launch_solve_yc(const SolveLaunch& L, Geom G, int slot0, int nch, const cx<R>* coef, const cx<R>* fac,
 	size_t plane, const cx<double>* lsc, const cx<R>* src, cx<R>* dst, const cx<R>* ai, cx<R>* ao);
+template <typename R>
+bool launch_solve_xg(const SolveLaunch& L, Geom G, int slot0, const cx<R>* coef, const cx<R>* fac, size_t plane,
+	const cx<double>* lsc, const cx<R>* src, cx<R>* dst, const cx<R>* ai, cx<R>* ao);
+void set_solve_smem_xg_f32(int bytes);
+void set_solve_smem_xg_f64(int bytes);
 void set_solve_smem_x_f32(int bytes);
 void set_solve_smem_x_f64(int bytes);
 void set_solve_smem_y_f32(int bytes);

@@ -19,6 +19,7 @@ bool launch_solve_yc<float>(const SolveLaunch& L, Geom G, int slot0, int nch, co
 		const cx<float>* ai, cx<float>* ao) {
 	NBPM_YC_PAIRS(ST_EXPL_X)
 	NBPM_YC_PAIRS(ST_WOOD_Y)
+	NBPM_YC_PAIRS(ST_GIVEN)
 	return false;
 }
 
@@ -31,6 +32,7 @@ bool launch_solve_yc<float>(const SolveLaunch& L, Geom G, int slot0, int nch, co
 void set_solve_smem_y_f32(int bytes) {
 	NBPM_YA_PAIRS(ST_EXPL_X)
 	NBPM_YA_PAIRS(ST_WOOD_Y)
+	NBPM_YA_PAIRS(ST_GIVEN)
 }
 
 }  // namespace nbpm
