@@ -221,13 +221,19 @@ def run_ours(args):
     e2e = e2e_measure(samples, prec, args.e2e_steps)
 
     hbm, src = peaks()
+    # DRAM bytes per launch of the dominant kernel from one ncu capture (dram__bytes_read.sum +
+    # dram__bytes_write.sum), scaled to this workload's launch by the slots it processes; the
+    # capture and its command are summarised under profiles/.
+    TRAFFIC = {("config3", "fp32", "wood_solve_x"): (2 * 723.8e6, "profiles/solve_xc_yc_koehler_256x256x8_fp32.md")}
     roof = None
     if prof:
         top = max(prof, key=lambda k: prof[k]["ms"])
         r = prof[top]
         ach = r["bytes"] / (r["ms"] / r["launches"] / 1e3) / 1e9 / r["launches"] if r["launches"] else 0
+        tr = TRAFFIC.get((args.workload, args.precision, top))
         roof = {"bound": "hbm", "kernel": top, "achieved": ach, "peak": hbm, "unit": "GB/s",
-                "frac": ach / hbm, "peak_source": src, "traffic": None,
+                "frac": ach / hbm, "peak_source": src, "traffic": tr[0] if tr else None,
+                "traffic_source": tr[1] if tr else None,
                 "share_of_step": r["ms"] / sum(v["ms"] for v in prof.values()),
                 "algorithmic_bytes_per_launch": r["bytes"] / max(1, r["launches"])}
     cpu = None

@@ -24,7 +24,8 @@ enum {
 	NBPM_ERR_CUDA = 4,      /* CUDA runtime failure (no device, launch error, ...) */
 	NBPM_ERR_MEMORY = 5,    /* device memory exhausted or above the configured budget */
 	NBPM_ERR_ARG = 6,       /* invalid argument (null pointer, bad option, bad handle) */
-	NBPM_ERR_INTERNAL = 7
+	NBPM_ERR_INTERNAL = 7,
+	NBPM_ERR_TIMEOUT = 8     /* nbpm_server_wait gave up before the request finished */
 };
 
 enum { NBPM_FP64 = 0, NBPM_FP32 = 1 };
@@ -143,6 +144,135 @@ int nbpm_periodic_tridiag_solve(int L, int nlines, const double* inf, const doub
  * it and must be serialised by the caller. No counterpart in the reference. */
 int nbpm_periodic_tridiag_solve_noalloc(int L, int nlines, const double* inf, const double* mid,
 		const double* sup, const double* rhs, double* x, void* stream);
+
+/* ---- Serving: continuous batching of samples on one GPU ----
+ *
+ * A thread-safe submit / poll interface over the same plans (no counterpart in the reference,
+ * whose backend runs one blocking call per sample, bpm_backend.cpp:7-164). A server thread
+ * admits queued requests first-come first-served while their estimated device memory fits
+ * the budget, advances every request in flight by slabs_per_round slabs per scheduling round
+ * (each on its own CUDA streams, so requests of different meshes run side by side and new
+ * ones join at slab boundaries), and copies each finished request's screen fields into its
+ * E_field_vals buffer. A request runs the same launch sequence as a standalone run with the
+ * same precision, so its result does not depend on the other requests. */
+typedef struct nbpm_server nbpm_server;
+
+typedef struct nbpm_server_options {
+	int precision;          /* NBPM_FP32 (default) or NBPM_FP64 */
+	int device;
+	double hbm_budget_gb;   /* admission budget for the requests in flight (default 150) */
+	int slabs_per_round;    /* slabs each request in flight advances per round (default 8) */
+	int max_active;         /* requests in flight at most; 0: limited by the budget only */
+} nbpm_server_options;
+
+enum { NBPM_REQ_QUEUED = 0, NBPM_REQ_RUNNING = 1, NBPM_REQ_DONE = 2, NBPM_REQ_FAILED = 3, NBPM_REQ_CANCELLED = 4 };
+
+typedef struct nbpm_request_info {
+	int state;               /* NBPM_REQ_* */
+	int error_code;          /* NBPM_ERR_* when FAILED */
+	char error[256];
+	long long voxel_steps;
+	long long device_bytes;  /* admission estimate */
+	double queue_ms;         /* submit -> admission */
+	double latency_ms;       /* submit -> result in E_field_vals */
+} nbpm_request_info;
+
+typedef struct nbpm_server_stats {
+	int queued, running;
+	long long done, failed, cancelled;
+	long long bytes_in_use, peak_bytes, budget_bytes;
+	long long voxel_steps_done;
+	int rounds;
+} nbpm_server_stats;
+
+void nbpm_default_server_options(nbpm_server_options* opts);
+/* Starts the server thread; the device is first used when a request is admitted. */
+int nbpm_server_create(const nbpm_server_options* opts, nbpm_server** out);
+/* Cancels queued requests, lets the ones in flight finish, stops the thread. */
+int nbpm_server_destroy(nbpm_server* server);
+/* Validates a request (the reference's messages and codes, as nbpm_run_backend_ex) and
+ * queues it; fails with NBPM_ERR_MEMORY when it alone exceeds the budget. The director, mask
+ * and E_field_vals buffers are borrowed until the request is DONE, FAILED or CANCELLED. */
+int nbpm_server_submit(nbpm_server* server, const nbpm_sample* request, long long* id);
+int nbpm_server_poll(nbpm_server* server, long long id, nbpm_request_info* info);
+/* Blocks until the request leaves the queue and the GPU (timeout_s < 0: no limit);
+ * NBPM_ERR_TIMEOUT when the time runs out first. */
+int nbpm_server_wait(nbpm_server* server, long long id, double timeout_s, nbpm_request_info* info);
+/* Queued requests are dropped; requests in flight stop at the next round boundary. */
+int nbpm_server_cancel(nbpm_server* server, long long id);
+/* Forgets a finished request (its id becomes unknown). */
+int nbpm_server_release(nbpm_server* server, long long id);
+int nbpm_server_get_stats(nbpm_server* server, nbpm_server_stats* stats);
+
+/* ---- Microscope stage: objective focalisation and incoherent spectra (FP64) ----
+ *
+ * Replaces the Python post-processing that follows the backend call:
+ *   OpticalFields (HighLevelPythonInterface/nemaktis/light_propagator.py:448-719): wavevector
+ *   grid :576-596, objective filter and NA mask :614-646, update_NA_objective :702-705,
+ *   focus_fields :708-719;
+ *   FieldViewer (nemaktis/field_viewer.py): _update_specter :348-388 and
+ *   _update_averaged_specter :391-455 (Jones matrices :472-513, Koehler weights :515-518).
+ * The fields stay on the device between focalisation and spectrum; the colour conversion of
+ * _update_POM_image (dtmm colour tables) is not part of the library. */
+typedef struct nbpm_microscope nbpm_microscope;
+
+typedef struct nbpm_microscope_params {
+	int Nx, Ny;                  /* mesh_dimensions */
+	double Lx, Ly;               /* mesh_lengths (spacing L / max(1, N-1)) */
+	int n_wavelengths;
+	const double* wavelengths;   /* µm, n_wavelengths values */
+	const double* n_out;         /* index of the output medium per wavelength; NULL: 1 */
+	double max_NA_objective;
+	double max_NA_condenser;
+	int N_radial_wavevectors;
+	int koehler_1D;
+	double zfoc_NA_corr;
+	int n_wavevectors;           /* > 0: explicit wavevectors (n x 2); 0: the OpticalFields grid */
+	const double* wavevectors;
+	int device;
+} nbpm_microscope_params;
+
+enum { NBPM_WAVEPLATE_NONE = 0, NBPM_WAVEPLATE_QUARTER = 1, NBPM_WAVEPLATE_HALF = 2, NBPM_WAVEPLATE_TINT = 3 };
+
+/* FieldViewer optical elements (angles in degrees) and condenser aperture. */
+typedef struct nbpm_viewer_settings {
+	int polariser;
+	double polariser_angle;
+	int analyser;
+	double analyser_angle;
+	int lower_waveplate;         /* NBPM_WAVEPLATE_* between polariser and sample */
+	double lower_waveplate_angle;
+	int upper_waveplate;         /* NBPM_WAVEPLATE_* between sample and analyser */
+	double upper_waveplate_angle;
+	double NA_condenser;
+} nbpm_viewer_settings;
+
+/* All elements off, NA_condenser 0. */
+void nbpm_default_viewer_settings(nbpm_viewer_settings* s);
+/* Allocates the device buffers (two field arrays, filter tables, spectrum) and tabulates the
+ * objective filter; fields start at zero. */
+int nbpm_microscope_create(const nbpm_microscope_params* params, nbpm_microscope** out);
+int nbpm_microscope_destroy(nbpm_microscope* m);
+int nbpm_microscope_shape(const nbpm_microscope* m, int* n_wavelengths, int* n_wavevectors, int* Ny, int* Nx);
+/* Wavevectors in use (n_wavevectors x 2); n must equal n_wavevectors. */
+int nbpm_microscope_wavevectors(const nbpm_microscope* m, double* out, int n);
+/* OpticalFields.vals setter: (Nl, Nq, 4, Ny, Nx) complex128 from host memory. */
+int nbpm_microscope_set_fields(nbpm_microscope* m, const double* vals, long long n_vals);
+/* The same from the device-resident output of sample `sample` of an executed plan (FP32
+ * plans are widened to FP64), without a host round trip. */
+int nbpm_microscope_set_fields_from_plan(nbpm_microscope* m, nbpm_plan* plan, int sample);
+/* update_NA_objective(NA_objective) then focus_fields(z_focus): NA is clamped to
+ * [0, max_NA_objective]. */
+int nbpm_microscope_focus(nbpm_microscope* m, double z_focus, double NA_objective);
+/* OpticalFields.focused_vals to host memory, (Nl, Nq, 4, Ny, Nx) complex128. */
+int nbpm_microscope_get_focused(nbpm_microscope* m, double* out, long long n_vals);
+/* FieldViewer._update_specter + _update_averaged_specter on the focused fields: writes the
+ * q-averaged spectrum, (Ny, Nx, n_wavelengths) float64, n = Ny*Nx*n_wavelengths. */
+int nbpm_microscope_spectrum(nbpm_microscope* m, const nbpm_viewer_settings* settings, double* spectrum,
+		long long n);
+/* Device time of the last focus and spectrum calls (ms) and device memory held (bytes). */
+int nbpm_microscope_timing(const nbpm_microscope* m, double* focus_ms, double* spectrum_ms,
+		long long* device_bytes);
 
 /* Message of the last failure on this thread ("" if none). */
 const char* nbpm_last_error(void);

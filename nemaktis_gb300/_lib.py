@@ -11,7 +11,7 @@ from . import build as _build
 c_int, c_double, c_char_p, c_void_p, c_ll = ctypes.c_int, ctypes.c_double, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_longlong
 
 ERRORS = {0: "NBPM_OK", 1: "NBPM_ERR_SETTINGS", 2: "NBPM_ERR_SIZE", 3: "NBPM_ERR_EXPR", 4: "NBPM_ERR_CUDA",
-          5: "NBPM_ERR_MEMORY", 6: "NBPM_ERR_ARG", 7: "NBPM_ERR_INTERNAL"}
+          5: "NBPM_ERR_MEMORY", 6: "NBPM_ERR_ARG", 7: "NBPM_ERR_INTERNAL", 8: "NBPM_ERR_TIMEOUT"}
 FP64, FP32 = 0, 1
 
 
@@ -38,6 +38,39 @@ class Sample(ctypes.Structure):
                 ("E_field_vals", c_void_p), ("n_E_vals", c_int)]
 
 
+class MicroscopeParams(ctypes.Structure):
+    _fields_ = [("Nx", c_int), ("Ny", c_int), ("Lx", c_double), ("Ly", c_double), ("n_wavelengths", c_int),
+                ("wavelengths", c_void_p), ("n_out", c_void_p), ("max_NA_objective", c_double),
+                ("max_NA_condenser", c_double), ("N_radial_wavevectors", c_int), ("koehler_1D", c_int),
+                ("zfoc_NA_corr", c_double), ("n_wavevectors", c_int), ("wavevectors", c_void_p), ("device", c_int)]
+
+
+class ViewerSettings(ctypes.Structure):
+    _fields_ = [("polariser", c_int), ("polariser_angle", c_double), ("analyser", c_int),
+                ("analyser_angle", c_double), ("lower_waveplate", c_int), ("lower_waveplate_angle", c_double),
+                ("upper_waveplate", c_int), ("upper_waveplate_angle", c_double), ("NA_condenser", c_double)]
+
+
+class ServerOptions(ctypes.Structure):
+    _fields_ = [("precision", c_int), ("device", c_int), ("hbm_budget_gb", c_double), ("slabs_per_round", c_int),
+                ("max_active", c_int)]
+
+
+class RequestInfo(ctypes.Structure):
+    _fields_ = [("state", c_int), ("error_code", c_int), ("error", ctypes.c_char * 256), ("voxel_steps", c_ll),
+                ("device_bytes", c_ll), ("queue_ms", c_double), ("latency_ms", c_double)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("queued", c_int), ("running", c_int), ("done", c_ll), ("failed", c_ll), ("cancelled", c_ll),
+                ("bytes_in_use", c_ll), ("peak_bytes", c_ll), ("budget_bytes", c_ll), ("voxel_steps_done", c_ll),
+                ("rounds", c_int)]
+
+
+REQ_STATES = {0: "queued", 1: "running", 2: "done", 3: "failed", 4: "cancelled"}
+
+WAVEPLATES = {"No": 0, "Quarter-wave": 1, "Half-wave": 2, "Tint-sensitive": 3}
+
 EXPORTS = {
     "nbpm_default_options": (None, [ctypes.POINTER(Options)]),
     "nbpm_run_backend_without_mask": (c_int, [c_char_p, c_void_p, c_int, c_void_p, c_int]),
@@ -58,6 +91,28 @@ EXPORTS = {
     "nbpm_periodic_tridiag_solve": (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "nbpm_periodic_tridiag_solve_noalloc": (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                                     c_void_p]),
+    "nbpm_default_server_options": (None, [ctypes.POINTER(ServerOptions)]),
+    "nbpm_server_create": (c_int, [ctypes.POINTER(ServerOptions), ctypes.POINTER(c_void_p)]),
+    "nbpm_server_destroy": (c_int, [c_void_p]),
+    "nbpm_server_submit": (c_int, [c_void_p, ctypes.POINTER(Sample), ctypes.POINTER(c_ll)]),
+    "nbpm_server_poll": (c_int, [c_void_p, c_ll, ctypes.POINTER(RequestInfo)]),
+    "nbpm_server_wait": (c_int, [c_void_p, c_ll, c_double, ctypes.POINTER(RequestInfo)]),
+    "nbpm_server_cancel": (c_int, [c_void_p, c_ll]),
+    "nbpm_server_release": (c_int, [c_void_p, c_ll]),
+    "nbpm_server_get_stats": (c_int, [c_void_p, ctypes.POINTER(ServerStats)]),
+    "nbpm_default_viewer_settings": (None, [ctypes.POINTER(ViewerSettings)]),
+    "nbpm_microscope_create": (c_int, [ctypes.POINTER(MicroscopeParams), ctypes.POINTER(c_void_p)]),
+    "nbpm_microscope_destroy": (c_int, [c_void_p]),
+    "nbpm_microscope_shape": (c_int, [c_void_p, ctypes.POINTER(c_int), ctypes.POINTER(c_int), ctypes.POINTER(c_int),
+                                      ctypes.POINTER(c_int)]),
+    "nbpm_microscope_wavevectors": (c_int, [c_void_p, c_void_p, c_int]),
+    "nbpm_microscope_set_fields": (c_int, [c_void_p, c_void_p, c_ll]),
+    "nbpm_microscope_set_fields_from_plan": (c_int, [c_void_p, c_void_p, c_int]),
+    "nbpm_microscope_focus": (c_int, [c_void_p, c_double, c_double]),
+    "nbpm_microscope_get_focused": (c_int, [c_void_p, c_void_p, c_ll]),
+    "nbpm_microscope_spectrum": (c_int, [c_void_p, ctypes.POINTER(ViewerSettings), c_void_p, c_ll]),
+    "nbpm_microscope_timing": (c_int, [c_void_p, ctypes.POINTER(c_double), ctypes.POINTER(c_double),
+                                       ctypes.POINTER(c_ll)]),
     "nbpm_last_error": (c_char_p, []),
     "nbpm_version": (c_char_p, []),
 }

@@ -22,44 +22,36 @@ struct FftPlan1D {
 	int radix[FFT_MAX_STAGES];
 };
 
+// Radix sequence for a length-n line: 4s, then 2s, then odd primes in increasing order.
+// Returns false when n needs more than FFT_MAX_STAGES stages.
+inline bool fft_plan_1d(int n, FftPlan1D& P) {
+	P.n = n;
+	P.nst = 0;
+	auto push = [&](int r) {
+		if(P.nst >= FFT_MAX_STAGES) return false;
+		P.radix[P.nst++] = r;
+		return true;
+	};
+	while(n % 4 == 0 && n > 1) { if(!push(4)) return false; n /= 4; }
+	while(n % 2 == 0) { if(!push(2)) return false; n /= 2; }
+	for(int p = 3; n > 1 && p * p <= n; p += 2)
+		while(n % p == 0) { if(!push(p)) return false; n /= p; }
+	if(n > 1 && !push(n)) return false;
+	return true;
+}
+
 template <typename R>
 __device__ __forceinline__ cx<R> tw_get(const cx<R>* tw, int idx, int sign) {
 	cx<R> w = tw[idx];
 	return sign > 0 ? conj(w) : w;
 }
 
-// Transform `nlines` lines of length P.n. Line l starts at base(l) = (l / lines_per_plane)
-// * plane_stride + (l % lines_per_plane) * line_stride and its elements are elem_stride apart.
+// Mixed-radix Stockham stages on nl lines held in shared memory (pitch n+1): `in` holds the
+// input; returns the buffer (in or out) that holds the transform. Ends with __syncthreads().
 template <typename R>
-__global__ void k_fft_lines(cx<R>* data, FftPlan1D P, int nlines, int lines_per_plane,
-		long long plane_stride, long long line_stride, long long elem_stride, int lpb,
-		const cx<R>* __restrict__ tw, int sign) {
-	extern __shared__ unsigned char smem_raw[];
-	cx<R>* sA = reinterpret_cast<cx<R>*>(smem_raw);
+__device__ cx<R>* fft_stages(cx<R>* in, cx<R>* out, const FftPlan1D& P, int nl, const cx<R>* __restrict__ tw,
+		int sign) {
 	const int n = P.n, pitch = n + 1;
-	cx<R>* sB = sA + (size_t)lpb * pitch;
-	int l0 = blockIdx.x * lpb;
-	int nl = min(lpb, nlines - l0);
-	if(nl <= 0) return;
-	auto base = [&](int l) {
-		return (long long)(l / lines_per_plane) * plane_stride + (long long)(l % lines_per_plane) * line_stride;
-	};
-	int tot = nl * n;
-	if(elem_stride == 1) {
-		for(int e = threadIdx.x; e < tot; e += blockDim.x) {
-			int li = e / n, i = e % n;
-			sA[li * pitch + i] = data[base(l0 + li) + i];
-		}
-	}
-	else {
-		for(int e = threadIdx.x; e < tot; e += blockDim.x) {
-			int li = e % nl, i = e / nl;
-			sA[li * pitch + i] = data[base(l0 + li) + (long long)i * elem_stride];
-		}
-	}
-	__syncthreads();
-	cx<R>* in = sA;
-	cx<R>* out = sB;
 	int Ns = 1;
 	for(int st = 0; st < P.nst; st++) {
 		int p = P.radix[st];
@@ -120,6 +112,42 @@ __global__ void k_fft_lines(cx<R>* data, FftPlan1D P, int nlines, int lines_per_
 		cx<R>* t = in; in = out; out = t;
 		Ns *= p;
 	}
+	return in;
+}
+
+// Transform `nlines` lines of length P.n. Line l starts at base(l) = (l / lines_per_plane)
+// * plane_stride + (l % lines_per_plane) * line_stride and its elements are elem_stride apart.
+// Reads from `src` (data when null) and writes to `data`.
+template <typename R>
+static __global__ void k_fft_lines(cx<R>* data, const cx<R>* src, FftPlan1D P, int nlines, int lines_per_plane,
+		long long plane_stride, long long line_stride, long long elem_stride, int lpb,
+		const cx<R>* __restrict__ tw, int sign) {
+	extern __shared__ unsigned char smem_raw[];
+	cx<R>* sA = reinterpret_cast<cx<R>*>(smem_raw);
+	const int n = P.n, pitch = n + 1;
+	cx<R>* sB = sA + (size_t)lpb * pitch;
+	int l0 = blockIdx.x * lpb;
+	int nl = min(lpb, nlines - l0);
+	if(nl <= 0) return;
+	const cx<R>* in_data = src ? src : data;
+	auto base = [&](int l) {
+		return (long long)(l / lines_per_plane) * plane_stride + (long long)(l % lines_per_plane) * line_stride;
+	};
+	int tot = nl * n;
+	if(elem_stride == 1) {
+		for(int e = threadIdx.x; e < tot; e += blockDim.x) {
+			int li = e / n, i = e % n;
+			sA[li * pitch + i] = in_data[base(l0 + li) + i];
+		}
+	}
+	else {
+		for(int e = threadIdx.x; e < tot; e += blockDim.x) {
+			int li = e % nl, i = e / nl;
+			sA[li * pitch + i] = in_data[base(l0 + li) + (long long)i * elem_stride];
+		}
+	}
+	__syncthreads();
+	cx<R>* in = fft_stages<R>(sA, sB, P, nl, tw, sign);
 	if(elem_stride == 1) {
 		for(int e = threadIdx.x; e < tot; e += blockDim.x) {
 			int li = e / n, i = e % n;

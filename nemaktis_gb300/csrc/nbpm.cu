@@ -23,6 +23,7 @@
 #include "../../include/nbpm.h"
 #include "bpm_kernels.cuh"
 #include "fft_kernels.cuh"
+#include "plan_iface.h"
 #include "host_settings.h"
 #include "solve_dispatch.cuh"
 
@@ -81,16 +82,6 @@ struct SampleHost {
 	DevBuf dir, dmask, dwts, F, E0, gpsd, shiftd, partial, wl, nout, qv;
 };
 
-static std::vector<int> fft_radices(int n) {
-	std::vector<int> r;
-	while(n % 4 == 0 && n > 1) { r.push_back(4); n /= 4; }
-	while(n % 2 == 0) { r.push_back(2); n /= 2; }
-	for(int p = 3; n > 1 && p * p <= n; p += 2)
-		while(n % p == 0) { r.push_back(p); n /= p; }
-	if(n > 1) r.push_back(n);
-	return r;
-}
-
 // Nearest-index divisions used by the shift operator are computed on the device from nref;
 // this kernel restates the SimpleShiftOperator constructor (SimpleShiftOperator.cpp:3-50).
 __global__ void k_nref_final(int ngroups, int nblocks, size_t nvox, const double* __restrict__ partial,
@@ -142,17 +133,6 @@ __global__ void k_shift_params(int ngroups, int Nq, int Nx, int Ny, const GroupP
 // ---------------------------------------------------------------------------------------
 // Plan
 // ---------------------------------------------------------------------------------------
-struct PlanBase {
-	virtual ~PlanBase() {}
-	virtual void upload() = 0;
-	virtual void execute(nbpm_timing* t) = 0;
-	virtual void download() = 0;
-	virtual long long device_bytes() const = 0;
-	virtual double slab_ms() const = 0;
-	virtual void profile(std::vector<std::string>& names, std::vector<double>& ms, std::vector<int>& cnt,
-		std::vector<double>& bytes) = 0;
-};
-
 template <typename R>
 struct Plan : PlanBase {
 	nbpm_options opt;
@@ -223,6 +203,9 @@ struct Plan : PlanBase {
 		for(auto& e : ev) e = nullptr;
 	}
 	~Plan() override {
+		if(stream) cudaStreamSynchronize(stream);
+		if(streamB) cudaStreamSynchronize(streamB);
+		if(eDone) cudaEventDestroy(eDone);
 		for(auto e : evpool) cudaEventDestroy(e);
 		if(gexec) cudaGraphExecDestroy(gexec);
 		for(auto& e : ev) if(e) cudaEventDestroy(e);
@@ -247,7 +230,7 @@ struct Plan : PlanBase {
 		return tw_tables.back().second;
 	}
 
-	void setup(int ns, const nbpm_sample* samples) {
+	void setup_host(int ns, const nbpm_sample* samples) {
 		for(int i = 0; i < ns; i++) {
 			const nbpm_sample& in = samples[i];
 			if(!in.json_str || !in.lc_field_vals || !in.E_field_vals)
@@ -317,6 +300,25 @@ struct Plan : PlanBase {
 			h->index = (int)S.size();
 			S.push_back(std::move(h));
 		}
+	}
+
+	// Device memory the plan will hold, from the host-side settings alone.
+	long long estimate_bytes() override {
+		dry = true;
+		allocate();
+		dry = false;
+		long long b = dev_bytes;
+		dev_bytes = 0;
+		scfg.clear();
+		return b;
+	}
+
+	void setup(int ns, const nbpm_sample* samples) {
+		setup_host(ns, samples);
+		setup_device();
+	}
+
+	void setup_device() override {
 		// Host-side validation is complete; only now touch the device.
 		CK(cudaSetDevice(opt.device));
 		CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
@@ -345,7 +347,16 @@ struct Plan : PlanBase {
 		return std::max(1, g);
 	}
 
+	// Sizes every device buffer; with dry set, only adds up the bytes (admission estimates).
+	bool dry = false;
+	void dalloc(DevBuf& b, size_t bytes) {
+		if(dry) b.bytes = bytes;
+		else b.alloc(bytes);
+	}
+
 	void allocate() {
+		scfg.clear();
+		dev_bytes = 0;
 		size_t maxT = 0, maxQ = 0, maxC = 0, maxD = 0, maxFx = 0, maxL = 0, maxScr = 0, maxStage = 0;
 		for(auto& hp : S) {
 			SampleHost& h = *hp;
@@ -391,37 +402,37 @@ struct Plan : PlanBase {
 			maxScr = std::max(maxScr, (size_t)2 * ng * 2 * 2 * N);  // x and y halves
 			if(sizeof(R) != sizeof(double)) maxStage = std::max(maxStage, (size_t)h.slots * 2 * N);
 			// per-sample buffers
-			h.dir.alloc(sizeof(double) * h.nvox * h.fd);
-			if(h.has_mask) h.dmask.alloc(h.nvox);
-			if(h.has_wts) h.dwts.alloc(sizeof(double) * h.wts.size());
-			h.F.alloc(sizeof(cx<R>) * (size_t)h.slots * 2 * N);
-			if(h.s.beam_type == 2) h.E0.alloc(sizeof(cx<R>) * (size_t)h.slots * 2 * N);
-			h.gpsd.alloc(sizeof(GroupParams) * h.G);
-			h.shiftd.alloc(sizeof(ShiftParams) * h.G * h.Nq);
-			h.partial.alloc(sizeof(double) * h.G * 1024);
-			h.wl.alloc(sizeof(double) * h.G);
-			h.nout.alloc(sizeof(double) * h.G);
-			h.qv.alloc(sizeof(double) * 2 * h.Nq);
+			dalloc(h.dir, sizeof(double) * h.nvox * h.fd);
+			if(h.has_mask) dalloc(h.dmask, h.nvox);
+			if(h.has_wts) dalloc(h.dwts, sizeof(double) * h.wts.size());
+			dalloc(h.F, sizeof(cx<R>) * (size_t)h.slots * 2 * N);
+			if(h.s.beam_type == 2) dalloc(h.E0, sizeof(cx<R>) * (size_t)h.slots * 2 * N);
+			dalloc(h.gpsd, sizeof(GroupParams) * h.G);
+			dalloc(h.shiftd, sizeof(ShiftParams) * h.G * h.Nq);
+			dalloc(h.partial, sizeof(double) * h.G * 1024);
+			dalloc(h.wl, sizeof(double) * h.G);
+			dalloc(h.nout, sizeof(double) * h.G);
+			dalloc(h.qv, sizeof(double) * 2 * h.Nq);
 			dev_bytes += h.dir.bytes + h.dmask.bytes + h.dwts.bytes + h.F.bytes + h.E0.bytes;
-			twiddles(h.s.Nx);
-			twiddles(h.s.Ny);
+			if(dry) dev_bytes += sizeof(cx<R>) * (size_t)(h.s.Nx + h.s.Ny);
+			else { twiddles(h.s.Nx); twiddles(h.s.Ny); }
 		}
-		T.alloc(sizeof(cx<R>) * maxT);
-		T2.alloc(sizeof(cx<R>) * maxT);
+		dalloc(T, sizeof(cx<R>) * maxT);
+		dalloc(T2, sizeof(cx<R>) * maxT);
 		bool need_t3 = false;
 		for(auto& c : scfg) need_t3 |= (c.My > 0 && c.ymode == 1);
-		if(need_t3) T3.alloc(sizeof(cx<R>) * maxT);
-		Qring.alloc(sizeof(double) * maxQ);
-		coef.alloc(sizeof(cx<R>) * maxC);
-		diag.alloc(sizeof(cx<R>) * maxD);
+		if(need_t3) dalloc(T3, sizeof(cx<R>) * maxT);
+		dalloc(Qring, sizeof(double) * maxQ);
+		dalloc(coef, sizeof(cx<R>) * maxC);
+		dalloc(diag, sizeof(cx<R>) * maxD);
 		facx_half = facy_half = maxFx;
 		lsc_half = maxL;
-		facx.alloc(sizeof(cx<R>) * maxFx * 2);
-		facy.alloc(sizeof(cx<R>) * maxFx * 2);
-		lscx.alloc(sizeof(cx<double>) * maxL * 2);
-		lscy.alloc(sizeof(cx<double>) * maxL * 2);
-		scr.alloc(sizeof(cx<R>) * maxScr);
-		stage.alloc(sizeof(cx<double>) * maxStage);
+		dalloc(facx, sizeof(cx<R>) * maxFx * 2);
+		dalloc(facy, sizeof(cx<R>) * maxFx * 2);
+		dalloc(lscx, sizeof(cx<double>) * maxL * 2);
+		dalloc(lscy, sizeof(cx<double>) * maxL * 2);
+		dalloc(scr, sizeof(cx<R>) * maxScr);
+		dalloc(stage, sizeof(cx<double>) * maxStage);
 		dev_bytes += T.bytes + T2.bytes + Qring.bytes + coef.bytes + diag.bytes + facx.bytes + facy.bytes +
 			lscx.bytes + lscy.bytes + scr.bytes + stage.bytes + T3.bytes;
 	}
@@ -479,10 +490,7 @@ struct Plan : PlanBase {
 			int n = pass == 0 ? Nx : Ny;
 			if(n == 1) continue;
 			FftPlan1D P;
-			auto rad = fft_radices(n);
-			if((int)rad.size() > FFT_MAX_STAGES) throw BackendError(E_INTERNAL, "FFT plan too deep");
-			P.n = n; P.nst = (int)rad.size();
-			for(int i = 0; i < P.nst; i++) P.radix[i] = rad[i];
+			if(!fft_plan_1d(n, P)) throw BackendError(E_INTERNAL, "FFT plan too deep");
 			size_t per_line = 2 * (size_t)(n + 1) * sizeof(cx<R>);
 			if(per_line > smem_limit)
 				throw BackendError(E_SETTINGS, "FFT line length " + std::to_string(n) + " exceeds shared memory");
@@ -499,7 +507,7 @@ struct Plan : PlanBase {
 			cx<R>* tw = twiddles(n);
 			double bytes = 2.0 * sizeof(cx<R>) * (double)nplanes * Nx * Ny;
 			launch(pass == 0 ? "fft_rows" : "fft_cols", bytes, [&] {
-				k_fft_lines<R><<<blocks, threads, smem, cs>>>(F, P, nlines, lpp, ps, ls, es, lpb, tw, sign);
+				k_fft_lines<R><<<blocks, threads, smem, cs>>>(F, nullptr, P, nlines, lpp, ps, ls, es, lpb, tw, sign);
 			});
 		}
 	}
@@ -510,116 +518,165 @@ struct Plan : PlanBase {
 		for(auto& hp : S) record_sample(*hp);
 	}
 
-	void record_sample(SampleHost& h) {
+	// State of one pass of wavelength groups through the slab loop. Kept between calls when a
+	// sample is advanced a few slabs at a time (serving), so that the launch sequence is the
+	// same as in one uninterrupted recording.
+	struct PassState {
+		int ga = 0, ng = 0, slot0 = 0, nsl = 0;
+		int iz = 0;  // next slab
+		const GroupParams* gps = nullptr;
+		cx<R>* Fp = nullptr;
+		cx<R>* Tb = nullptr;
+		cx<R>* T2b = nullptr;
+		double* Qr[2] = {nullptr, nullptr};
+		cx<R>* Cring[2] = {nullptr, nullptr};
+		cx<R>* Dg = nullptr;
+		const cx<R>* Cprev = nullptr;
+		double eps_bytes = 0, field_pts = 0;
+	};
+
+	// nref of every group, then the shift parameters (device side).
+	void rec_prologue(SampleHost& h) {
+		const uint8_t* mk_ = h.has_mask ? h.dmask.as<uint8_t>() : nullptr;
+		int nb = (int)std::min<size_t>(1024, (h.nvox + 255) / 256);
+		launch("neff_partial", (double)h.nvox * h.fd * 8 * h.G, [&] {
+			k_neff_partial<<<dim3(nb, h.G), 256, 0, cs>>>(h.dir.as<double>(), h.fd, mk_, h.nvox,
+				h.gpsd.as<GroupParams>(), h.partial.as<double>());
+		});
+		launch("nref_final", 8.0 * nb * h.G, [&] {
+			k_nref_final<<<(h.G + 63) / 64, 64, 0, cs>>>(h.G, nb, h.nvox, h.partial.as<double>(),
+				h.gpsd.as<GroupParams>());
+		});
+		launch("shift_params", sizeof(ShiftParams) * h.G * h.Nq, [&] {
+			k_shift_params<<<(h.G * h.Nq + 63) / 64, 64, 0, cs>>>(h.G, h.Nq, h.geom.Nx, h.geom.Ny,
+				h.gpsd.as<GroupParams>(), h.qv.as<double>(), h.shiftd.as<ShiftParams>());
+		});
+	}
+
+	// Entrance of a pass: eps plane 0 and the initial fields.
+	PassState rec_pass_begin(SampleHost& h, int ga) {
 		const Geom Gm = h.geom;
-		const int N = Gm.N, Nx = Gm.Nx, Ny = Gm.Ny, Nz = Gm.Nz;
+		const int N = Gm.N;
+		const double sc = sizeof(cx<R>);
+		const uint8_t* mk_ = h.has_mask ? h.dmask.as<uint8_t>() : nullptr;
+		PassState ps;
+		ps.ga = ga;
+		ps.ng = std::min(gpp(h), h.G - ga);
+		ps.slot0 = ga * h.spg;
+		ps.nsl = ps.ng * h.spg;
+		ps.gps = h.gpsd.as<GroupParams>() + ga;
+		ps.Fp = h.F.as<cx<R>>() + (size_t)ps.slot0 * 2 * N;
+		ps.Tb = T.as<cx<R>>();
+		ps.T2b = T2.as<cx<R>>();
+		ps.Qr[0] = Qring.as<double>();
+		ps.Qr[1] = ps.Qr[0] + (size_t)ps.ng * NQ * N;
+		ps.Cring[0] = coef.as<cx<R>>();
+		ps.Cring[1] = coef.as<cx<R>>() + (size_t)ps.ng * NCOEF * N;
+		ps.Dg = diag.as<cx<R>>();
+		ps.eps_bytes = (double)N * ps.ng * (h.fd * 8 + (mk_ ? 1 : 0) + NQ * 8);
+		ps.field_pts = (double)N * ps.nsl;
+		const int ng = ps.ng, nsl = ps.nsl, slot0 = ps.slot0;
+		const GroupParams* gps = ps.gps;
+		launch("eps_plane", ps.eps_bytes, [&] {
+			k_eps_plane<<<pgrid(N, ng), 256, 0, cs>>>(h.dir.as<double>(), h.fd, mk_, N, 0, gps, ps.Qr[0]);
+		});
+		if(h.s.beam_type != 2) {
+			launch("init_fields", ps.field_pts * 2 * sc + (double)N * ng * 3 * 8, [&] {
+				k_init_fields<R><<<pgrid(N, nsl), 256, 0, cs>>>(Gm, slot0, gps, ps.Qr[0], h.s.beam_type,
+					h.s.waist, h.s.dx, h.s.dy, ps.Fp);
+			});
+		}
+		else {
+			size_t n = (size_t)nsl * 2 * N;
+			launch("copy_fields", 2.0 * n * sc, [&] {
+				k_copy<R><<<(unsigned)((n + 255) / 256), 256, 0, cs>>>(n, h.E0.as<cx<R>>() + (size_t)slot0 * 2 * N, ps.Fp);
+			});
+		}
+		return ps;
+	}
+
+	// Slabs [ps.iz, iz_end) of a pass. Setup of slab iz (eps plane iz+1, coefficients,
+	// factorisations) runs on streamB and overlaps the right-hand-side work of slab iz-1 on
+	// the main stream; both streams are joined again before returning.
+	void rec_pass_slabs(SampleHost& h, PassState& ps, int iz_end) {
+		const Geom Gm = h.geom;
+		const int N = Gm.N, Nx = Gm.Nx, Ny = Gm.Ny;
 		const int Nw = h.s.n_woodbury;
 		const double sc = sizeof(cx<R>);
-		cx<R>* F = h.F.as<cx<R>>();
 		const uint8_t* mk_ = h.has_mask ? h.dmask.as<uint8_t>() : nullptr;
 		const double* wts = h.has_wts ? h.dwts.as<double>() : nullptr;
-		// nref for every group, then shift parameters (device side)
-		{
-			int nb = (int)std::min<size_t>(1024, (h.nvox + 255) / 256);
-			launch("neff_partial", (double)h.nvox * h.fd * 8 * h.G, [&] {
-				k_neff_partial<<<dim3(nb, h.G), 256, 0, cs>>>(h.dir.as<double>(), h.fd, mk_, h.nvox,
-					h.gpsd.as<GroupParams>(), h.partial.as<double>());
+		const int ng = ps.ng, nsl = ps.nsl, slot0 = ps.slot0;
+		const GroupParams* gps = ps.gps;
+		if(ps.iz >= iz_end) return;
+		CK(cudaEventRecord(eFork, stream));
+		CK(cudaStreamWaitEvent(streamB, eFork, 0));
+		for(int iz = ps.iz; iz < iz_end; iz++) {
+			double* QA = ps.Qr[iz & 1];
+			double* QB = ps.Qr[(iz + 1) & 1];
+			cx<R>* C = ps.Cring[iz & 1];
+			const SolveCfg& scf = scfg[h.index];
+			cx<R>* fx = facx.as<cx<R>>() + (size_t)(iz & 1) * facx_half;
+			cx<R>* fy = facy.as<cx<R>>() + (size_t)(iz & 1) * facy_half;
+			cx<double>* lx = lscx.as<cx<double>>() + (size_t)(iz & 1) * lsc_half;
+			cx<double>* ly = lscy.as<cx<double>>() + (size_t)(iz & 1) * lsc_half;
+			// ---- setup stream ----
+			cs = streamB;
+			launch("eps_plane", ps.eps_bytes, [&] {
+				k_eps_plane<<<pgrid(N, ng), 256, 0, cs>>>(h.dir.as<double>(), h.fd, mk_, N, iz + 1, gps, QB);
 			});
-			launch("nref_final", 8.0 * nb * h.G, [&] {
-				k_nref_final<<<(h.G + 63) / 64, 64, 0, cs>>>(h.G, nb, h.nvox, h.partial.as<double>(),
-					h.gpsd.as<GroupParams>());
+			// coef(iz) overwrites the set the transition of slab iz-1 read (slab iz-2)
+			if(iz >= 1) CK(cudaStreamWaitEvent(streamB, eTrans, 0));
+			launch("coef", (double)N * ng * (2 * NQ * 8 + NCOEF * sc + NDIAG * sc + (wts ? 16 : 0)), [&] {
+				k_coef<R><<<pgrid(N, ng, 128), 128, 0, cs>>>(QA, QB, wts, iz, Gm, gps, C, ps.Dg);
 			});
-			launch("shift_params", sizeof(ShiftParams) * h.G * h.Nq, [&] {
-				k_shift_params<<<(h.G * h.Nq + 63) / 64, 64, 0, cs>>>(h.G, h.Nq, Nx, Ny, h.gpsd.as<GroupParams>(),
-					h.qv.as<double>(), h.shiftd.as<ShiftParams>());
+			CK(cudaEventRecord(eCoef, streamB));
+			// factor(iz) overwrites the half the line solves of slab iz-2 used
+			if(iz >= 2) CK(cudaStreamWaitEvent(streamB, eAdi[iz & 1], 0));
+			int lx_n = ng * 2 * Ny, ly_n = ng * 2 * Nx;
+			const double fb = (double)N * ng * 2 * (3 * sc + NFAC * sc + 4 * sc);
+			launch("factor", 2 * fb, [&] {
+				k_factor<R><<<(lx_n + ly_n + 63) / 64, 64, 0, cs>>>(Gm, ng, scf.Mx, ps.Dg, fx, scf.plane_x, lx, fy,
+					scf.plane_y, ly, scr.as<cx<R>>());
 			});
-		}
-		int ngp = gpp(h);
-		for(int ga = 0; ga < h.G; ga += ngp) {
-			int ng = std::min(ngp, h.G - ga);
-			int slot0 = ga * h.spg, nsl = ng * h.spg;
-			const GroupParams* gps = h.gpsd.as<GroupParams>() + ga;
-			cx<R>* Fp = F + (size_t)slot0 * 2 * N;
-			cx<R>* Tb = T.as<cx<R>>();
-			cx<R>* T2b = T2.as<cx<R>>();
-			double* Q0 = Qring.as<double>();
-			double* Q1 = Q0 + (size_t)ng * NQ * N;
-			double* Qr[2] = {Q0, Q1};
-			cx<R>* Cring[2] = {coef.as<cx<R>>(), coef.as<cx<R>>() + (size_t)ng * NCOEF * N};
-			cx<R>* Dg = diag.as<cx<R>>();
-			const double eps_bytes = (double)N * ng * (h.fd * 8 + (mk_ ? 1 : 0) + NQ * 8);
-			const double field_pts = (double)N * nsl;
-
-			launch("eps_plane", eps_bytes, [&] {
-				k_eps_plane<<<pgrid(N, ng), 256, 0, cs>>>(h.dir.as<double>(), h.fd, mk_, N, 0, gps, Qr[0]);
-			});
-			if(h.s.beam_type != 2) {
-				launch("init_fields", field_pts * 2 * sc + (double)N * ng * 3 * 8, [&] {
-					k_init_fields<R><<<pgrid(N, nsl), 256, 0, cs>>>(Gm, slot0, gps, Qr[0], h.s.beam_type,
-						h.s.waist, h.s.dx, h.s.dy, Fp);
-				});
-			}
-			else {
-				size_t n = (size_t)nsl * 2 * N;
-				launch("copy_fields", 2.0 * n * sc, [&] {
-					k_copy<R><<<(unsigned)((n + 255) / 256), 256, 0, cs>>>(n, h.E0.as<cx<R>>() + (size_t)slot0 * 2 * N, Fp);
-				});
-			}
-			const cx<R>* Cprev = nullptr;
-			// Setup of slab iz (eps plane iz+1, coefficients, factorisations) runs on streamB and
-			// overlaps the right-hand-side work of slab iz-1 on the main stream.
-			CK(cudaEventRecord(eFork, stream));
-			CK(cudaStreamWaitEvent(streamB, eFork, 0));
-			for(int iz = 0; iz < Nz - 1; iz++) {
-				double* QA = Qr[iz & 1];
-				double* QB = Qr[(iz + 1) & 1];
-				cx<R>* C = Cring[iz & 1];
-				const SolveCfg& scf = scfg[h.index];
-				cx<R>* fx = facx.as<cx<R>>() + (size_t)(iz & 1) * facx_half;
-				cx<R>* fy = facy.as<cx<R>>() + (size_t)(iz & 1) * facy_half;
-				cx<double>* lx = lscx.as<cx<double>>() + (size_t)(iz & 1) * lsc_half;
-				cx<double>* ly = lscy.as<cx<double>>() + (size_t)(iz & 1) * lsc_half;
-				// ---- setup stream ----
-				cs = streamB;
-				launch("eps_plane", eps_bytes, [&] {
-					k_eps_plane<<<pgrid(N, ng), 256, 0, cs>>>(h.dir.as<double>(), h.fd, mk_, N, iz + 1, gps, QB);
-				});
-				// coef(iz) overwrites the set the transition of slab iz-1 read (slab iz-2)
-				if(iz >= 1) CK(cudaStreamWaitEvent(streamB, eTrans, 0));
-				launch("coef", (double)N * ng * (2 * NQ * 8 + NCOEF * sc + NDIAG * sc + (wts ? 16 : 0)), [&] {
-					k_coef<R><<<pgrid(N, ng, 128), 128, 0, cs>>>(QA, QB, wts, iz, Gm, gps, C, Dg);
-				});
-				CK(cudaEventRecord(eCoef, streamB));
-				// factor(iz) overwrites the half the line solves of slab iz-2 used
-				if(iz >= 2) CK(cudaStreamWaitEvent(streamB, eAdi[iz & 1], 0));
-				int lx_n = ng * 2 * Ny, ly_n = ng * 2 * Nx;
-				const double fb = (double)N * ng * 2 * (3 * sc + NFAC * sc + 4 * sc);
-				launch("factor", 2 * fb, [&] {
-					k_factor<R><<<(lx_n + ly_n + 63) / 64, 64, 0, cs>>>(Gm, ng, scf.Mx, Dg, fx, scf.plane_x, lx, fy,
-						scf.plane_y, ly, scr.as<cx<R>>());
-				});
-				CK(cudaEventRecord(eFac, streamB));
-				// ---- main stream ----
-				cs = stream;
-				CK(cudaStreamWaitEvent(stream, eCoef, 0));
-				// [phase(iz-1)] shift(iz-1) | shift(iz) phase(iz)   (BPMIteration.cpp:133-146)
-				rec_transition(h, slot0, nsl, Cprev, C, Fp, Tb, T2b, iz > 0);
-				CK(cudaEventRecord(eTrans, stream));
-				CK(cudaStreamWaitEvent(stream, eFac, 0));
-				fx_cur = fx; fy_cur = fy; lx_cur = lx; ly_cur = ly;
-				rec_adi(h, Gm, slot0, nsl, ng, Nw, C, Fp, Tb, T2b);
-				CK(cudaEventRecord(eAdi[iz & 1], stream));
-				Cprev = C;
-			}
-			CK(cudaEventRecord(eJoin, streamB));
-			CK(cudaStreamWaitEvent(stream, eJoin, 0));
+			CK(cudaEventRecord(eFac, streamB));
+			// ---- main stream ----
 			cs = stream;
-			if(Nz > 1) rec_transition(h, slot0, nsl, Cprev, nullptr, Fp, Tb, T2b, false);
-			launch("fresnel_out", field_pts * 4 * sc + (double)N * ng * 3 * 8, [&] {
-				k_fresnel_out<R><<<pgrid(N, nsl), 256, 0, cs>>>(Gm, slot0, gps, Qr[(Nz - 1) & 1], Fp);
-			});
+			CK(cudaStreamWaitEvent(stream, eCoef, 0));
+			// [phase(iz-1)] shift(iz-1) | shift(iz) phase(iz)   (BPMIteration.cpp:133-146)
+			rec_transition(h, slot0, nsl, ps.Cprev, C, ps.Fp, ps.Tb, ps.T2b, iz > 0);
+			CK(cudaEventRecord(eTrans, stream));
+			CK(cudaStreamWaitEvent(stream, eFac, 0));
+			fx_cur = fx; fy_cur = fy; lx_cur = lx; ly_cur = ly;
+			rec_adi(h, Gm, slot0, nsl, ng, Nw, C, ps.Fp, ps.Tb, ps.T2b);
+			CK(cudaEventRecord(eAdi[iz & 1], stream));
+			ps.Cprev = C;
 		}
-		// Screen filter over every plane of the sample (ScreenOutput.cpp:184-224).
+		ps.iz = iz_end;
+		CK(cudaEventRecord(eJoin, streamB));
+		CK(cudaStreamWaitEvent(stream, eJoin, 0));
+		cs = stream;
+	}
+
+	// Exit of a pass: the last slab's trailing phase and shift, then the Fresnel exit operator.
+	void rec_pass_end(SampleHost& h, PassState& ps) {
+		const Geom Gm = h.geom;
+		const int N = Gm.N, Nz = Gm.Nz;
+		const double sc = sizeof(cx<R>);
+		cs = stream;
+		if(Nz > 1) rec_transition(h, ps.slot0, ps.nsl, ps.Cprev, nullptr, ps.Fp, ps.Tb, ps.T2b, false);
+		const GroupParams* gps = ps.gps;
+		double* Qlast = ps.Qr[(Nz - 1) & 1];
+		const int nsl = ps.nsl, slot0 = ps.slot0;
+		launch("fresnel_out", ps.field_pts * 4 * sc + (double)N * ps.ng * 3 * 8, [&] {
+			k_fresnel_out<R><<<pgrid(N, nsl), 256, 0, cs>>>(Gm, slot0, gps, Qlast, ps.Fp);
+		});
+	}
+
+	// Screen filter over every plane of the sample (ScreenOutput.cpp:184-224).
+	void rec_screen(SampleHost& h) {
+		const int N = h.geom.N;
+		const double sc = sizeof(cx<R>);
+		cx<R>* F = h.F.as<cx<R>>();
 		int nplanes = h.slots * 2;
 		fft2(h, F, nplanes, -1);
 		launch("screen_filter", (double)N * h.slots * 4 * sc, [&] {
@@ -627,6 +684,16 @@ struct Plan : PlanBase {
 				h.nout.as<double>(), h.qv.as<double>());
 		});
 		fft2(h, F, nplanes, +1);
+	}
+
+	void record_sample(SampleHost& h) {
+		rec_prologue(h);
+		for(int ga = 0; ga < h.G; ga += gpp(h)) {
+			PassState ps = rec_pass_begin(h, ga);
+			rec_pass_slabs(h, ps, h.geom.Nz - 1);
+			rec_pass_end(h, ps);
+		}
+		rec_screen(h);
 	}
 
 	// Between the Strang half-steps of consecutive slabs: phase(CA) -> shift -> [shift] ->
@@ -861,6 +928,70 @@ struct Plan : PlanBase {
 
 	long long device_bytes() const override { return dev_bytes; }
 	double slab_ms() const override { return last_slab_ms; }
+	long long voxel_steps() const override {
+		long long vs = 0;
+		for(auto& hp : S) vs += (long long)hp->geom.N * (hp->geom.Nz - 1) * hp->slots;
+		return vs;
+	}
+
+	PassState sps;
+	cudaEvent_t eDone = nullptr;
+	void step_begin() override {
+		if(S.size() != 1 || gpp(*S[0]) != S[0]->G) throw BackendError(E_ARG, "stepped plans hold one sample in one pass");
+		CK(cudaSetDevice(opt.device));
+		if(!eDone) CK(cudaEventCreateWithFlags(&eDone, cudaEventDisableTiming));
+		cs = stream;
+		rec_prologue(*S[0]);
+		sps = rec_pass_begin(*S[0], 0);
+	}
+	int step_advance(int nslabs) override {
+		CK(cudaSetDevice(opt.device));
+		SampleHost& h = *S[0];
+		int end = std::min(h.geom.Nz - 1, sps.iz + std::max(0, nslabs));
+		rec_pass_slabs(h, sps, end);
+		return h.geom.Nz - 1 - sps.iz;
+	}
+	void step_finish() override {
+		CK(cudaSetDevice(opt.device));
+		SampleHost& h = *S[0];
+		rec_pass_end(h, sps);
+		rec_screen(h);
+		size_t n = (size_t)h.slots * 2 * h.geom.N;
+		if(sizeof(R) == sizeof(double)) {
+			CK(cudaMemcpyAsync(h.E, h.F.p, n * sizeof(cx<double>), cudaMemcpyDeviceToHost, stream));
+		}
+		else {
+			k_widen<R><<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, h.F.as<cx<R>>(), stage.as<cx<double>>());
+			CK(cudaGetLastError());
+			CK(cudaMemcpyAsync(h.E, stage.p, n * sizeof(cx<double>), cudaMemcpyDeviceToHost, stream));
+		}
+		CK(cudaEventRecord(eDone, stream));
+	}
+	void sync() override {
+		CK(cudaStreamSynchronize(stream));
+		CK(cudaStreamSynchronize(streamB));
+	}
+	bool step_done() override {
+		cudaError_t e = cudaEventQuery(eDone);
+		if(e == cudaErrorNotReady) return false;
+		CK(e);
+		return true;
+	}
+
+	bool fields_view(int sample, PlanFieldsView& v) const override {
+		if(sample < 0 || sample >= (int)S.size()) return false;
+		const SampleHost& h = *S[sample];
+		v.ptr = h.F.p;
+		v.n = (size_t)h.slots * 2 * h.geom.N;
+		v.fp32 = sizeof(R) == sizeof(float);
+		v.Nx = h.s.Nx;
+		v.Ny = h.s.Ny;
+		v.Nl = (int)h.s.wavelengths.size();
+		v.Nq = (int)h.s.q.size();
+		v.device = opt.device;
+		v.stream = stream;
+		return true;
+	}
 };
 
 }  // namespace nbpm
@@ -870,6 +1001,25 @@ using namespace nbpm;
 struct nbpm_plan {
 	std::unique_ptr<PlanBase> impl;
 };
+
+std::unique_ptr<PlanBase> nbpm::make_plan_host(int n_samples, const nbpm_sample* samples, const nbpm_options& o) {
+	if(n_samples <= 0 || !samples) throw BackendError(E_ARG, "invalid plan arguments");
+	if(o.precision == NBPM_FP64) {
+		std::unique_ptr<Plan<double>> p(new Plan<double>(o));
+		p->setup_host(n_samples, samples);
+		return std::unique_ptr<PlanBase>(p.release());
+	}
+	if(o.precision == NBPM_FP32) {
+		std::unique_ptr<Plan<float>> p(new Plan<float>(o));
+		p->setup_host(n_samples, samples);
+		return std::unique_ptr<PlanBase>(p.release());
+	}
+	throw BackendError(E_ARG, "unknown precision");
+}
+
+bool nbpm::plan_fields_view(nbpm_plan* p, int sample, PlanFieldsView& v) {
+	return p && p->impl && p->impl->fields_view(sample, v);
+}
 
 static int fail(int code, const std::string& msg) {
 	g_last_error = msg;
