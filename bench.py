@@ -378,19 +378,84 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def run_serve(args):
+    """Serving mix: a seeded Poisson trace replayed in real time against the FP32 server, then the
+    same trace through a plain FP64 one-request-at-a-time loop (requests served in arrival order,
+    one wavelength per launch; each request's queueing is simulated from the measured service
+    times). Reports throughput and p50/p99 latency of both, and the server's per-request relative
+    L2 error against the FP64 results."""
+    from nemaktis_gb300 import api, workloads
+    from nemaktis_gb300.serving import Server
+    trace = workloads.serving_trace(args.serve_requests, rate=50.0, seed=0)
+    total_vs = sum(t["voxel_steps"] for t in trace)
+    # warm-up: context, modules, allocator
+    wu = workloads.serving_trace(1, seed=99)[0]
+    with Server(precision="fp32") as srv:
+        E = np.zeros(wu["shape"], np.complex128)
+        srv.submit(wu["json"], wu["lc"], E, wu["mask"], wu["formula"]).wait()
+        out32 = [np.zeros(t["shape"], np.complex128) for t in trace]
+        clk = Clocks()
+        clk.start()
+        t0 = time.perf_counter()
+        hs = []
+        for t, E in zip(trace, out32):
+            dt = t0 + t["arrival"] - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            hs.append(srv.submit(t["json"], t["lc"], E, t["mask"], t["formula"]))
+        infos = [h.wait() for h in hs]
+        t_end = time.perf_counter()
+        clocks = clk.stop()
+        st = srv.stats()
+    lat32 = np.array([i["latency_ms"] for i in infos])
+    wall32 = t_end - t0
+    # FP64 plain, one request at a time, same trace
+    clock = 0.0
+    lat64, errs = [], []
+    t64_busy = 0.0
+    for t, E32 in zip(trace, out32):
+        E = np.zeros(t["shape"], np.complex128)
+        s = time.perf_counter()
+        api.run(t["json"], t["lc"], E, mask=t["mask"], formula=t["formula"], precision="fp64", groups_per_pass=1)
+        svc = time.perf_counter() - s
+        t64_busy += svc
+        clock = max(clock, t["arrival"]) + svc
+        lat64.append(1e3 * (clock - t["arrival"]))
+        errs.append(float(np.linalg.norm(E32 - E) / np.linalg.norm(E)))
+    lat64 = np.array(lat64)
+    line = {
+        "metric": "serving: voxel-steps/s and p50/p99 end-to-end latency, FP32 continuous batching vs FP64 one at a time",
+        "value": total_vs / wall32, "unit": "voxel-steps/s", "n_gpus": 1, "steps": 1, "warmup": 1,
+        "higher_is_better": True, "dtype": "complex-f32", "data": "synthetic (seeded trace and director fields)",
+        "config": {"workload": "serving mix: %d requests, Poisson 50 req/s, meshes 64^2x32..512^2x128, 1-32 "
+                               "wavelengths, 1-19 q, d=0.25um, budget 150 GB" % len(trace),
+                   "requests": [{k: t[k] for k in ("arrival", "kind", "dims", "n_wavelengths", "n_q", "voxel_steps")}
+                                for t in trace]},
+        "server": {"wall_s": wall32, "p50_ms": float(np.percentile(lat32, 50)), "p99_ms": float(np.percentile(lat32, 99)),
+                   "mean_queue_ms": float(np.mean([i["queue_ms"] for i in infos])), "peak_device_gb": st["peak_bytes"] / 1e9,
+                   "rounds": st["rounds"], "done": st["done"], "failed": st["failed"]},
+        "fp64_one_at_a_time": {"value": total_vs / clock, "busy_s": t64_busy, "makespan_s": clock,
+                               "p50_ms": float(np.percentile(lat64, 50)), "p99_ms": float(np.percentile(lat64, 99))},
+        "max_rel_l2_fp32_vs_fp64": max(errs),
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="config3", choices=["config1", "config2", "config3", "config3s", "config4"])
+    ap.add_argument("--workload", default="config3", choices=["config1", "config2", "config3", "config3s", "config4", "serve"])
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--only-value", action="store_true", help="time the device-resident run only")
+    ap.add_argument("--serve-requests", type=int, default=12, help="requests in the serving trace")
     args = ap.parse_args()
     world, rank, local = dist_env()
     if world > 1:
@@ -400,6 +465,8 @@ def main():
         dist.init_process_group("nccl")
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "serve":
+        run_serve(args)
     else:
         run_ours(args)
     if world > 1:

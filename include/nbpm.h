@@ -150,7 +150,7 @@ int nbpm_periodic_tridiag_solve_noalloc(int L, int nlines, const double* inf, co
  * A thread-safe submit / poll interface over the same plans (no counterpart in the reference,
  * whose backend runs one blocking call per sample, bpm_backend.cpp:7-164). A server thread
  * admits queued requests first-come first-served while their estimated device memory fits
- * the budget, advances every request in flight by slabs_per_round slabs per scheduling round
+ * the budget, advances every request in flight by a few slabs per scheduling round
  * (each on its own CUDA streams, so requests of different meshes run side by side and new
  * ones join at slab boundaries), and copies each finished request's screen fields into its
  * E_field_vals buffer. A request runs the same launch sequence as a standalone run with the
@@ -161,8 +161,12 @@ typedef struct nbpm_server_options {
 	int precision;          /* NBPM_FP32 (default) or NBPM_FP64 */
 	int device;
 	double hbm_budget_gb;   /* admission budget for the requests in flight (default 150) */
-	int slabs_per_round;    /* slabs each request in flight advances per round (default 8) */
+	int slabs_per_round;    /* slabs each request in flight advances per round when
+	                           round_voxel_steps is 0 (default 8) */
 	int max_active;         /* requests in flight at most; 0: limited by the budget only */
+	double round_voxel_steps; /* > 0 (default 4e8): each request advances as many slabs per
+	                           round as fit this many voxel-steps (at least one), so small
+	                           requests finish in few rounds next to large ones */
 } nbpm_server_options;
 
 enum { NBPM_REQ_QUEUED = 0, NBPM_REQ_RUNNING = 1, NBPM_REQ_DONE = 2, NBPM_REQ_FAILED = 3, NBPM_REQ_CANCELLED = 4 };

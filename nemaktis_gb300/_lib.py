@@ -53,7 +53,7 @@ class ViewerSettings(ctypes.Structure):
 
 class ServerOptions(ctypes.Structure):
     _fields_ = [("precision", c_int), ("device", c_int), ("hbm_budget_gb", c_double), ("slabs_per_round", c_int),
-                ("max_active", c_int)]
+                ("max_active", c_int), ("round_voxel_steps", c_double)]
 
 
 class RequestInfo(ctypes.Structure):

@@ -93,9 +93,11 @@ __device__ __forceinline__ double neff_of(double xxtr, double yytr, double xytr)
 	return (sqrt(tr + r) + sqrt(tr - r)) / 2.;
 }
 
-// One transverse plane of derived quantities for every group of the pass.
+// One transverse plane of derived quantities for every group of the pass, computed in FP64
+// and stored in the plan's precision Q.
+template <typename Q>
 static __global__ void k_eps_plane(const double* __restrict__ dir, int fd, const uint8_t* __restrict__ mask,
-		int N, int iz, const GroupParams* __restrict__ gps, double* __restrict__ out) {
+		int N, int iz, const GroupParams* __restrict__ gps, Q* __restrict__ out) {
 	int p = blockIdx.x * blockDim.x + threadIdx.x;
 	int g = blockIdx.y;
 	if(p >= N) return;
@@ -107,16 +109,16 @@ static __global__ void k_eps_plane(const double* __restrict__ dir, int fd, const
 	double yytr = e[1] - (e[5] * e[5]) / e[2];
 	double xytr = e[3] - e[4] * e[5] / e[2];
 	double neff = neff_of(xxtr, yytr, xytr);
-	double* o = out + (size_t)g * NQ * N + p;
-	o[Q_XXTR * N] = xxtr;
-	o[Q_YYTR * N] = yytr;
-	o[Q_XYTR * N] = xytr;
-	o[Q_XXS * N] = neff + (xxtr - yytr) / (4 * neff);
-	o[Q_YYS * N] = neff + (yytr - xxtr) / (4 * neff);
-	o[Q_XYS * N] = xytr / (2 * neff);
-	o[Q_VX * N] = e[4] / e[2];
-	o[Q_VY * N] = e[5] / e[2];
-	o[Q_IZZ * N] = 1. / e[2];
+	Q* o = out + (size_t)g * NQ * N + p;
+	o[Q_XXTR * N] = (Q)xxtr;
+	o[Q_YYTR * N] = (Q)yytr;
+	o[Q_XYTR * N] = (Q)xytr;
+	o[Q_XXS * N] = (Q)(neff + (xxtr - yytr) / (4 * neff));
+	o[Q_YYS * N] = (Q)(neff + (yytr - xxtr) / (4 * neff));
+	o[Q_XYS * N] = (Q)(xytr / (2 * neff));
+	o[Q_VX * N] = (Q)(e[4] / e[2]);
+	o[Q_VY * N] = (Q)(e[5] / e[2]);
+	o[Q_IZZ * N] = (Q)(1. / e[2]);
 }
 
 // Partial sums of neff over the volume for nref (PermittivityTensorField.cpp:183-211),
@@ -156,17 +158,17 @@ static __global__ void k_neff_partial(const double* __restrict__ dir, int fd, co
 // ---------------------------------------------------------------------------------------
 template <typename T>
 struct CoefCtx {
-	const double* A;
-	const double* B;
+	const T* A;
+	const T* B;
 	int N, Nx;
 	T hmu, rxx, ryy, rxy, va0, va1;
 	__device__ __forceinline__ T avg(int q, int x, int y) const {
 		int i = x + Nx * y;
-		return (T)((A[q * N + i] + B[q * N + i]) / 2);
+		return (A[q * N + i] + B[q * N + i]) / (T)2;
 	}
 	__device__ __forceinline__ T vsum(int a, int x, int y) const {
 		int i = x + Nx * y, q = a == 0 ? Q_VX : Q_VY;
-		return (T)(A[q * N + i] + B[q * N + i]);
+		return A[q * N + i] + B[q * N + i];
 	}
 	__device__ __forceinline__ void sinv(int x, int y, T& ixx, T& iyy, T& ixy) const {
 		T exx = avg(Q_XXS, x, y), eyy = avg(Q_YYS, x, y), exy = avg(Q_XYS, x, y);
@@ -206,41 +208,69 @@ struct CoefCtx {
 	}
 };
 
+// Phase operator of one point (PhaseEvolutionOperator.cpp:14-32) from eps planes A, B of the
+// slab's two ends, in the arithmetic type T.
+template <typename T>
+__device__ __forceinline__ void phase_op(const T* A, const T* B, int N, int p, T w0, T w1, const GroupParams& gp,
+		cx<T>& oxx, cx<T>& oyy, cx<T>& oxy) {
+	T hz = (T)(0.5 * gp.dZ);
+	T dxx = hz * (w0 * A[Q_XXS * N + p] + w1 * B[Q_XXS * N + p] - (T)gp.no);
+	T dyy = hz * (w0 * A[Q_YYS * N + p] + w1 * B[Q_YYS * N + p] - (T)gp.no);
+	T dxy = hz * (w0 * A[Q_XYS * N + p] + w1 * B[Q_XYS * N + p]);
+	T diff = (dxx - dyy) / (T)2, tr = (dxx + dyy) / (T)2;
+	T det = sqrt(dxy * dxy + diff * diff);
+	cx<T> a = mk<T>((T)1, (T)gp.absorp_im);
+	cx<T> sinc = mk<T>((T)1, (T)0);
+	cx<T> e, c;
+	if(sizeof(T) == sizeof(double)) {
+		cx<double> ad = cvt<double>(a);
+		if(!(fabs((double)det) < 1e-8)) {
+			cx<double> sn = csin_d((double)det * ad);
+			sinc = cvt<T>(mk(sn.x / (double)det, sn.y / (double)det));
+		}
+		e = cvt<T>(cexp_d(mk(-ad.y * (double)tr, ad.x * (double)tr)));  // exp(i*a*tr)
+		c = cvt<T>(ccos_d((double)det * ad));
+	}
+	else {
+		cx<float> af = cvt<float>(a);
+		if(!(fabsf((float)det) < 1e-8f)) {
+			cx<float> sn = csin_f((float)det * af);
+			sinc = cvt<T>(mk(sn.x / (float)det, sn.y / (float)det));
+		}
+		e = cvt<T>(cexp_f(mk(-af.y * (float)tr, af.x * (float)tr)));
+		c = cvt<T>(ccos_f((float)det * af));
+	}
+	cx<T> ids = mk<T>((T)0, diff) * sinc;
+	oxx = e * (c + ids);
+	oyy = e * (c - ids);
+	oxy = ((e * mk<T>((T)0, (T)1)) * dxy) * sinc;
+}
+
 template <typename S>
-__global__ void k_coef(const double* __restrict__ QA, const double* __restrict__ QB,
+__global__ void k_coef(const S* __restrict__ QA, const S* __restrict__ QB,
 		const double* __restrict__ wts, int iz, Geom G, const GroupParams* __restrict__ gps,
 		cx<S>* __restrict__ coef, cx<S>* __restrict__ diag) {
-	typedef S T;  // arithmetic type of the R coefficients (the phase operator is always FP64)
+	typedef S T;  // arithmetic type of the eps planes, the phase operator and the R coefficients
 	int p = blockIdx.x * blockDim.x + threadIdx.x;
 	int g = blockIdx.y;
 	int N = G.N, Nx = G.Nx, Ny = G.Ny;
 	if(p >= N) return;
 	int ix = p % Nx, iy = p / Nx;
 	const GroupParams gp = gps[g];
-	const double* A = QA + (size_t)g * NQ * N;
-	const double* B = QB + (size_t)g * NQ * N;
+	const T* A = QA + (size_t)g * NQ * N;
+	const T* B = QB + (size_t)g * NQ * N;
 	cx<S>* C = coef + (size_t)g * NCOEF * N + p;
 	cx<S>* Dg = diag + (size_t)g * NDIAG * N + p;
 
 	// Phase operator.
 	{
-		double w0 = 0.5, w1 = 0.5;
-		if(wts) { size_t vi = (size_t)iz * N + p; w0 = wts[2 * vi]; w1 = wts[2 * vi + 1]; }
-		double hz = 0.5 * gp.dZ;
-		double dxx = hz * (w0 * A[Q_XXS * N + p] + w1 * B[Q_XXS * N + p] - gp.no);
-		double dyy = hz * (w0 * A[Q_YYS * N + p] + w1 * B[Q_YYS * N + p] - gp.no);
-		double dxy = hz * (w0 * A[Q_XYS * N + p] + w1 * B[Q_XYS * N + p]);
-		double diff = (dxx - dyy) / 2., tr = (dxx + dyy) / 2.;
-		double det = sqrt(dxy * dxy + diff * diff);
-		cx<double> a = mk(1.0, gp.absorp_im);
-		cx<double> sinc = mk(1.0, 0.0);
-		if(!(fabs(det) < 1e-8)) { cx<double> sn = csin_d(det * a); sinc = mk(sn.x / det, sn.y / det); }
-		cx<double> e = cexp_d(mk(-a.y * tr, a.x * tr));  // exp(i*a*tr)
-		cx<double> c = ccos_d(det * a);
-		cx<double> ids = mk(0.0, diff) * sinc;
-		C[(size_t)(C_PH + 0) * N] = cvt<S>(e * (c + ids));
-		C[(size_t)(C_PH + 1) * N] = cvt<S>(e * (c - ids));
-		C[(size_t)(C_PH + 2) * N] = cvt<S>(((e * mk(0.0, 1.0)) * dxy) * sinc);
+		T w0 = (T)0.5, w1 = (T)0.5;
+		if(wts) { size_t vi = (size_t)iz * N + p; w0 = (T)wts[2 * vi]; w1 = (T)wts[2 * vi + 1]; }
+		cx<T> oxx, oyy, oxy;
+		phase_op<T>(A, B, N, p, w0, w1, gp, oxx, oyy, oxy);
+		C[(size_t)(C_PH + 0) * N] = oxx;
+		C[(size_t)(C_PH + 1) * N] = oyy;
+		C[(size_t)(C_PH + 2) * N] = oxy;
 	}
 
 	CoefCtx<T> X;
@@ -250,7 +280,7 @@ __global__ void k_coef(const double* __restrict__ QA, const double* __restrict__
 	X.va0 = X.vsum(0, ix, iy);
 	X.va1 = X.vsum(1, ix, iy);
 	const T dX = (T)gp.dX, dY = (T)gp.dY;
-	auto ezz = [&](int x, int y) { int i = x + Nx * y; return (T)((A[Q_IZZ * N + i] + B[Q_IZZ * N + i]) / 2); };
+	auto ezz = [&](int x, int y) { int i = x + Nx * y; return (A[Q_IZZ * N + i] + B[Q_IZZ * N + i]) / (T)2; };
 	T e0 = ezz(ix, iy);
 	int pxq = (ix == Nx - 1) ? 1 : ix + 1, mxq = (ix == 0) ? Nx - 2 : ix - 1;
 	int pyq = (iy == Ny - 1) ? 1 : iy + 1, myq = (iy == 0) ? Ny - 2 : iy - 1;
@@ -983,7 +1013,13 @@ __device__ __forceinline__ cx<R> shfl_xor_c(cx<R> v, int m) {
 // accesses stay coalesced; the factor planes are stored chunk-interleaved (element l*M+k at
 // k*32+l) and are also loaded once for the KS slots. Block = LT warps = LT lines.
 template <typename R, int M, int KIND, int KS>
-__global__ void __launch_bounds__(128) k_solve_xc(Geom G, int slot0, int nch, const cx<R>* __restrict__ coef,
+#ifndef NBPM_XC_MINB
+#define NBPM_XC_MINB 1
+#endif
+#ifndef NBPM_YC_MINB
+#define NBPM_YC_MINB 1
+#endif
+__global__ void __launch_bounds__(128, NBPM_XC_MINB) k_solve_xc(Geom G, int slot0, int nch, const cx<R>* __restrict__ coef,
 		const cx<R>* __restrict__ fac, size_t plane, const cx<double>* __restrict__ lsc,
 		const cx<R>* __restrict__ src, cx<R>* __restrict__ dst, const cx<R>* acc_in, cx<R>* acc_out) {
 	extern __shared__ unsigned char smem_raw[];
@@ -1124,7 +1160,7 @@ __global__ void __launch_bounds__(128) k_solve_xc(Geom G, int slot0, int nch, co
 // slots of one wavelength; warp w owns the rows [w*M, w*M+M) of the 32 lines for all KS
 // slots. Chunk maps are combined across warps through shared memory.
 template <typename R, int M, int KIND, int KS>
-__global__ void __launch_bounds__(512) k_solve_yc(Geom G, int slot0, int nch, const cx<R>* __restrict__ coef,
+__global__ void __launch_bounds__(512, NBPM_YC_MINB) k_solve_yc(Geom G, int slot0, int nch, const cx<R>* __restrict__ coef,
 		const cx<R>* __restrict__ fac, size_t plane, const cx<double>* __restrict__ lsc,
 		const cx<R>* __restrict__ src, cx<R>* __restrict__ dst, const cx<R>* acc_in, cx<R>* acc_out) {
 	extern __shared__ unsigned char smem_raw[];
@@ -1381,6 +1417,181 @@ __global__ void k_shift_y(Geom G, int slot0, const ShiftParams* __restrict__ sp,
 	F[(size_t)s * 2 * N + N + p] = v1;
 }
 
+// Whole transition between two slabs in one pass (replaces shift_x(A), shift_y, shift_x,
+// shift_y(B)): F_out = phase_B(ph^n * Y^n X^n (phase_A(F))), n = nshift (1 or 2). X and Y are
+// the circulant cubic shifts of SimpleShiftOperator (period Nx-1 / Ny-1; they act on rows and
+// columns and commute, so Y X Y X = Y Y X X). For a tile of 32 x 32 outputs of one slot the
+// block stages the input window (phase_A applied) in shared memory, runs the n x-passes and
+// the n y-passes there, and writes the tile. Indices wrap with i mod (N-1), which equals the
+// reference's wrap rule for every index above -(N-1) (the composition of two wrapped passes
+// then also reduces to one mod); a slot whose integer shift reaches -(N-2) or below takes the
+// exact per-point path instead. The duplicate row and column of F are never read, as in the
+// separate passes.
+constexpr int SHT = 32;  // tile edge
+
+__device__ __forceinline__ int pmod(int i, int n) {
+	int r = i % n;
+	return r < 0 ? r + n : r;
+}
+
+template <typename R>
+__device__ __forceinline__ void tap_in(const cx<R>* f, const cx<R>* Ca, size_t N, int q, cx<R>& a, cx<R>& b) {
+	a = f[q];
+	b = f[N + q];
+	if(Ca) phase_apply(Ca, N, q, a, b);
+}
+
+// Exact composition with the reference's wrap rule, one output point (rarely used).
+template <typename R>
+__device__ void shift_point_exact(const Geom& G, const ShiftParams& P, const cx<R>* f, const cx<R>* Ca, int nsh,
+		int ix, int iy, cx<R>& o0, cx<R>& o1) {
+	const size_t N = G.N;
+	const int Nx = G.Nx, Ny = G.Ny;
+	const bool ax = Nx > 3, ay = Ny > 3;
+	auto xrow = [&](int r, int x, cx<R>& a, cx<R>& b) {  // X^n of row r at column x
+		if(!ax) { tap_in(f, Ca, N, x + Nx * r, a, b); return; }
+		a = b = mk<R>(0, 0);
+		for(int k1 = 0; k1 < 4; k1++) {
+			int j = ref_wrap(x + P.msx - 1 + k1, Nx);
+			cx<R> u0 = mk<R>(0, 0), u1 = mk<R>(0, 0);
+			if(nsh == 2) {
+				for(int k0 = 0; k0 < 4; k0++) {
+					cx<R> t0, t1;
+					tap_in(f, Ca, N, ref_wrap(j + P.msx - 1 + k0, Nx) + Nx * r, t0, t1);
+					u0 += (R)P.wx[k0] * t0;
+					u1 += (R)P.wx[k0] * t1;
+				}
+			}
+			else tap_in(f, Ca, N, j + Nx * r, u0, u1);
+			a += (R)P.wx[k1] * u0;
+			b += (R)P.wx[k1] * u1;
+		}
+	};
+	if(!ay) { xrow(iy, ix, o0, o1); return; }
+	o0 = o1 = mk<R>(0, 0);
+	for(int l1 = 0; l1 < 4; l1++) {
+		int r1 = ref_wrap(iy + P.msy - 1 + l1, Ny);
+		cx<R> u0 = mk<R>(0, 0), u1 = mk<R>(0, 0);
+		if(nsh == 2) {
+			for(int l0 = 0; l0 < 4; l0++) {
+				cx<R> t0, t1;
+				xrow(ref_wrap(r1 + P.msy - 1 + l0, Ny), ix, t0, t1);
+				u0 += (R)P.wy[l0] * t0;
+				u1 += (R)P.wy[l0] * t1;
+			}
+		}
+		else xrow(r1, ix, u0, u1);
+		o0 += (R)P.wy[l1] * u0;
+		o1 += (R)P.wy[l1] * u1;
+	}
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_shift_fused(Geom G, int slot0, const ShiftParams* __restrict__ sp,
+		const cx<R>* __restrict__ CA, const cx<R>* __restrict__ CB, int nsh, const cx<R>* __restrict__ F,
+		cx<R>* __restrict__ Fo) {
+	extern __shared__ unsigned char smem_raw[];
+	const int PW = SHT + 6;                    // window pitch (room for two 4-tap passes)
+	cx<R>* A = reinterpret_cast<cx<R>*>(smem_raw);  // [2][PW][PW]
+	cx<R>* B = A + 2 * PW * PW;                     // [2][PW][PW]
+	const int s = blockIdx.z;
+	const int gs = slot0 + s;
+	const int g = gs / G.spg - slot0 / G.spg;
+	const int gq = (gs / G.spg) * G.Nq + (gs / 2) % G.Nq;
+	const ShiftParams P = sp[gq];
+	const size_t N = G.N;
+	const int Nx = G.Nx, Ny = G.Ny;
+	const bool ax = Nx > 3, ay = Ny > 3;
+	const int x0 = blockIdx.x * SHT, y0 = blockIdx.y * SHT;
+	const int tid = threadIdx.x;
+	const cx<R>* f = F + (size_t)s * 2 * N;
+	cx<R>* fo = Fo + (size_t)s * 2 * N;
+	const cx<R>* Ca = CA ? CA + (size_t)g * NCOEF * N : nullptr;
+	const cx<R>* Cb = CB ? CB + (size_t)g * NCOEF * N : nullptr;
+	const int Px = Nx - 1, Py = Ny - 1;
+	const int bx = ax ? nsh * (P.msx - 1) : 0, by = ay ? nsh * (P.msy - 1) : 0;
+	const int wx = ax ? SHT + 3 * nsh : SHT, wy = ay ? SHT + 3 * nsh : SHT;
+	cx<R> ph = mk<R>((R)P.ph_re, (R)P.ph_im);
+	if(nsh == 2) ph = ph * ph;
+	// every tap index of both passes stays above -(N-1): mod arithmetic equals the wrap rule
+	const bool regular = (!ax || P.msx - 1 > -Px) && (!ay || P.msy - 1 > -Py);
+	if(!regular) {
+		for(int e = tid; e < SHT * SHT; e += blockDim.x) {
+			int ix = x0 + e % SHT, iy = y0 + e / SHT;
+			if(ix >= Nx || iy >= Ny) continue;
+			cx<R> o0, o1;
+			shift_point_exact(G, P, f, Ca, nsh, ix, iy, o0, o1);
+			o0 = o0 * ph;
+			o1 = o1 * ph;
+			int p = ix + Nx * iy;
+			if(Cb) phase_apply(Cb, N, p, o0, o1);
+			fo[p] = o0;
+			fo[N + p] = o1;
+		}
+		return;
+	}
+	// 1. input window, phase_A applied
+	for(int e = tid; e < wx * wy; e += blockDim.x) {
+		int u = e % wx, v = e / wx;
+		int xi = ax ? pmod(x0 + bx + u, Px) : x0 + u;
+		int yi = ay ? pmod(y0 + by + v, Py) : y0 + v;
+		cx<R> a = mk<R>(0, 0), b = mk<R>(0, 0);
+		if(xi < Nx && yi < Ny) tap_in(f, Ca, N, xi + Nx * yi, a, b);
+		A[v * PW + u] = a;
+		A[PW * PW + v * PW + u] = b;
+	}
+	__syncthreads();
+	cx<R>* cur = A;
+	cx<R>* nxt = B;
+	int cw = wx;
+	// 2. x-passes on every window row
+	if(ax) {
+		for(int pass = 0; pass < nsh; pass++) {
+			int ow = cw - 3;
+			for(int e = tid; e < ow * wy; e += blockDim.x) {
+				int t = e % ow, v = e / ow;
+				for(int c = 0; c < 2; c++) {
+					const cx<R>* in = cur + c * PW * PW + v * PW + t;
+					nxt[c * PW * PW + v * PW + t] = (R)P.wx[0] * in[0] + (R)P.wx[1] * in[1] + (R)P.wx[2] * in[2] +
+						(R)P.wx[3] * in[3];
+				}
+			}
+			__syncthreads();
+			cx<R>* tmp = cur; cur = nxt; nxt = tmp;
+			cw = ow;
+		}
+	}
+	int ch = wy;
+	// 3. y-passes on the SHT columns of the tile
+	if(ay) {
+		for(int pass = 0; pass < nsh; pass++) {
+			int oh = ch - 3;
+			for(int e = tid; e < SHT * oh; e += blockDim.x) {
+				int t = e % SHT, v = e / SHT;
+				for(int c = 0; c < 2; c++) {
+					const cx<R>* in = cur + c * PW * PW + v * PW + t;
+					nxt[c * PW * PW + v * PW + t] = (R)P.wy[0] * in[0] + (R)P.wy[1] * in[PW] +
+						(R)P.wy[2] * in[2 * PW] + (R)P.wy[3] * in[3 * PW];
+				}
+			}
+			__syncthreads();
+			cx<R>* tmp = cur; cur = nxt; nxt = tmp;
+			ch = oh;
+		}
+	}
+	// 4. phase factor, phase_B, store
+	for(int e = tid; e < SHT * SHT; e += blockDim.x) {
+		int t = e % SHT, v = e / SHT;
+		int ix = x0 + t, iy = y0 + v;
+		if(ix >= Nx || iy >= Ny) continue;
+		cx<R> o0 = cur[v * PW + t] * ph, o1 = cur[PW * PW + v * PW + t] * ph;
+		int p = ix + Nx * iy;
+		if(Cb) phase_apply(Cb, N, p, o0, o1);
+		fo[p] = o0;
+		fo[N + p] = o1;
+	}
+}
+
 // All slots at q = 0: phase_A, then the shift operator's duplicate-border copy (column 0 ->
 // column Nx-1, then row 0 -> row Ny-1), then phase_B, in one in-place pass. The thread of a
 // source point also writes the border points copied from it, so no thread reads a value
@@ -1418,7 +1629,7 @@ __global__ void k_phase_sync(Geom G, int slot0, const cx<R>* __restrict__ CA, co
 // BeamProfile.cpp:17-39) followed by the input Fresnel operator (FresnelOperator.cpp:16-38)
 // built on sqrt(eps_tr) at iz = 0.
 template <typename R>
-__global__ void k_init_fields(Geom G, int slot0, const GroupParams* __restrict__ gps, const double* __restrict__ Q0,
+__global__ void k_init_fields(Geom G, int slot0, const GroupParams* __restrict__ gps, const R* __restrict__ Q0,
 		int beam_type, double waist, double dx, double dy, cx<R>* F) {
 	int p = blockIdx.x * blockDim.x + threadIdx.x;
 	if(p >= G.N) return;
@@ -1432,7 +1643,7 @@ __global__ void k_init_fields(Geom G, int slot0, const GroupParams* __restrict__
 	double x = ((p % Nx) - (Nx - 1) / 2.) * dx, y = ((p / Nx) - (Ny - 1) / 2.) * dy;
 	double amp = beam_type == 1 ? exp(-(x * x + y * y) / (2 * waist * waist)) : 1.0;
 	double ex = cos(th) * amp, ey = sin(th) * amp;
-	const double* Q = Q0 + (size_t)g * NQ * N;
+	const R* Q = Q0 + (size_t)g * NQ * N;
 	double nxx = Q[Q_XXS * N + p], nyy = Q[Q_YYS * N + p], nxy = Q[Q_XYS * N + p];
 	double n = gps[g].nin;
 	double det = (n + nxx) * (n + nyy) - nxy * nxy;
@@ -1444,14 +1655,14 @@ __global__ void k_init_fields(Geom G, int slot0, const GroupParams* __restrict__
 
 // Output Fresnel operator at iz = Nz-1 (FresnelOperator.cpp:45-69).
 template <typename R>
-__global__ void k_fresnel_out(Geom G, int slot0, const GroupParams* __restrict__ gps, const double* __restrict__ QL,
+__global__ void k_fresnel_out(Geom G, int slot0, const GroupParams* __restrict__ gps, const R* __restrict__ QL,
 		cx<R>* F) {
 	int p = blockIdx.x * blockDim.x + threadIdx.x;
 	if(p >= G.N) return;
 	int s = blockIdx.y;
 	int N = G.N;
 	int g = (slot0 + s) / G.spg - slot0 / G.spg;
-	const double* Q = QL + (size_t)g * NQ * N;
+	const R* Q = QL + (size_t)g * NQ * N;
 	double nxx = Q[Q_XXS * N + p], nyy = Q[Q_YYS * N + p], nxy = Q[Q_XYS * N + p];
 	double n = gps[g].nout_fresnel;
 	double det = (n + nxx) * (n + nyy) - nxy * nxy;

@@ -66,4 +66,21 @@ __host__ __device__ __forceinline__ cx<double> ccos_d(cx<double> z) {
 	return mk<double>(c * cosh(z.y), -s * sinh(z.y));
 }
 
+// FP32 counterparts (library expf, sincosf, coshf, sinhf).
+__host__ __device__ __forceinline__ cx<float> cexp_f(cx<float> z) {
+	float e = expf(z.x), s, c;
+	sincosf(z.y, &s, &c);
+	return mk<float>(e * c, e * s);
+}
+__host__ __device__ __forceinline__ cx<float> csin_f(cx<float> z) {
+	float s, c;
+	sincosf(z.x, &s, &c);
+	return mk<float>(s * coshf(z.y), c * sinhf(z.y));
+}
+__host__ __device__ __forceinline__ cx<float> ccos_f(cx<float> z) {
+	float s, c;
+	sincosf(z.x, &s, &c);
+	return mk<float>(c * coshf(z.y), -s * sinhf(z.y));
+}
+
 }  // namespace nbpm

@@ -185,6 +185,7 @@ struct Plan : PlanBase {
 	}
 	double last_slab_ms = 0;
 	size_t smem_limit = 0;
+	bool shift_fused = true;  // one-pass transition kernel (NBPM_SHIFT_FUSED=0: four passes)
 	// line-solve configuration per sample (chunk sizes of the parallel kernels; 0 = sequential)
 	// x: k_solve_xc with KSx slots per warp, or (NBPM_XMODE=1) the group-cooperative k_solve_xg
 	// (all slots of a wavelength per block) when its shared memory fits. y: ymode 0 = fused
@@ -332,6 +333,8 @@ struct Plan : PlanBase {
 		CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
 		smem_limit = (size_t)optin;
 		CK(cudaFuncSetAttribute(k_fft_lines<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit));
+		CK(cudaFuncSetAttribute(k_shift_fused<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit));
+		if(const char* e = std::getenv("NBPM_SHIFT_FUSED")) shift_fused = std::atoi(e) != 0;
 		if(sizeof(R) == sizeof(float)) {
 			set_solve_smem_x_f32((int)smem_limit); set_solve_smem_y_f32((int)smem_limit); set_solve_smem_xg_f32((int)smem_limit);
 		}
@@ -369,19 +372,24 @@ struct Plan : PlanBase {
 			}
 			if(h.s.Ny > 3) {
 				// block of 32 columns x WY <= 16 warps (<= 512 threads, <= 128 registers)
-				for(int M = 2; M <= 32; M *= 2) if((uy + M - 1) / M <= 16) { sc.My = M; break; }
+				int wmax = 16;
+				if(const char* e = std::getenv("NBPM_YWMAX")) wmax = std::min(16, std::max(1, std::atoi(e)));
+				for(int M = 2; M <= 32; M *= 2) if((uy + M - 1) / M <= wmax) { sc.My = M; break; }
 				if(sc.My) sc.WY = (uy + sc.My - 1) / sc.My;
 			}
 			// slots per thread: largest KS dividing 2*Nq with a compiled (M, KS) instance
 			// per-thread chunk values (M*KS complex) kept within 32 FP32 / 16 FP64 complex registers
 			const int cap = sizeof(R) == sizeof(float) ? 32 : 16;
-			auto pick_ks = [&](int M) {
+			int kmx = 4, kmy = 4;
+			if(const char* e = std::getenv("NBPM_KSX")) kmx = std::max(1, std::atoi(e));
+			if(const char* e = std::getenv("NBPM_KSY")) kmy = std::max(1, std::atoi(e));
+			auto pick_ks = [&](int M, int kmax) {
 				for(int ks : {4, 2, 1})
-					if(h.spg % ks == 0 && solve_pair_ok(M, ks) && (M * ks <= cap || ks == 1)) return ks;
+					if(ks <= kmax && h.spg % ks == 0 && solve_pair_ok(M, ks) && (M * ks <= cap || ks == 1)) return ks;
 				return 0;
 			};
-			if(sc.Mx) { sc.KSx = pick_ks(sc.Mx); if(!sc.KSx) sc.Mx = 0; }
-			if(sc.My) { sc.KSy = pick_ks(sc.My); if(!sc.KSy) { sc.My = 0; sc.WY = 0; } }
+			if(sc.Mx) { sc.KSx = pick_ks(sc.Mx, kmx); if(!sc.KSx) sc.Mx = 0; }
+			if(sc.My) { sc.KSy = pick_ks(sc.My, kmy); if(!sc.KSy) { sc.My = 0; sc.WY = 0; } }
 			if(opt.verbose)
 				std::printf("line solves: x M=%d KS=%d, y M=%d WY=%d KS=%d\n", sc.Mx, sc.KSx, sc.My, sc.WY, sc.KSy);
 			sc.plane_x = sc.Mx ? std::max(N, (size_t)h.s.Ny * 32 * sc.Mx) : N;
@@ -422,7 +430,7 @@ struct Plan : PlanBase {
 		bool need_t3 = false;
 		for(auto& c : scfg) need_t3 |= (c.My > 0 && c.ymode == 1);
 		if(need_t3) dalloc(T3, sizeof(cx<R>) * maxT);
-		dalloc(Qring, sizeof(double) * maxQ);
+		dalloc(Qring, sizeof(R) * maxQ);
 		dalloc(coef, sizeof(cx<R>) * maxC);
 		dalloc(diag, sizeof(cx<R>) * maxD);
 		facx_half = facy_half = maxFx;
@@ -528,7 +536,7 @@ struct Plan : PlanBase {
 		cx<R>* Fp = nullptr;
 		cx<R>* Tb = nullptr;
 		cx<R>* T2b = nullptr;
-		double* Qr[2] = {nullptr, nullptr};
+		R* Qr[2] = {nullptr, nullptr};
 		cx<R>* Cring[2] = {nullptr, nullptr};
 		cx<R>* Dg = nullptr;
 		const cx<R>* Cprev = nullptr;
@@ -568,17 +576,17 @@ struct Plan : PlanBase {
 		ps.Fp = h.F.as<cx<R>>() + (size_t)ps.slot0 * 2 * N;
 		ps.Tb = T.as<cx<R>>();
 		ps.T2b = T2.as<cx<R>>();
-		ps.Qr[0] = Qring.as<double>();
+		ps.Qr[0] = Qring.as<R>();
 		ps.Qr[1] = ps.Qr[0] + (size_t)ps.ng * NQ * N;
 		ps.Cring[0] = coef.as<cx<R>>();
 		ps.Cring[1] = coef.as<cx<R>>() + (size_t)ps.ng * NCOEF * N;
 		ps.Dg = diag.as<cx<R>>();
-		ps.eps_bytes = (double)N * ps.ng * (h.fd * 8 + (mk_ ? 1 : 0) + NQ * 8);
+		ps.eps_bytes = (double)N * ps.ng * (h.fd * 8 + (mk_ ? 1 : 0) + NQ * sizeof(R));
 		ps.field_pts = (double)N * ps.nsl;
 		const int ng = ps.ng, nsl = ps.nsl, slot0 = ps.slot0;
 		const GroupParams* gps = ps.gps;
 		launch("eps_plane", ps.eps_bytes, [&] {
-			k_eps_plane<<<pgrid(N, ng), 256, 0, cs>>>(h.dir.as<double>(), h.fd, mk_, N, 0, gps, ps.Qr[0]);
+			k_eps_plane<R><<<pgrid(N, ng), 256, 0, cs>>>(h.dir.as<double>(), h.fd, mk_, N, 0, gps, ps.Qr[0]);
 		});
 		if(h.s.beam_type != 2) {
 			launch("init_fields", ps.field_pts * 2 * sc + (double)N * ng * 3 * 8, [&] {
@@ -611,8 +619,8 @@ struct Plan : PlanBase {
 		CK(cudaEventRecord(eFork, stream));
 		CK(cudaStreamWaitEvent(streamB, eFork, 0));
 		for(int iz = ps.iz; iz < iz_end; iz++) {
-			double* QA = ps.Qr[iz & 1];
-			double* QB = ps.Qr[(iz + 1) & 1];
+			R* QA = ps.Qr[iz & 1];
+			R* QB = ps.Qr[(iz + 1) & 1];
 			cx<R>* C = ps.Cring[iz & 1];
 			const SolveCfg& scf = scfg[h.index];
 			cx<R>* fx = facx.as<cx<R>>() + (size_t)(iz & 1) * facx_half;
@@ -622,11 +630,11 @@ struct Plan : PlanBase {
 			// ---- setup stream ----
 			cs = streamB;
 			launch("eps_plane", ps.eps_bytes, [&] {
-				k_eps_plane<<<pgrid(N, ng), 256, 0, cs>>>(h.dir.as<double>(), h.fd, mk_, N, iz + 1, gps, QB);
+				k_eps_plane<R><<<pgrid(N, ng), 256, 0, cs>>>(h.dir.as<double>(), h.fd, mk_, N, iz + 1, gps, QB);
 			});
 			// coef(iz) overwrites the set the transition of slab iz-1 read (slab iz-2)
 			if(iz >= 1) CK(cudaStreamWaitEvent(streamB, eTrans, 0));
-			launch("coef", (double)N * ng * (2 * NQ * 8 + NCOEF * sc + NDIAG * sc + (wts ? 16 : 0)), [&] {
+			launch("coef", (double)N * ng * (2 * NQ * sizeof(R) + NCOEF * sc + NDIAG * sc + (wts ? 16 : 0)), [&] {
 				k_coef<R><<<pgrid(N, ng, 128), 128, 0, cs>>>(QA, QB, wts, iz, Gm, gps, C, ps.Dg);
 			});
 			CK(cudaEventRecord(eCoef, streamB));
@@ -643,11 +651,11 @@ struct Plan : PlanBase {
 			cs = stream;
 			CK(cudaStreamWaitEvent(stream, eCoef, 0));
 			// [phase(iz-1)] shift(iz-1) | shift(iz) phase(iz)   (BPMIteration.cpp:133-146)
-			rec_transition(h, slot0, nsl, ps.Cprev, C, ps.Fp, ps.Tb, ps.T2b, iz > 0);
+			const cx<R>* xsrc = rec_transition(h, slot0, nsl, ps.Cprev, C, ps.Fp, ps.Tb, ps.T2b, iz > 0);
 			CK(cudaEventRecord(eTrans, stream));
 			CK(cudaStreamWaitEvent(stream, eFac, 0));
 			fx_cur = fx; fy_cur = fy; lx_cur = lx; ly_cur = ly;
-			rec_adi(h, Gm, slot0, nsl, ng, Nw, C, ps.Fp, ps.Tb, ps.T2b);
+			rec_adi(h, Gm, slot0, nsl, ng, Nw, C, ps.Fp, ps.Tb, ps.T2b, xsrc);
 			CK(cudaEventRecord(eAdi[iz & 1], stream));
 			ps.Cprev = C;
 		}
@@ -665,7 +673,7 @@ struct Plan : PlanBase {
 		cs = stream;
 		if(Nz > 1) rec_transition(h, ps.slot0, ps.nsl, ps.Cprev, nullptr, ps.Fp, ps.Tb, ps.T2b, false);
 		const GroupParams* gps = ps.gps;
-		double* Qlast = ps.Qr[(Nz - 1) & 1];
+		R* Qlast = ps.Qr[(Nz - 1) & 1];
 		const int nsl = ps.nsl, slot0 = ps.slot0;
 		launch("fresnel_out", ps.field_pts * 4 * sc + (double)N * ps.ng * 3 * 8, [&] {
 			k_fresnel_out<R><<<pgrid(N, nsl), 256, 0, cs>>>(Gm, slot0, gps, Qlast, ps.Fp);
@@ -700,7 +708,9 @@ struct Plan : PlanBase {
 	// phase(CB), with CA / CB the coefficient sets of the previous / current slab (null: no
 	// phase) and two_shifts selecting shift(iz-1) followed by shift(iz). If every slot is at
 	// q = 0 the shifts reduce to the duplicate-border copy and the whole transition is one pass.
-	void rec_transition(SampleHost& h, int slot0, int nsl, const cx<R>* CA, const cx<R>* CB, cx<R>* Fp,
+	// Returns where the transitioned field is: Fp, or T2b when the one-pass kernel ran (only
+	// before a fused x-solve, which then reads it from there).
+	const cx<R>* rec_transition(SampleHost& h, int slot0, int nsl, const cx<R>* CA, const cx<R>* CB, cx<R>* Fp,
 			cx<R>* Tb, cx<R>* T2b, bool two_shifts) {
 		const Geom Gm = h.geom;
 		const double sc = sizeof(cx<R>);
@@ -710,7 +720,16 @@ struct Plan : PlanBase {
 			launch("phase_sync", fpb, [&] {
 				k_phase_sync<R><<<pgrid(Gm.N, nsl), 256, 0, cs>>>(Gm, slot0, CA, CB, Fp);
 			});
-			return;
+			return Fp;
+		}
+		if(CB && scfg[h.index].Mx > 0 && shift_fused) {
+			const int nsh = two_shifts ? 2 : 1;
+			dim3 grid((unsigned)((Gm.Nx + SHT - 1) / SHT), (unsigned)((Gm.Ny + SHT - 1) / SHT), (unsigned)nsl);
+			size_t smem = (size_t)4 * (SHT + 6) * (SHT + 6) * sizeof(cx<R>);
+			launch("shift_fused", fpb + (double)Gm.N * (nsl / Gm.spg) * 6 * sc, [&] {
+				k_shift_fused<R><<<grid, 256, smem, cs>>>(Gm, slot0, sp, CA, CB, nsh, Fp, T2b);
+			});
+			return T2b;
 		}
 		launch("shift_x", fpb, [&] {
 			k_shift_x<R><<<pgrid(Gm.N, nsl), 256, 0, cs>>>(Gm, slot0, sp, CA, Fp, T2b);
@@ -726,6 +745,7 @@ struct Plan : PlanBase {
 		launch("shift_y", fpb, [&] {
 			k_shift_y<R><<<pgrid(Gm.N, nsl), 256, 0, cs>>>(Gm, slot0, sp, CB, T2b, Fp);
 		});
+		return Fp;
 	}
 
 	// Sequential line solve (lines too long for the chunked kernels).
@@ -810,7 +830,7 @@ struct Plan : PlanBase {
 
 	// ParaxialPrimaryEvolutionOperator::apply (ParaxialPrimaryEvolutionOperator.cpp:153-209).
 	void rec_adi(SampleHost& h, const Geom& Gm, int slot0, int nsl, int ng, int Nw, const cx<R>* C, cx<R>* Fp,
-			cx<R>* Tb, cx<R>* T2b) {
+			cx<R>* Tb, cx<R>* T2b, const cx<R>* xsrc) {
 		const int N = Gm.N;
 		const double sc = sizeof(cx<R>);
 		dim3 gr = pgrid(N, nsl);
@@ -821,7 +841,7 @@ struct Plan : PlanBase {
 			if(fused) {
 				// t0 = solve(f + mu R f) written to T; Woodbury: t_k = solve(mu R' t_{k-1}),
 				// F = t0 + t1 + ... accumulated by the solves (the last t_k is not stored).
-				rec_solve_fused(dirn, false, h, Gm, slot0, nsl, ng, C, Fp, Tb, nullptr, nullptr);
+				rec_solve_fused(dirn, false, h, Gm, slot0, nsl, ng, C, dirn == 0 ? xsrc : Fp, Tb, nullptr, nullptr);
 			}
 			else {
 				if(dirn == 0)
@@ -928,6 +948,7 @@ struct Plan : PlanBase {
 
 	long long device_bytes() const override { return dev_bytes; }
 	double slab_ms() const override { return last_slab_ms; }
+	int slabs() const override { return S.empty() ? 0 : S[0]->geom.Nz - 1; }
 	long long voxel_steps() const override {
 		long long vs = 0;
 		for(auto& hp : S) vs += (long long)hp->geom.N * (hp->geom.Nz - 1) * hp->slots;

@@ -44,6 +44,8 @@ struct PlanBase {
 	// Streams, events, buffers; the first call that touches the device.
 	virtual void setup_device() = 0;
 	virtual long long voxel_steps() const = 0;
+	// Slabs of a one-sample plan (Nz - 1).
+	virtual int slabs() const = 0;
 	virtual long long device_bytes() const = 0;
 	virtual double slab_ms() const = 0;
 	virtual void profile(std::vector<std::string>& names, std::vector<double>& ms, std::vector<int>& cnt,

@@ -7,9 +7,10 @@
 //   * admission is first-come first-served under a device-memory budget: the head of the
 //     queue is admitted when its estimate fits next to the requests in flight, its director
 //     is uploaded and its entrance operators recorded;
-//   * every scheduling round advances each request in flight by a fixed number of slabs on
-//     its own CUDA streams, so requests of different meshes run side by side and new ones
-//     join at slab boundaries as earlier ones finish and free their memory;
+//   * every scheduling round advances each request in flight by as many slabs as fit a
+//     voxel-step quantum (at least one) on its own CUDA streams, so requests of different
+//     meshes run side by side, small ones finish in few rounds, and new ones join at slab
+//     boundaries as earlier ones finish and free their memory;
 //   * a finished request gets its exit operators, screen filter and the copy into the
 //     caller's buffer; its memory returns to the budget.
 // Each request runs exactly the launch sequence of a standalone run of the same plan, so its
@@ -17,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -51,6 +53,7 @@ struct Request {
 	double t_submit = 0, t_admit = 0, t_done = 0;
 	bool cancel = false;
 	bool finishing = false;
+	int slabs_per_round = 1;
 };
 
 }  // namespace
@@ -103,7 +106,6 @@ struct Server {
 
 	void loop() {
 		bool dev_ok = cudaSetDevice(opt.device) == cudaSuccess;
-		const int K = std::max(1, opt.slabs_per_round);
 		for(;;) {
 			std::vector<Request*> admit;
 			{
@@ -161,7 +163,7 @@ struct Server {
 			for(Request* r : cur) {
 				try {
 					if(!r->finishing) {
-						int left = r->plan->step_advance(K);
+						int left = r->plan->step_advance(r->slabs_per_round);
 						if(left == 0) {
 							r->plan->step_finish();
 							r->finishing = true;
@@ -249,6 +251,7 @@ void nbpm_default_server_options(nbpm_server_options* o) {
 	o->hbm_budget_gb = 150.0;
 	o->slabs_per_round = 8;
 	o->max_active = 0;
+	o->round_voxel_steps = 4e8;
 }
 
 int nbpm_server_create(const nbpm_server_options* opts, nbpm_server** out) {
@@ -286,6 +289,13 @@ int nbpm_server_submit(nbpm_server* h, const nbpm_sample* req, long long* id) {
 		r->plan = make_plan_host(1, req, po);
 		r->bytes = r->plan->estimate_bytes();
 		r->vs = r->plan->voxel_steps();
+		{
+			int nslab = std::max(1, r->plan->slabs());
+			double per_slab = (double)r->vs / nslab;
+			r->slabs_per_round = S.opt.round_voxel_steps > 0
+				? (int)std::max(1.0, std::min((double)nslab, std::floor(S.opt.round_voxel_steps / std::max(1.0, per_slab))))
+				: std::max(1, S.opt.slabs_per_round);
+		}
 		if(r->bytes > S.budget) {
 			char msg[200];
 			std::snprintf(msg, sizeof msg, "request needs %.3f GB of device memory, above the server budget of %.3f GB",

@@ -49,7 +49,8 @@ class Request:
 
 
 class Server:
-    def __init__(self, precision="fp32", hbm_budget_gb=150.0, slabs_per_round=8, max_active=0, device=0):
+    def __init__(self, precision="fp32", hbm_budget_gb=150.0, slabs_per_round=8, max_active=0, device=0,
+                 round_voxel_steps=4e8):
         lib = _lib.load()
         o = _lib.ServerOptions()
         lib.nbpm_default_server_options(ctypes.byref(o))
@@ -57,6 +58,7 @@ class Server:
         o.hbm_budget_gb = float(hbm_budget_gb)
         o.slabs_per_round = int(slabs_per_round)
         o.max_active = int(max_active)
+        o.round_voxel_steps = float(round_voxel_steps)
         o.device = int(device)
         h = ctypes.c_void_p()
         _lib.check(lib.nbpm_server_create(ctypes.byref(o), ctypes.byref(h)))

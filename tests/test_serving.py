@@ -62,7 +62,7 @@ def test_alone_equals_mix_equals_standalone(gpu, precision):
     E_mix = np.zeros_like(E_alone)
     E_plan = np.zeros_like(E_alone)
     api.run(js, lc, E_plan, precision=precision)
-    with Server(precision=precision, slabs_per_round=3) as srv:
+    with Server(precision=precision, slabs_per_round=3, round_voxel_steps=0) as srv:
         srv.submit(js, lc, E_alone).wait(timeout=300)
         others = [small_request(Nx=48, Ny=40, Nz=13, nl=2, seed=2), small_request(Nx=16, Ny=16, Nz=4, nl=1, seed=3,
                                                                                   q=((0.0, 0.0),)),
@@ -80,6 +80,18 @@ def test_alone_equals_mix_equals_standalone(gpu, precision):
         ref = np.zeros_like(E_o)
         api.run(js_o, lc_o, ref, precision=precision)
         np.testing.assert_array_equal(E_o, ref)
+
+
+@pytest.mark.gpu
+def test_round_quantum_does_not_change_results(gpu):
+    from nemaktis_gb300.serving import Server
+    js, lc, E1 = small_request(Nx=36, Ny=30, Nz=11, nl=3, seed=7)
+    E2 = np.zeros_like(E1)
+    with Server(round_voxel_steps=1.0) as srv:  # one slab per round
+        srv.submit(js, lc, E1).wait(timeout=300)
+    with Server(round_voxel_steps=1e12) as srv:  # every slab in one round
+        srv.submit(js, lc, E2).wait(timeout=300)
+    np.testing.assert_array_equal(E1, E2)
 
 
 @pytest.mark.gpu
