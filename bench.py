@@ -236,6 +236,15 @@ def run_ours(args):
                 "traffic_source": tr[1] if tr else None,
                 "share_of_step": r["ms"] / sum(v["ms"] for v in prof.values()),
                 "algorithmic_bytes_per_launch": r["bytes"] / max(1, r["launches"])}
+    peaks_meas = None
+    if not args.only_value:
+        from nemaktis_gb300 import _lib
+        lib = _lib.load()
+        peaks_meas = {}
+        for name, prec in (("fp32_tflops", _lib.FP32), ("fp64_tflops", _lib.FP64)):
+            t = ctypes.c_double()
+            if lib.nbpm_fma_peak(prec, ctypes.byref(t)) == 0:
+                peaks_meas[name] = t.value
     cpu = None
     if rank == 0 and not args.skip_cpu:
         cpu = cpu_baseline(samples, args.cpu_seconds)
@@ -251,7 +260,7 @@ def run_ours(args):
                          (sum(np.prod(c["shape"]) for c in samples) * (8 if prec == "fp32" else 16) / 1e6),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "clocks": clocks, "gpu_launches": launches, "wall_s": wall,
-        "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "fp64_plain": fp64,
+        "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "fp64_plain": fp64, "fma_peaks_measured": peaks_meas,
         "kernel_profile": {k: {"ms_per_step": v["ms"], "launches_per_step": v["launches"]} for k, v in (prof or {}).items()},
     }
     if rank == 0:

@@ -278,6 +278,11 @@ int nbpm_microscope_spectrum(nbpm_microscope* m, const nbpm_viewer_settings* set
 int nbpm_microscope_timing(const nbpm_microscope* m, double* focus_ms, double* spectrum_ms,
 		long long* device_bytes);
 
+/* Measured FMA throughput of the current device in TFLOP/s (2 flop per FMA), FP32 or FP64:
+ * the compute ceiling the FP64 plain path and the compute-heavy kernels are reported against.
+ * No counterpart in the reference. */
+int nbpm_fma_peak(int precision, double* tflops);
+
 /* Message of the last failure on this thread ("" if none). */
 const char* nbpm_last_error(void);
 

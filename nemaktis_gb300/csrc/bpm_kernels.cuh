@@ -385,7 +385,7 @@ __global__ void k_coef(const S* __restrict__ QA, const S* __restrict__ QB,
 // One launch covers the x factorisations (threads [0, ngroups*2*Ny)) and the y ones (the
 // following ngroups*2*Nx threads); scratch halves are separate.
 template <typename S>
-__global__ void k_factor(Geom G, int ngroups, int chunkMx, const cx<S>* __restrict__ diag,
+__global__ void k_factor(Geom G, int ngroups, int chunkMx, int chunksX, const cx<S>* __restrict__ diag,
 		cx<S>* __restrict__ facx, size_t planex, cx<double>* __restrict__ lscx,
 		cx<S>* __restrict__ facy, size_t planey, cx<double>* __restrict__ lscy, cx<S>* __restrict__ scr_all) {
 	typedef S T;
@@ -415,10 +415,11 @@ __global__ void k_factor(Geom G, int ngroups, int chunkMx, const cx<S>* __restri
 	// point index of element i (stencil coefficient / scratch layout)
 	auto P = [&](int i) { return base + i * stride; };
 	// factor storage index: natural layout, or chunk-interleaved x-line layout where element
-	// i = lane*M + k of a line sits at k*32 + lane (coalesced for one-warp-per-line solves)
+	// i = ci*M + k of chunk ci (of chunksX chunks per line) sits at k*chunksX + ci (coalesced
+	// for the chunked solves, one lane per chunk)
 	auto Q = [&](int i) -> size_t {
 		if(chunkM <= 0) return (size_t)P(i);
-		return (size_t)line * 32 * chunkM + (size_t)(i % chunkM) * 32 + (i / chunkM);
+		return (size_t)line * chunksX * chunkM + (size_t)(i % chunkM) * chunksX + (i / chunkM);
 	};
 	const cx<T> one = mk<T>(1, 0);
 	auto sup = [&](int i) { return -Dg[2 * (size_t)N + P(i)]; };
@@ -468,7 +469,7 @@ __global__ void k_factor(Geom G, int ngroups, int chunkMx, const cx<S>* __restri
 	}
 	if(chunkM > 0) {
 		// padding elements of the interleaved layout act as identity maps
-		for(int i = L - 1; i < 32 * chunkM; i++) {
+		for(int i = L - 1; i < chunksX * chunkM; i++) {
 			Fc[F_A * plane + Q(i)] = mk<S>(0, 0);
 			Fc[F_RB * plane + Q(i)] = mk<S>(0, 0);
 			Fc[F_W * plane + Q(i)] = mk<S>(0, 0);
@@ -1012,14 +1013,302 @@ __device__ __forceinline__ cx<R> shfl_xor_c(cx<R> v, int m) {
 // coefficient loaded once for the KS slots and staged through shared memory so that global
 // accesses stay coalesced; the factor planes are stored chunk-interleaved (element l*M+k at
 // k*32+l) and are also loaded once for the KS slots. Block = LT warps = LT lines.
+// ---------------------------------------------------------------------------------------
+// Chunk-parallel factorisation: the same outputs as k_factor, with every line split into
+// chunks processed by different threads. The pivots follow the continued fraction
+// beta_i = mid'_i - inf_i sup_{i-1} / beta_{i-1}, a Moebius map: (p, q) -> M_i (p, q) with
+// M_i = [[mid'_i, -inf_i sup_{i-1}], [1, 0]] and beta = p / q. Each chunk forms the product of
+// its maps (rescaled to keep it bounded; the map is projective), the chunk products are
+// combined with an exclusive scan, and each chunk replays its elements from the pivot before
+// it. corr (forward), the back-substituted corr and w are affine recurrences combined the same
+// way. x-lines: one warp per line, lanes = chunks of chunkM elements (the interleaved factor
+// layout), combined with shuffles. y-lines: 32 columns per block (lanes), warps = chunks of
+// rows, combined through shared memory. Intermediate values go to the output planes and are
+// read back by the same thread.
+template <typename T>
+struct Mob {
+	cx<T> a, b, c, d;  // [[a, b], [c, d]]
+};
+template <typename T>
+__device__ __forceinline__ Mob<T> mob_mul(const Mob<T>& X, const Mob<T>& Y) {  // X . Y
+	return Mob<T>{X.a * Y.a + X.b * Y.c, X.a * Y.b + X.b * Y.d, X.c * Y.a + X.d * Y.c, X.c * Y.b + X.d * Y.d};
+}
+template <typename T>
+__device__ __forceinline__ T l1abs(cx<T> z) { return fabs(z.x) + fabs(z.y); }
+template <typename T>
+__device__ __forceinline__ void mob_norm(Mob<T>& X) {
+	T m = fmax(fmax(l1abs(X.a), l1abs(X.b)), fmax(l1abs(X.c), l1abs(X.d)));
+	if(m > (T)0) {
+		T r = (T)1 / m;
+		X.a = X.a * r; X.b = X.b * r; X.c = X.c * r; X.d = X.d * r;
+	}
+}
+template <typename T>
+struct Aff {
+	cx<T> A, B;  // x -> A x + B
+};
+template <typename T>
+__device__ __forceinline__ Aff<T> aff_after(const Aff<T>& second, const Aff<T>& first) {
+	return Aff<T>{second.A * first.A, second.A * first.B + second.B};
+}
+template <typename T>
+__device__ __forceinline__ Mob<T> shfl_up_m(const Mob<T>& X, int o) {
+	return Mob<T>{shfl_up_c(X.a, o), shfl_up_c(X.b, o), shfl_up_c(X.c, o), shfl_up_c(X.d, o)};
+}
+template <typename T>
+__device__ __forceinline__ Aff<T> shfl_up_a(const Aff<T>& X, int o) { return Aff<T>{shfl_up_c(X.A, o), shfl_up_c(X.B, o)}; }
+template <typename T>
+__device__ __forceinline__ Aff<T> shfl_down_a(const Aff<T>& X, int o) { return Aff<T>{shfl_down_c(X.A, o), shfl_down_c(X.B, o)}; }
+
+template <typename S, int DIRN>
+__global__ void __launch_bounds__(256) k_factor_chunked(Geom G, int ngroups, int chunkMx, int chunksX, int W,
+		const cx<S>* __restrict__ diag, cx<S>* __restrict__ fac, size_t plane, cx<double>* __restrict__ lsc) {
+	typedef S T;
+	const int Nx = G.Nx, Ny = G.Ny, N = G.N;
+	const int L = DIRN == 0 ? Nx : Ny;
+	const int nlines = DIRN == 0 ? Ny : Nx;
+	const int n = L - 1;
+	const int lane = threadIdx.x, w = threadIdx.y;
+	int line, gc, chunk, nchunks, M;
+	if(DIRN == 0) {
+		line = blockIdx.x * blockDim.y + w;
+		gc = blockIdx.y;
+		chunk = lane;
+		nchunks = 32;
+		M = (n + 31) / 32;
+	}
+	else {
+		line = blockIdx.x * 32 + lane;
+		gc = blockIdx.y;
+		chunk = w;
+		nchunks = W;
+		M = (n + W - 1) / W;
+	}
+	const bool active = line < nlines && L > 3;
+	const int g = gc / 2, c = gc % 2;
+	const int i0 = chunk * M, i1 = min(i0 + M, n);
+	const cx<T>* Dg = diag + (size_t)g * NDIAG * N + (size_t)(DIRN * 6 + c * 3) * N;
+	cx<S>* Fc = fac + ((size_t)g * 2 + c) * NFAC * plane;
+	const int stride = DIRN == 0 ? 1 : Nx;
+	const int base = DIRN == 0 ? Nx * line : line;
+	auto P = [&](int i) { return base + i * stride; };
+	// storage: natural layout, or the solves' chunk-interleaved x layout (chunksX chunks of
+	// chunkMx elements per line, element i = ci*chunkMx + k at k*chunksX + ci)
+	auto Q = [&](int i) -> size_t {
+		if(DIRN == 1 || chunkMx <= 0) return (size_t)P(i);
+		return (size_t)line * chunksX * chunkMx + (size_t)(i % chunkMx) * chunksX + (i / chunkMx);
+	};
+	const cx<T> one = mk<T>(1, 0), zero = mk<T>(0, 0);
+	auto sup = [&](int i) { return -Dg[2 * (size_t)N + P(i)]; };
+	auto mid = [&](int i) { return one - Dg[1 * (size_t)N + P(i)]; };
+	auto inf = [&](int i) { return -Dg[P(i)]; };
+	cx<T> m0 = zero, a0 = zero, corner = zero;
+	if(active) {
+		m0 = mid(0);
+		a0 = inf(0);
+		corner = cdiv(sup(n - 1) * a0, m0);
+	}
+	auto midp = [&](int i) { return i == n - 1 ? mid(i) + corner : mid(i); };
+	// shared memory for the y combine: [W][32] per quantity
+	extern __shared__ unsigned char smem_raw[];
+	Mob<T>* shM = reinterpret_cast<Mob<T>*>(smem_raw);
+	Aff<T>* shA = reinterpret_cast<Aff<T>*>(shM + (DIRN == 1 ? W * 32 : 0));
+	Aff<T>* shB = shA + (DIRN == 1 ? W * 32 : 0);
+	cx<T>* shX = reinterpret_cast<cx<T>*>(shB + (DIRN == 1 ? W * 32 : 0));  // [2][32] corr_last, cv0
+
+	// ---- 1. pivots: chunk product of the Moebius maps ----
+	Mob<T> Pm{one, zero, zero, one};
+	if(active) {
+		for(int i = i0; i < i1; i++) {
+			Mob<T> Mi;
+			if(i == 0) Mi = Mob<T>{zero, (T)2 * m0, zero, one};
+			else Mi = Mob<T>{midp(i), -(inf(i) * sup(i - 1)), one, zero};
+			Pm = mob_mul(Mi, Pm);
+			mob_norm(Pm);
+		}
+	}
+	// exclusive scan over chunks in order: Sx = P_{c-1} ... P_0
+	Mob<T> Sx{one, zero, zero, one};
+	if(DIRN == 0) {
+		Mob<T> X = Pm;
+#pragma unroll
+		for(int o = 1; o < 32; o <<= 1) {
+			Mob<T> Y = shfl_up_m(X, o);
+			if(lane >= o) { X = mob_mul(X, Y); mob_norm(X); }
+		}
+		Mob<T> E = shfl_up_m(X, 1);
+		if(lane > 0) Sx = E;
+	}
+	else {
+		shM[w * 32 + lane] = Pm;
+		__syncthreads();
+		if(w == 0) {
+			Mob<T> acc{one, zero, zero, one};
+			for(int k = 0; k < W; k++) {
+				Mob<T> pk = shM[k * 32 + lane];
+				shM[k * 32 + lane] = acc;
+				acc = mob_mul(pk, acc);
+				mob_norm(acc);
+			}
+		}
+		__syncthreads();
+		Sx = shM[w * 32 + lane];
+	}
+	// replay: beta, and the chunk maps of corr (forward) and w
+	Aff<T> Fcorr{one, zero}, Fw{one, zero};
+	cx<T> beta_prev = zero;
+	if(active && i0 < i1) {
+		if(i0 > 0) beta_prev = cdiv(Sx.b, Sx.d);  // state before the chunk: Sx . (0, 1)
+		for(int i = i0; i < i1; i++) {
+			cx<T> beta = i == 0 ? (T)2 * m0 : midp(i) - cdiv(inf(i) * sup(i - 1), beta_prev);
+			cx<T> rb = crecip(beta);
+			cx<T> alpha = i == 0 ? zero : -(inf(i) * rb);
+			Fc[F_RB * plane + Q(i)] = cvt<S>(rb);
+			Fc[F_A * plane + Q(i)] = cvt<S>(alpha);
+			Fc[F_C * plane + Q(i)] = i < n - 1 ? cvt<S>(-(sup(i) * rb)) : mk<S>(0, 0);
+			// corr_0 = -1/2, corr_i = alpha_i corr_{i-1} (+ sup_{n-1} rb_{n-1} on the last row)
+			Aff<T> ec = i == 0 ? Aff<T>{zero, mk<T>(-0.5, 0)} : Aff<T>{alpha, i == n - 1 ? sup(i) * rb : zero};
+			Fcorr = aff_after(ec, Fcorr);
+			// w_0 = 1, w_i = -gamma_{i-1} w_{i-1}, gamma_{i-1} = sup_{i-1} / beta_{i-1}
+			Aff<T> ew = i == 0 ? Aff<T>{zero, one} : Aff<T>{-cdiv(sup(i - 1), beta_prev), zero};
+			Fw = aff_after(ew, Fw);
+			beta_prev = beta;
+		}
+	}
+	// ---- 2. exclusive scans of the corr and w maps, replay ----
+	Aff<T> Ec{one, zero}, Ew{one, zero};
+	if(DIRN == 0) {
+		Aff<T> Xc = Fcorr, Xw = Fw;
+#pragma unroll
+		for(int o = 1; o < 32; o <<= 1) {
+			Aff<T> Yc = shfl_up_a(Xc, o), Yw = shfl_up_a(Xw, o);
+			if(lane >= o) { Xc = aff_after(Xc, Yc); Xw = aff_after(Xw, Yw); }
+		}
+		Aff<T> Pc = shfl_up_a(Xc, 1), Pw = shfl_up_a(Xw, 1);
+		if(lane > 0) { Ec = Pc; Ew = Pw; }
+	}
+	else {
+		__syncthreads();
+		shA[w * 32 + lane] = Fcorr;
+		shB[w * 32 + lane] = Fw;
+		__syncthreads();
+		if(w == 0) {
+			Aff<T> ac{one, zero}, aw{one, zero};
+			for(int k = 0; k < W; k++) {
+				Aff<T> fc = shA[k * 32 + lane], fw = shB[k * 32 + lane];
+				shA[k * 32 + lane] = ac;
+				shB[k * 32 + lane] = aw;
+				ac = aff_after(fc, ac);
+				aw = aff_after(fw, aw);
+			}
+		}
+		__syncthreads();
+		Ec = shA[w * 32 + lane];
+		Ew = shB[w * 32 + lane];
+	}
+	if(DIRN == 0) __syncwarp();  // F_C of the previous chunk, written by another lane
+	cx<T> corr_last = zero;
+	bool own_last = active && i0 <= n - 1 && n - 1 < i1;
+	if(active && i0 < i1) {
+		cx<T> cr = Ec.B, wv = Ew.B;  // values before the chunk (maps applied to 0)
+		for(int i = i0; i < i1; i++) {
+			cx<T> alpha = cvt<T>(Fc[F_A * plane + Q(i)]);
+			cx<T> rb = cvt<T>(Fc[F_RB * plane + Q(i)]);
+			if(i == 0) { cr = mk<T>(-0.5, 0); wv = one; }
+			else {
+				cx<T> gm = -cvt<T>(Fc[F_C * plane + Q(i - 1)]);  // gamma_{i-1}
+				cr = alpha * cr + (i == n - 1 ? sup(i) * rb : zero);
+				wv = -(gm * wv);
+			}
+			Fc[F_COR * plane + Q(i)] = cvt<S>(cr);  // forward corr, replaced below
+			Fc[F_W * plane + Q(i)] = cvt<S>(wv);
+			if(i == n - 1) corr_last = cr;
+		}
+	}
+	// broadcast corr_last to the line
+	if(DIRN == 0) {
+		corr_last = shfl_idx_c(corr_last, (n - 1) / M);
+	}
+	else {
+		__syncthreads();
+		if(own_last) shX[lane] = corr_last;
+		__syncthreads();
+		corr_last = shX[lane];
+	}
+	// ---- 3. back-substituted corr: cv_{n-1} = corr_last, cv_j = -gamma_j cv_{j+1} + corr_j ----
+	Aff<T> Bm{one, zero};
+	if(active && i0 < i1) {
+		for(int j = i1 - 1; j >= i0; j--) {
+			Aff<T> e = j == n - 1 ? Aff<T>{zero, corr_last}
+				: Aff<T>{cvt<T>(Fc[F_C * plane + Q(j)]), cvt<T>(Fc[F_COR * plane + Q(j)])};
+			Bm = aff_after(e, Bm);
+		}
+	}
+	Aff<T> Eb{one, zero};
+	if(DIRN == 0) {
+		Aff<T> X = Bm;
+#pragma unroll
+		for(int o = 1; o < 32; o <<= 1) {
+			Aff<T> Y = shfl_down_a(X, o);
+			if(lane + o < 32) X = aff_after(X, Y);
+		}
+		Aff<T> Nn = shfl_down_a(X, 1);
+		if(lane < 31) Eb = Nn;
+	}
+	else {
+		__syncthreads();
+		shA[w * 32 + lane] = Bm;
+		__syncthreads();
+		if(w == 0) {
+			Aff<T> acc{one, zero};
+			for(int k = W - 1; k >= 0; k--) {
+				Aff<T> f = shA[k * 32 + lane];
+				shA[k * 32 + lane] = acc;
+				acc = aff_after(f, acc);
+			}
+		}
+		__syncthreads();
+		Eb = shA[w * 32 + lane];
+	}
+	cx<T> cv0 = zero;
+	if(active && i0 < i1) {
+		cx<T> cv = Eb.B;  // cv of the element after the chunk
+		for(int j = i1 - 1; j >= i0; j--) {
+			cv = j == n - 1 ? corr_last
+				: cvt<T>(Fc[F_C * plane + Q(j)]) * cv + cvt<T>(Fc[F_COR * plane + Q(j)]);
+			Fc[F_COR * plane + Q(j)] = cvt<S>(cv);
+		}
+		if(i0 == 0) cv0 = cv;
+	}
+	// padding of the interleaved x layout: identity maps
+	if(DIRN == 0 && chunkMx > 0 && active) {
+		for(int i = n + lane; i < chunksX * chunkMx; i += 32) {
+			Fc[F_A * plane + Q(i)] = mk<S>(0, 0);
+			Fc[F_RB * plane + Q(i)] = mk<S>(0, 0);
+			Fc[F_W * plane + Q(i)] = mk<S>(0, 0);
+			Fc[F_C * plane + Q(i)] = mk<S>(0, 0);
+			Fc[F_COR * plane + Q(i)] = mk<S>(0, 0);
+		}
+	}
+	// Sherman-Morrison scalars in FP64
+	if(active && chunk == 0) {
+		cx<double>* ls = lsc + (((size_t)g * 2 + c) * nlines + line) * 2;
+		cx<double> r0 = cdiv(cvt<double>(a0), cvt<double>(m0));
+		ls[0] = r0;
+		ls[1] = crecip(mk(1.0, 0.0) + cvt<double>(cv0) - r0 * cvt<double>(corr_last));
+	}
+}
+
 template <typename R, int M, int KIND, int KS>
+// Resident blocks per SM requested from the compiler: 8 (64 registers) for the instances
+// whose chunk values fit, measured faster on GB300; the larger instances keep their registers.
 #ifndef NBPM_XC_MINB
-#define NBPM_XC_MINB 1
+#define NBPM_XC_MINB(MK) ((MK) <= 16 ? 8 : 1)
 #endif
 #ifndef NBPM_YC_MINB
 #define NBPM_YC_MINB 1
 #endif
-__global__ void __launch_bounds__(128, NBPM_XC_MINB) k_solve_xc(Geom G, int slot0, int nch, const cx<R>* __restrict__ coef,
+__global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_xc(Geom G, int slot0, int nch, const cx<R>* __restrict__ coef,
 		const cx<R>* __restrict__ fac, size_t plane, const cx<double>* __restrict__ lsc,
 		const cx<R>* __restrict__ src, cx<R>* __restrict__ dst, const cx<R>* acc_in, cx<R>* acc_out) {
 	extern __shared__ unsigned char smem_raw[];
@@ -1292,6 +1581,466 @@ __global__ void __launch_bounds__(512, NBPM_YC_MINB) k_solve_yc(Geom G, int slot
 #pragma unroll
 			for(int j = 0; j < KS; j++) {
 				d[j] = cc * d[j] + v[j][k];
+				cx<R> x = d[j] - fr[j] * cr;
+				size_t off = (size_t)(s0 + j) * 2 * N + (size_t)c * N;
+				if(dst) dst[off + q] = x;
+				if(acc_out) acc_out[off + q] = acc_in[off + q] + x;
+				if(i == 0) {
+					size_t qe = (size_t)ix + (size_t)Nx * (Ny - 1);
+					if(dst) dst[off + qe] = x;
+					if(acc_out) acc_out[off + qe] = acc_in[off + qe] + x;
+				}
+			}
+		}
+	}
+}
+
+// x-line solve for long lines: one block of W warps per line, 32*W chunks of M points (the
+// chunk-interleaved factor layout with 32*W chunks). Within a warp the chunk maps combine with
+// shuffles as in k_solve_xc, across the warps of the line through shared memory.
+template <typename R, int M, int KIND, int KS>
+__global__ void __launch_bounds__(256) k_solve_xw(Geom G, int slot0, int nch, const cx<R>* __restrict__ coef,
+		const cx<R>* __restrict__ fac, size_t plane, const cx<double>* __restrict__ lsc,
+		const cx<R>* __restrict__ src, cx<R>* __restrict__ dst, const cx<R>* acc_in, cx<R>* acc_out) {
+	extern __shared__ unsigned char smem_raw[];
+	const int W = blockDim.x / 32;
+	const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+	const int Nx = G.Nx, Ny = G.Ny, N = G.N;
+	const int iy = blockIdx.x;
+	const int c = blockIdx.y % 2, bc = blockIdx.y / 2;
+	const int g = bc / nch, ch = bc % nch;
+	const int s0 = g * G.spg + ch * KS;
+	const int n_unk = Nx - 1;
+	const int CH = 32 * W;
+	const int ci = warp * 32 + lane;
+	const int PITCH = CH * (M + 1);
+	cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw);  // [KS][CH][M+1]
+	cx<R>* sA = buf + KS * PITCH;                     // [KS][W]
+	cx<R>* sB = sA + KS * W;
+	cx<R>* sD = sB + KS * W;
+	cx<R>* sP = sD + KS * W;
+	cx<R>* sX = sP + KS * W;                          // [KS][2]: d at the last unknown, fr
+	const cx<R>* Fc = fac + ((size_t)g * 2 + c) * NFAC * plane + (size_t)iy * CH * M;
+	const cx<double>* ls = lsc + (((size_t)g * 2 + c) * Ny + iy) * 2;
+	const cx<double> r0 = ls[0], rden = ls[1];
+	const int i0 = ci * M;
+	const int last = n_unk - 1;
+	const cx<R> one = mk<R>(1, 0), zero = mk<R>(0, 0);
+	const Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
+	const cx<R>* f0 = src + (size_t)s0 * 2 * N;
+	for(int e = threadIdx.x; e < n_unk; e += blockDim.x) {
+		cx<R> r[KS];
+		composite_m<R, KIND, KS>(st, c, e, iy, f0, r);
+#pragma unroll
+		for(int j = 0; j < KS; j++) buf[j * PITCH + (e / M) * (M + 1) + e % M] = r[j];
+	}
+	__syncthreads();
+	cx<R> v[KS][M];
+	cx<R> A[KS], B[KS];
+#pragma unroll
+	for(int j = 0; j < KS; j++) { A[j] = one; B[j] = zero; }
+#pragma unroll
+	for(int k = 0; k < M; k++) {
+		bool ok = i0 + k < n_unk;
+		cx<R> a = zero, rb = zero;
+		if(ok) { a = Fc[F_A * plane + k * CH + ci]; rb = Fc[F_RB * plane + k * CH + ci]; }
+#pragma unroll
+		for(int j = 0; j < KS; j++) {
+			v[j][k] = zero;
+			if(ok) {
+				cx<R> b = buf[j * PITCH + ci * (M + 1) + k] * rb;
+				v[j][k] = b;
+				B[j] = a * B[j] + b;
+				A[j] = a * A[j];
+			}
+		}
+	}
+	// forward: inclusive scan within the warp, then the warps' totals in order
+#pragma unroll
+	for(int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+		for(int j = 0; j < KS; j++) {
+			cx<R> Ap = shfl_up_c(A[j], o), Bp = shfl_up_c(B[j], o);
+			if(lane >= o) { B[j] = A[j] * Bp + B[j]; A[j] = A[j] * Ap; }
+		}
+	}
+	if(lane == 31) {
+#pragma unroll
+		for(int j = 0; j < KS; j++) { sA[j * W + warp] = A[j]; sB[j * W + warp] = B[j]; }
+	}
+	__syncthreads();
+	if(threadIdx.x < KS) {
+		int j = threadIdx.x;
+		cx<R> D = zero;
+		for(int ww = 0; ww < W; ww++) {
+			sD[j * W + ww] = D;
+			D = sA[j * W + ww] * D + sB[j * W + ww];
+		}
+	}
+	__syncthreads();
+	cx<R> d[KS], acc[KS];
+#pragma unroll
+	for(int j = 0; j < KS; j++) {
+		cx<R> Ae = shfl_up_c(A[j], 1), Be = shfl_up_c(B[j], 1);
+		if(lane == 0) { Ae = one; Be = zero; }
+		d[j] = Ae * sD[j * W + warp] + Be;
+		acc[j] = zero;
+	}
+#pragma unroll
+	for(int k = 0; k < M; k++) {
+		if(i0 + k < n_unk) {
+			cx<R> a = Fc[F_A * plane + k * CH + ci], w = Fc[F_W * plane + k * CH + ci];
+#pragma unroll
+			for(int j = 0; j < KS; j++) {
+				d[j] = a * d[j] + v[j][k];
+				v[j][k] = d[j];
+				acc[j] += w * d[j];
+			}
+			if(i0 + k == last) {
+#pragma unroll
+				for(int j = 0; j < KS; j++) sX[2 * j] = d[j];
+			}
+		}
+	}
+#pragma unroll
+	for(int j = 0; j < KS; j++) {
+#pragma unroll
+		for(int o = 16; o > 0; o >>= 1) acc[j] += shfl_xor_c(acc[j], o);
+		if(lane == 0) sP[j * W + warp] = acc[j];
+	}
+	__syncthreads();
+	if(threadIdx.x < KS) {
+		int j = threadIdx.x;
+		cx<R> tot = zero;
+		for(int ww = 0; ww < W; ww++) tot += sP[j * W + ww];
+		sX[2 * j + 1] = cvt<R>((cvt<double>(tot) - r0 * cvt<double>(sX[2 * j])) * rden);
+	}
+	// backward: chunk maps, inclusive scan from the line's end
+#pragma unroll
+	for(int j = 0; j < KS; j++) { A[j] = one; B[j] = zero; }
+#pragma unroll
+	for(int k = M - 1; k >= 0; k--) {
+		if(i0 + k < n_unk) {
+			cx<R> cc = Fc[F_C * plane + k * CH + ci];
+#pragma unroll
+			for(int j = 0; j < KS; j++) { B[j] = cc * B[j] + v[j][k]; A[j] = cc * A[j]; }
+		}
+	}
+#pragma unroll
+	for(int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+		for(int j = 0; j < KS; j++) {
+			cx<R> An = shfl_down_c(A[j], o), Bn = shfl_down_c(B[j], o);
+			if(lane + o < 32) { B[j] = A[j] * Bn + B[j]; A[j] = A[j] * An; }
+		}
+	}
+	__syncthreads();  // sD of the forward pass has been read
+	if(lane == 0) {
+#pragma unroll
+		for(int j = 0; j < KS; j++) { sA[j * W + warp] = A[j]; sB[j * W + warp] = B[j]; }
+	}
+	__syncthreads();
+	if(threadIdx.x < KS) {
+		int j = threadIdx.x;
+		cx<R> D = zero;
+		for(int ww = W - 1; ww >= 0; ww--) {
+			sD[j * W + ww] = D;
+			D = sA[j * W + ww] * D + sB[j * W + ww];
+		}
+	}
+	__syncthreads();
+	cx<R> fr[KS];
+#pragma unroll
+	for(int j = 0; j < KS; j++) {
+		fr[j] = sX[2 * j + 1];
+		cx<R> An = shfl_down_c(A[j], 1), Bn = shfl_down_c(B[j], 1);
+		if(lane == 31) { An = one; Bn = zero; }
+		d[j] = An * sD[j * W + warp] + Bn;
+	}
+#pragma unroll
+	for(int k = M - 1; k >= 0; k--) {
+		if(i0 + k < n_unk) {
+			cx<R> cc = Fc[F_C * plane + k * CH + ci], cr = Fc[F_COR * plane + k * CH + ci];
+#pragma unroll
+			for(int j = 0; j < KS; j++) {
+				d[j] = cc * d[j] + v[j][k];
+				buf[j * PITCH + ci * (M + 1) + k] = d[j] - fr[j] * cr;
+			}
+		}
+	}
+	__syncthreads();
+	for(int j = 0; j < KS; j++) {
+		const size_t off = (size_t)(s0 + j) * 2 * N + (size_t)c * N + (size_t)iy * Nx;
+		for(int e = threadIdx.x; e < Nx; e += blockDim.x) {
+			int ee = e == Nx - 1 ? 0 : e;
+			cx<R> x = buf[j * PITCH + (ee / M) * (M + 1) + ee % M];
+			if(dst) dst[off + e] = x;
+			if(acc_out) acc_out[off + e] = acc_in[off + e] + x;
+		}
+	}
+}
+
+// x-line solve with the chunk values in the warp's shared-memory buffer instead of registers
+// (same algorithm and layout as k_solve_xc): for long lines (large M) the per-thread state
+// stays small, so more warps stay resident.
+template <typename R, int KIND, int KS>
+__global__ void __launch_bounds__(128) k_solve_xs(Geom G, int slot0, int nch, int M, const cx<R>* __restrict__ coef,
+		const cx<R>* __restrict__ fac, size_t plane, const cx<double>* __restrict__ lsc,
+		const cx<R>* __restrict__ src, cx<R>* __restrict__ dst, const cx<R>* acc_in, cx<R>* acc_out) {
+	extern __shared__ unsigned char smem_raw[];
+	const int LT = blockDim.x / 32;
+	const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+	const int Nx = G.Nx, Ny = G.Ny, N = G.N;
+	const int iy = blockIdx.x * LT + warp;
+	if(iy >= Ny) return;
+	const int c = blockIdx.y % 2, bc = blockIdx.y / 2;
+	const int g = bc / nch, ch = bc % nch;
+	const int s0 = g * G.spg + ch * KS;
+	const int n_unk = Nx - 1;
+	const int PITCH = 32 * (M + 1);
+	cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw) + (size_t)warp * KS * PITCH;
+	const cx<R>* Fc = fac + ((size_t)g * 2 + c) * NFAC * plane + (size_t)iy * 32 * M;
+	const cx<double>* ls = lsc + (((size_t)g * 2 + c) * Ny + iy) * 2;
+	const cx<double> r0 = ls[0], rden = ls[1];
+	const int i0 = lane * M;
+	const int last = n_unk - 1, lane_last = last / M, k_last = last % M;
+	const cx<R> one = mk<R>(1, 0), zero = mk<R>(0, 0);
+	const Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
+	const cx<R>* f0 = src + (size_t)s0 * 2 * N;
+	for(int e = lane; e < n_unk; e += 32) {
+		cx<R> r[KS];
+		composite_m<R, KIND, KS>(st, c, e, iy, f0, r);
+#pragma unroll
+		for(int j = 0; j < KS; j++) buf[j * PITCH + (e / M) * (M + 1) + e % M] = r[j];
+	}
+	__syncwarp();
+	auto V = [&](int j, int k) -> cx<R>& { return buf[j * PITCH + lane * (M + 1) + k]; };
+	cx<R> A[KS], B[KS];
+#pragma unroll
+	for(int j = 0; j < KS; j++) { A[j] = one; B[j] = zero; }
+	for(int k = 0; k < M; k++) {
+		if(i0 + k < n_unk) {
+			cx<R> a = Fc[F_A * plane + k * 32 + lane], rb = Fc[F_RB * plane + k * 32 + lane];
+#pragma unroll
+			for(int j = 0; j < KS; j++) {
+				cx<R> b = V(j, k) * rb;
+				V(j, k) = b;
+				B[j] = a * B[j] + b;
+				A[j] = a * A[j];
+			}
+		}
+	}
+#pragma unroll
+	for(int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+		for(int j = 0; j < KS; j++) {
+			cx<R> Ap = shfl_up_c(A[j], o), Bp = shfl_up_c(B[j], o);
+			if(lane >= o) { B[j] = A[j] * Bp + B[j]; A[j] = A[j] * Ap; }
+		}
+	}
+	cx<R> d[KS], acc[KS], dl[KS];
+#pragma unroll
+	for(int j = 0; j < KS; j++) {
+		d[j] = shfl_up_c(B[j], 1);
+		if(lane == 0) d[j] = zero;
+		acc[j] = zero;
+		dl[j] = zero;
+	}
+	for(int k = 0; k < M; k++) {
+		if(i0 + k < n_unk) {
+			cx<R> a = Fc[F_A * plane + k * 32 + lane], w = Fc[F_W * plane + k * 32 + lane];
+#pragma unroll
+			for(int j = 0; j < KS; j++) {
+				d[j] = a * d[j] + V(j, k);
+				V(j, k) = d[j];
+				acc[j] += w * d[j];
+			}
+		}
+		if(k == k_last) {
+#pragma unroll
+			for(int j = 0; j < KS; j++) dl[j] = d[j];
+		}
+	}
+	cx<R> fr[KS];
+#pragma unroll
+	for(int j = 0; j < KS; j++) {
+#pragma unroll
+		for(int o = 16; o > 0; o >>= 1) acc[j] += shfl_xor_c(acc[j], o);
+		dl[j] = shfl_idx_c(dl[j], lane_last);
+		fr[j] = cvt<R>((cvt<double>(acc[j]) - r0 * cvt<double>(dl[j])) * rden);
+		A[j] = one;
+		B[j] = zero;
+	}
+	for(int k = M - 1; k >= 0; k--) {
+		if(i0 + k < n_unk) {
+			cx<R> cc = Fc[F_C * plane + k * 32 + lane];
+#pragma unroll
+			for(int j = 0; j < KS; j++) { B[j] = cc * B[j] + V(j, k); A[j] = cc * A[j]; }
+		}
+	}
+#pragma unroll
+	for(int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+		for(int j = 0; j < KS; j++) {
+			cx<R> An = shfl_down_c(A[j], o), Bn = shfl_down_c(B[j], o);
+			if(lane + o < 32) { B[j] = A[j] * Bn + B[j]; A[j] = A[j] * An; }
+		}
+	}
+#pragma unroll
+	for(int j = 0; j < KS; j++) {
+		d[j] = shfl_down_c(B[j], 1);
+		if(lane == 31) d[j] = zero;
+	}
+	for(int k = M - 1; k >= 0; k--) {
+		if(i0 + k < n_unk) {
+			cx<R> cc = Fc[F_C * plane + k * 32 + lane], cr = Fc[F_COR * plane + k * 32 + lane];
+#pragma unroll
+			for(int j = 0; j < KS; j++) {
+				d[j] = cc * d[j] + V(j, k);
+				V(j, k) = d[j] - fr[j] * cr;
+			}
+		}
+	}
+	__syncwarp();
+	for(int j = 0; j < KS; j++) {
+		const size_t off = (size_t)(s0 + j) * 2 * N + (size_t)c * N + (size_t)iy * Nx;
+		for(int e = lane; e < Nx; e += 32) {
+			int ee = e == Nx - 1 ? 0 : e;
+			cx<R> x = buf[j * PITCH + (ee / M) * (M + 1) + ee % M];
+			if(dst) dst[off + e] = x;
+			if(acc_out) acc_out[off + e] = acc_in[off + e] + x;
+		}
+	}
+}
+
+// y-line solve for any Ny (same algorithm as k_solve_yc): block = 32 columns x W warps,
+// warp w owns rows [w*M, w*M+M) with M = ceil((Ny-1)/W); the chunk values are kept in the
+// scratch array vbuf (field layout, L2-resident while the block runs) instead of registers,
+// so neither Ny nor the chunk length is bounded by the register file.
+template <typename R, int KIND, int KS>
+__global__ void __launch_bounds__(256) k_solve_ys(Geom G, int slot0, int nch, const cx<R>* __restrict__ coef,
+		const cx<R>* __restrict__ fac, size_t plane, const cx<double>* __restrict__ lsc,
+		const cx<R>* __restrict__ src, cx<R>* __restrict__ dst, const cx<R>* acc_in, cx<R>* acc_out,
+		cx<R>* __restrict__ vbuf) {
+	extern __shared__ unsigned char smem_raw[];
+	const int WY = blockDim.y;
+	const int lane = threadIdx.x, w = threadIdx.y;
+	const int Nx = G.Nx, Ny = G.Ny, N = G.N;
+	const int ix = blockIdx.x * 32 + lane;
+	const bool col = ix < Nx;
+	const int c = blockIdx.y % 2, bc = blockIdx.y / 2;
+	const int g = bc / nch, ch = bc % nch;
+	const int s0 = g * G.spg + ch * KS;
+	const int n_unk = Ny - 1;
+	const int M = (n_unk + WY - 1) / WY;
+	const int i0 = w * M, i1 = min(i0 + M, n_unk);
+	const int SZ = WY * 32;
+	cx<R>* sA = reinterpret_cast<cx<R>*>(smem_raw);  // [KS][WY][32]
+	cx<R>* sB = sA + KS * SZ;
+	cx<R>* sD = sB + KS * SZ;
+	cx<R>* sP = sD + KS * SZ;
+	cx<R>* sL = sP + KS * SZ;                         // [KS][32]
+	cx<R>* sF = sL + KS * 32;                         // [KS][32]
+	const cx<R>* Fc = fac + ((size_t)g * 2 + c) * NFAC * plane;
+	const cx<R> one = mk<R>(1, 0), zero = mk<R>(0, 0);
+	cx<double> r0 = mk(0.0, 0.0), rden = mk(0.0, 0.0);
+	if(col) {
+		const cx<double>* ls = lsc + (((size_t)g * 2 + c) * Nx + ix) * 2;
+		r0 = ls[0];
+		rden = ls[1];
+	}
+	const Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
+	const cx<R>* f0 = src + (size_t)s0 * 2 * N;
+	auto va = [&](int j, int i) { return (size_t)(s0 + j) * 2 * N + (size_t)c * N + (size_t)ix + (size_t)Nx * i; };
+	cx<R> A[KS], B[KS];
+#pragma unroll
+	for(int j = 0; j < KS; j++) { A[j] = one; B[j] = zero; }
+	if(col) {
+		for(int i = i0; i < i1; i++) {
+			size_t q = (size_t)ix + (size_t)Nx * i;
+			cx<R> a = Fc[F_A * plane + q], rb = Fc[F_RB * plane + q];
+			cx<R> r[KS];
+			composite_m<R, KIND, KS>(st, c, ix, i, f0, r);
+#pragma unroll
+			for(int j = 0; j < KS; j++) {
+				cx<R> b = r[j] * rb;
+				vbuf[va(j, i)] = b;
+				B[j] = a * B[j] + b;
+				A[j] = a * A[j];
+			}
+		}
+	}
+#pragma unroll
+	for(int j = 0; j < KS; j++) { sA[j * SZ + w * 32 + lane] = A[j]; sB[j * SZ + w * 32 + lane] = B[j]; }
+	__syncthreads();
+	if(w == 0) {
+		for(int j = 0; j < KS; j++) {
+			cx<R> D = zero;
+			for(int ww = 0; ww < WY; ww++) {
+				sD[j * SZ + ww * 32 + lane] = D;
+				D = sA[j * SZ + ww * 32 + lane] * D + sB[j * SZ + ww * 32 + lane];
+			}
+		}
+	}
+	__syncthreads();
+	cx<R> d[KS], acc[KS];
+#pragma unroll
+	for(int j = 0; j < KS; j++) { d[j] = sD[j * SZ + w * 32 + lane]; acc[j] = zero; }
+	if(col) {
+		for(int i = i0; i < i1; i++) {
+			size_t q = (size_t)ix + (size_t)Nx * i;
+			cx<R> a = Fc[F_A * plane + q], wv = Fc[F_W * plane + q];
+#pragma unroll
+			for(int j = 0; j < KS; j++) {
+				d[j] = a * d[j] + vbuf[va(j, i)];
+				vbuf[va(j, i)] = d[j];
+				acc[j] += wv * d[j];
+				if(i == n_unk - 1) sL[j * 32 + lane] = d[j];
+			}
+		}
+	}
+#pragma unroll
+	for(int j = 0; j < KS; j++) sP[j * SZ + w * 32 + lane] = acc[j];
+	__syncthreads();
+	if(w == 0) {
+		for(int j = 0; j < KS; j++) {
+			cx<R> tot = zero;
+			for(int ww = 0; ww < WY; ww++) tot += sP[j * SZ + ww * 32 + lane];
+			sF[j * 32 + lane] = cvt<R>((cvt<double>(tot) - r0 * cvt<double>(sL[j * 32 + lane])) * rden);
+		}
+	}
+#pragma unroll
+	for(int j = 0; j < KS; j++) { A[j] = one; B[j] = zero; }
+	if(col) {
+		for(int i = i1 - 1; i >= i0; i--) {
+			cx<R> cc = Fc[F_C * plane + (size_t)ix + (size_t)Nx * i];
+#pragma unroll
+			for(int j = 0; j < KS; j++) { B[j] = cc * B[j] + vbuf[va(j, i)]; A[j] = cc * A[j]; }
+		}
+	}
+#pragma unroll
+	for(int j = 0; j < KS; j++) { sA[j * SZ + w * 32 + lane] = A[j]; sB[j * SZ + w * 32 + lane] = B[j]; }
+	__syncthreads();
+	if(w == 0) {
+		for(int j = 0; j < KS; j++) {
+			cx<R> D = zero;
+			for(int ww = WY - 1; ww >= 0; ww--) {
+				sD[j * SZ + ww * 32 + lane] = D;
+				D = sA[j * SZ + ww * 32 + lane] * D + sB[j * SZ + ww * 32 + lane];
+			}
+		}
+	}
+	__syncthreads();
+	cx<R> fr[KS];
+#pragma unroll
+	for(int j = 0; j < KS; j++) { fr[j] = sF[j * 32 + lane]; d[j] = sD[j * SZ + w * 32 + lane]; }
+	if(col) {
+		for(int i = i1 - 1; i >= i0; i--) {
+			size_t q = (size_t)ix + (size_t)Nx * i;
+			cx<R> cc = Fc[F_C * plane + q], cr = Fc[F_COR * plane + q];
+#pragma unroll
+			for(int j = 0; j < KS; j++) {
+				d[j] = cc * d[j] + vbuf[va(j, i)];
 				cx<R> x = d[j] - fr[j] * cr;
 				size_t off = (size_t)(s0 + j) * 2 * N + (size_t)c * N;
 				if(dst) dst[off + q] = x;

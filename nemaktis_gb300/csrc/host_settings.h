@@ -77,6 +77,7 @@ struct BackendSettings {
 	std::vector<double> wavelengths;
 	std::vector<std::pair<double, double>> q;
 	bool bulk_activate = false, screen_activate = true;
+	std::string bulk_base_name;
 	std::vector<double> iso_thick, iso_index;
 	double z_foc = 0, NA = 0;
 	// Evaluated per wavelength (PhysicsCoefficients::get_*).
@@ -156,7 +157,7 @@ inline BackendSettings parse_settings(const std::string& json_str) {
 	Section post(j, "Postprocessor settings");
 	Section bulk(*post.node, "Bulk output");
 	s.bulk_activate = bulk.boolean("Activate");
-	bulk.str("Base name");
+	s.bulk_base_name = bulk.str("Base name");
 	Section scr(*post.node, "Screen output");
 	s.screen_activate = scr.boolean("Activate");
 	scr.str("Base name");

@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <deque>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -24,6 +25,7 @@
 #include "bpm_kernels.cuh"
 #include "fft_kernels.cuh"
 #include "plan_iface.h"
+#include "vti_writer.h"
 #include "host_settings.h"
 #include "solve_dispatch.cuh"
 
@@ -78,9 +80,40 @@ struct SampleHost {
 	bool any_shift = false, any_zero_q = false;
 	int index = 0;
 	ScreenParams sp;
+	// bulk output (fields of every plane): [slot][re, im][iz * N + p][Ex, Ey, 0]
+	bool bulk = false;
+	std::vector<double> bulk_data;
+	cx<double>* hstage = nullptr;  // pinned host staging of one pass's plane
 	// device
-	DevBuf dir, dmask, dwts, F, E0, gpsd, shiftd, partial, wl, nout, qv;
+	DevBuf dir, dmask, dwts, F, E0, gpsd, shiftd, partial, wl, nout, qv, bstage;
+	~SampleHost() { if(hstage) cudaFreeHost(hstage); }
 };
+
+// One recorded bulk-output copy: the host function scatters the staged plane into the
+// sample's bulk arrays.
+struct BulkRec {
+	SampleHost* h;
+	int slot0, nsl, iz;
+};
+
+static void CUDART_CB bulk_host_fn(void* p) {
+	const BulkRec& r = *static_cast<const BulkRec*>(p);
+	SampleHost& h = *r.h;
+	const size_t N = (size_t)h.geom.N, Nz = (size_t)h.geom.Nz;
+	for(int s = 0; s < r.nsl; s++) {
+		size_t slot = (size_t)r.slot0 + s;
+		double* re = h.bulk_data.data() + slot * 2 * 3 * N * Nz;
+		double* im = re + 3 * N * Nz;
+		for(int c = 0; c < 2; c++) {
+			const cx<double>* src = h.hstage + ((size_t)s * 2 + c) * N;
+			for(size_t p = 0; p < N; p++) {
+				size_t o = 3 * ((size_t)r.iz * N + p);
+				re[o + c] = src[p].x;
+				im[o + c] = src[p].y;
+			}
+		}
+	}
+}
 
 // Nearest-index divisions used by the shift operator are computed on the device from nref;
 // this kernel restates the SimpleShiftOperator constructor (SimpleShiftOperator.cpp:3-50).
@@ -186,6 +219,7 @@ struct Plan : PlanBase {
 	double last_slab_ms = 0;
 	size_t smem_limit = 0;
 	bool shift_fused = true;  // one-pass transition kernel (NBPM_SHIFT_FUSED=0: four passes)
+	bool factor_seq = false;  // one thread per line factorisation (NBPM_FACTOR_SEQ=1)
 	// line-solve configuration per sample (chunk sizes of the parallel kernels; 0 = sequential)
 	// x: k_solve_xc with KSx slots per warp, or (NBPM_XMODE=1) the group-cooperative k_solve_xg
 	// (all slots of a wavelength per block) when its shared memory fits. y: ymode 0 = fused
@@ -194,6 +228,9 @@ struct Plan : PlanBase {
 	struct SolveCfg {
 		int Mx = 0, My = 0, WY = 0, KSx = 1, KSy = 1;
 		bool xg = false;
+		bool ys = false;  // y-lines too long for k_solve_yc: k_solve_ys with scratch-held chunks
+		bool xs = false;  // x-lines with long chunks: k_solve_xs with the chunks in shared memory
+		int WPLx = 1;     // warps per x-line (k_solve_xw when > 1: 32*WPLx chunks of Mx points)
 		int ymode = 0;
 		size_t plane_x = 0, plane_y = 0, smem_xg = 0;
 	};
@@ -298,6 +335,10 @@ struct Plan : PlanBase {
 			sp.z_foc = zf;
 			for(int l = 0; l < 8; l++) sp.thick[l] = l < sp.n_iso ? s.iso_thick[l] : 0;
 			for(int l = 0; l < 9; l++) sp.index[l] = l < sp.n_iso ? s.iso_index[l] : 1;
+			if(s.bulk_activate) {
+				h->bulk = true;
+				h->bulk_data.assign((size_t)h->slots * 2 * 3 * (size_t)s.Nx * s.Ny * s.Nz, 0.0);
+			}
 			h->index = (int)S.size();
 			S.push_back(std::move(h));
 		}
@@ -335,11 +376,14 @@ struct Plan : PlanBase {
 		CK(cudaFuncSetAttribute(k_fft_lines<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit));
 		CK(cudaFuncSetAttribute(k_shift_fused<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit));
 		if(const char* e = std::getenv("NBPM_SHIFT_FUSED")) shift_fused = std::atoi(e) != 0;
+		if(const char* e = std::getenv("NBPM_FACTOR_SEQ")) factor_seq = std::atoi(e) != 0;
 		if(sizeof(R) == sizeof(float)) {
 			set_solve_smem_x_f32((int)smem_limit); set_solve_smem_y_f32((int)smem_limit); set_solve_smem_xg_f32((int)smem_limit);
+			set_solve_smem_xs_f32((int)smem_limit); set_solve_smem_xw_f32((int)smem_limit);
 		}
 		else {
 			set_solve_smem_x_f64((int)smem_limit); set_solve_smem_y_f64((int)smem_limit); set_solve_smem_xg_f64((int)smem_limit);
+			set_solve_smem_xs_f64((int)smem_limit); set_solve_smem_xw_f64((int)smem_limit);
 		}
 		CK(cudaGetLastError());
 		allocate();
@@ -369,6 +413,10 @@ struct Plan : PlanBase {
 			int ux = h.s.Nx - 1, uy = h.s.Ny - 1;
 			if(h.s.Nx > 3) {
 				for(int M = 2; M <= 32; M *= 2) if(32 * M >= ux) { sc.Mx = M; break; }
+				// long lines: several warps per line with 8-point chunks (k_solve_xw), unless
+				// NBPM_XW=0
+				const char* exw = std::getenv("NBPM_XW");
+				if(ux > 256 && ux <= 8 * 256 && !(exw && std::atoi(exw) == 0)) { sc.Mx = 8; sc.WPLx = (ux + 255) / 256; }
 			}
 			if(h.s.Ny > 3) {
 				// block of 32 columns x WY <= 16 warps (<= 512 threads, <= 128 registers)
@@ -390,9 +438,23 @@ struct Plan : PlanBase {
 			};
 			if(sc.Mx) { sc.KSx = pick_ks(sc.Mx, kmx); if(!sc.KSx) sc.Mx = 0; }
 			if(sc.My) { sc.KSy = pick_ks(sc.My, kmy); if(!sc.KSy) { sc.My = 0; sc.WY = 0; } }
+			if(const char* e = std::getenv("NBPM_YS")) if(std::atoi(e) == 1 && h.s.Ny > 3) { sc.My = 0; sc.WY = 0; }
+			if(sc.WPLx == 1 && (sc.Mx >= 32 || (sc.Mx && std::getenv("NBPM_XS") && std::atoi(std::getenv("NBPM_XS")) == 1))) {
+				sc.xs = true;
+				sc.KSx = 1;
+				for(int ks : {4, 2}) if(ks <= kmx && h.spg % ks == 0 && (size_t)4 * ks * 32 * (sc.Mx + 1) * sizeof(cx<R>) <= 100 * 1024) { sc.KSx = ks; break; }
+			}
+			// y-lines beyond the chunked kernel's reach (Ny > 513) use the one-thread-per-column
+			// solve, measured faster on GB300 than k_solve_ys for 1024-row meshes; NBPM_YS=1
+			// selects k_solve_ys for every mesh.
+			if(h.s.Ny > 3 && sc.My == 0 && std::getenv("NBPM_YS") && std::atoi(std::getenv("NBPM_YS")) == 1) {
+				sc.ys = true;
+				sc.KSy = 1;
+				for(int ks : {4, 2}) if(ks <= kmy && h.spg % ks == 0) { sc.KSy = ks; break; }
+			}
 			if(opt.verbose)
 				std::printf("line solves: x M=%d KS=%d, y M=%d WY=%d KS=%d\n", sc.Mx, sc.KSx, sc.My, sc.WY, sc.KSy);
-			sc.plane_x = sc.Mx ? std::max(N, (size_t)h.s.Ny * 32 * sc.Mx) : N;
+			sc.plane_x = sc.Mx ? std::max(N, (size_t)h.s.Ny * 32 * sc.WPLx * sc.Mx) : N;
 			if(sc.Mx) {
 				sc.smem_xg = ((size_t)h.spg * 32 * (sc.Mx + 1) + (size_t)NFAC * 32 * sc.Mx) * sizeof(cx<R>);
 				sc.xg = false;  // measured slower than k_solve_xc on the 256x256 batched workload
@@ -421,6 +483,12 @@ struct Plan : PlanBase {
 			dalloc(h.wl, sizeof(double) * h.G);
 			dalloc(h.nout, sizeof(double) * h.G);
 			dalloc(h.qv, sizeof(double) * 2 * h.Nq);
+			if(h.bulk) {
+				size_t nb = sizeof(cx<double>) * (size_t)ng * h.spg * 2 * N;
+				dalloc(h.bstage, nb);
+				dev_bytes += h.bstage.bytes;
+				if(!dry && !h.hstage) CK(cudaMallocHost(reinterpret_cast<void**>(&h.hstage), nb));
+			}
 			dev_bytes += h.dir.bytes + h.dmask.bytes + h.dwts.bytes + h.F.bytes + h.E0.bytes;
 			if(dry) dev_bytes += sizeof(cx<R>) * (size_t)(h.s.Nx + h.s.Ny);
 			else { twiddles(h.s.Nx); twiddles(h.s.Ny); }
@@ -428,7 +496,7 @@ struct Plan : PlanBase {
 		dalloc(T, sizeof(cx<R>) * maxT);
 		dalloc(T2, sizeof(cx<R>) * maxT);
 		bool need_t3 = false;
-		for(auto& c : scfg) need_t3 |= (c.My > 0 && c.ymode == 1);
+		for(auto& c : scfg) need_t3 |= (c.My > 0 && c.ymode == 1) || c.ys;
 		if(need_t3) dalloc(T3, sizeof(cx<R>) * maxT);
 		dalloc(Qring, sizeof(R) * maxQ);
 		dalloc(coef, sizeof(cx<R>) * maxC);
@@ -487,6 +555,13 @@ struct Plan : PlanBase {
 			}
 		}
 		CK(cudaStreamSynchronize(stream));
+		host_finish();
+	}
+
+	// Host-side outputs of a finished run: the bulk-output files.
+	void host_finish() override {
+		for(auto& hp : S)
+			if(hp->bulk) write_bulk(*hp);
 	}
 
 	// ---- launch helpers (count launches while recording) ----
@@ -642,10 +717,24 @@ struct Plan : PlanBase {
 			if(iz >= 2) CK(cudaStreamWaitEvent(streamB, eAdi[iz & 1], 0));
 			int lx_n = ng * 2 * Ny, ly_n = ng * 2 * Nx;
 			const double fb = (double)N * ng * 2 * (3 * sc + NFAC * sc + 4 * sc);
-			launch("factor", 2 * fb, [&] {
-				k_factor<R><<<(lx_n + ly_n + 63) / 64, 64, 0, cs>>>(Gm, ng, scf.Mx, ps.Dg, fx, scf.plane_x, lx, fy,
-					scf.plane_y, ly, scr.as<cx<R>>());
-			});
+			if(factor_seq) {
+				launch("factor", 2 * fb, [&] {
+					k_factor<R><<<(lx_n + ly_n + 63) / 64, 64, 0, cs>>>(Gm, ng, scf.Mx, 32 * scf.WPLx, ps.Dg, fx, scf.plane_x, lx, fy,
+						scf.plane_y, ly, scr.as<cx<R>>());
+				});
+			}
+			else {
+				const int LT = 4, WF = 8;
+				launch("factor_x", fb, [&] {
+					k_factor_chunked<R, 0><<<dim3((unsigned)((Ny + LT - 1) / LT), (unsigned)(ng * 2)), dim3(32, LT), 0, cs>>>(
+						Gm, ng, scf.Mx, 32 * scf.WPLx, 1, ps.Dg, fx, scf.plane_x, lx);
+				});
+				size_t smem = (size_t)WF * 32 * 8 * sizeof(cx<R>) + 64 * sizeof(cx<R>);
+				launch("factor_y", fb, [&] {
+					k_factor_chunked<R, 1><<<dim3((unsigned)((Nx + 31) / 32), (unsigned)(ng * 2)), dim3(32, WF), smem, cs>>>(
+						Gm, ng, 0, 32, WF, ps.Dg, fy, scf.plane_y, ly);
+				});
+			}
 			CK(cudaEventRecord(eFac, streamB));
 			// ---- main stream ----
 			cs = stream;
@@ -656,6 +745,7 @@ struct Plan : PlanBase {
 			CK(cudaStreamWaitEvent(stream, eFac, 0));
 			fx_cur = fx; fy_cur = fy; lx_cur = lx; ly_cur = ly;
 			rec_adi(h, Gm, slot0, nsl, ng, Nw, C, ps.Fp, ps.Tb, ps.T2b, xsrc);
+			rec_bulk(h, ps, iz + 1, C);
 			CK(cudaEventRecord(eAdi[iz & 1], stream));
 			ps.Cprev = C;
 		}
@@ -694,10 +784,69 @@ struct Plan : PlanBase {
 		fft2(h, F, nplanes, +1);
 	}
 
+	// Bulk output of plane iz of a pass (BPMIteration.cpp:111-121, 153-168). The entrance
+	// plane (C null) is the current field; plane iz >= 1 is the field after the slab's
+	// trailing phase and shift, which the slab loop defers to the next transition, so it is
+	// formed out of place here.
+	std::deque<BulkRec> bulk_recs;
+	void rec_bulk(SampleHost& h, PassState& ps, int iz, const cx<R>* C) {
+		if(!h.bulk) return;
+		const Geom Gm = h.geom;
+		const int N = Gm.N;
+		const size_t n = (size_t)ps.nsl * 2 * N;
+		const double sc = sizeof(cx<R>);
+		cx<double>* st = h.bstage.as<cx<double>>();
+		const cx<R>* src = ps.Fp;
+		cs = stream;
+		if(C) {
+			cx<R>* o = sizeof(R) == sizeof(double) ? reinterpret_cast<cx<R>*>(st) : ps.T2b;
+			dim3 grid((unsigned)((Gm.Nx + SHT - 1) / SHT), (unsigned)((Gm.Ny + SHT - 1) / SHT), (unsigned)ps.nsl);
+			size_t smem = (size_t)4 * (SHT + 6) * (SHT + 6) * sizeof(cx<R>);
+			launch("bulk_plane", (double)n * 2 * sc, [&] {
+				k_shift_fused<R><<<grid, 256, smem, cs>>>(Gm, ps.slot0, h.shiftd.as<ShiftParams>(), C, nullptr, 1, ps.Fp, o);
+			});
+			src = o;
+		}
+		if(reinterpret_cast<const void*>(src) != reinterpret_cast<const void*>(st)) {
+			launch("bulk_widen", (double)n * (sc + 16), [&] {
+				k_widen<R><<<(unsigned)((n + 255) / 256), 256, 0, cs>>>(n, src, st);
+			});
+		}
+		CK(cudaMemcpyAsync(h.hstage, st, n * sizeof(cx<double>), cudaMemcpyDeviceToHost, cs));
+		bulk_recs.push_back(BulkRec{&h, ps.slot0, ps.nsl, iz});
+		CK(cudaLaunchHostFunc(cs, bulk_host_fn, &bulk_recs.back()));
+	}
+
+	void write_bulk(SampleHost& h) {
+		const auto& s = h.s;
+		const size_t NV = (size_t)s.Nx * s.Ny * s.Nz;
+		std::vector<VtiArray> fd, pd;
+		std::vector<double> qx, qy;
+		for(auto& q : s.q) { qx.push_back(q.first); qy.push_back(q.second); }
+		fd.push_back({"lambda", 1, s.wavelengths.data(), s.wavelengths.size()});
+		fd.push_back({"qx", 1, qx.data(), qx.size()});
+		fd.push_back({"qy", 1, qy.data(), qy.size()});
+		const char* pols[2] = {"inputX_", "inputY_"};
+		for(int w = 0; w < h.G; w++)
+			for(int q = 0; q < h.Nq; q++)
+				for(int pol = 0; pol < 2; pol++) {
+					size_t slot = (size_t)pol + 2 * ((size_t)q + (size_t)h.Nq * w);
+					const double* re = h.bulk_data.data() + slot * 2 * 3 * NV;
+					std::string tag = std::string(pols[pol]) + std::to_string(q) + "_" + std::to_string(w);
+					pd.push_back({"E_real_" + tag, 3, re, NV});
+					pd.push_back({"E_imag_" + tag, 3, re + 3 * NV, NV});
+				}
+		std::string path = bulk_output_path(s.results_folder, s.bulk_base_name);
+		if(opt.verbose) std::printf("Exporting bulk optical field to %s\n", path.c_str());
+		std::string err = write_vti(path, s.Nx, s.Ny, s.Nz, s.dx, s.dy, s.dz, fd, pd);
+		if(!err.empty()) throw BackendError(E_INTERNAL, "bulk output: " + err);
+	}
+
 	void record_sample(SampleHost& h) {
 		rec_prologue(h);
 		for(int ga = 0; ga < h.G; ga += gpp(h)) {
 			PassState ps = rec_pass_begin(h, ga);
+			rec_bulk(h, ps, 0, nullptr);
 			rec_pass_slabs(h, ps, h.geom.Nz - 1);
 			rec_pass_end(h, ps);
 		}
@@ -794,6 +943,26 @@ struct Plan : PlanBase {
 			const int LT = 4;
 			L.KS = sc.KSx;
 			int nch = h.spg / L.KS;
+			if(sc.WPLx > 1) {
+				L.grid = dim3((unsigned)Gm.Ny, (unsigned)(ng * nch * 2));
+				L.block = dim3(32 * sc.WPLx);
+				L.smem = ((size_t)L.KS * 32 * sc.WPLx * (L.M + 1) + 4 * L.KS * sc.WPLx + 2 * L.KS) * sizeof(cx<R>);
+				launch(wood ? "wood_solve_x" : "expl_solve_x", bytes, [&] {
+					if(!launch_solve_xw<R>(L, Gm, slot0, nch, C, fx_cur, sc.plane_x, lx_cur, src, dst, acc_in, acc_out))
+						throw BackendError(E_INTERNAL, "no x-solve instance");
+				});
+				return;
+			}
+			if(sc.xs) {
+				L.grid = dim3((unsigned)((Gm.Ny + LT - 1) / LT), (unsigned)(ng * nch * 2));
+				L.block = dim3(32 * LT);
+				L.smem = (size_t)LT * L.KS * 32 * (L.M + 1) * sizeof(cx<R>);
+				launch(wood ? "wood_solve_x" : "expl_solve_x", bytes, [&] {
+					if(!launch_solve_xs<R>(L, Gm, slot0, nch, C, fx_cur, sc.plane_x, lx_cur, src, dst, acc_in, acc_out))
+						throw BackendError(E_INTERNAL, "no x-solve instance");
+				});
+				return;
+			}
 			L.grid = dim3((unsigned)((Gm.Ny + LT - 1) / LT), (unsigned)(ng * nch * 2));
 			L.block = dim3(32 * LT);
 			L.smem = (size_t)LT * L.KS * 32 * (L.M + 1) * sizeof(cx<R>);
@@ -814,6 +983,20 @@ struct Plan : PlanBase {
 					else k_rhs<R, ST_EXPL_X><<<gr, 256, 0, cs>>>(Gm, slot0, C, src, R3);
 				});
 				rsrc = R3;
+			}
+			if(sc.ys) {
+				const int WS = 8;
+				L.M = 0; L.KS = sc.KSy; L.kind = wood ? ST_WOOD_Y : ST_EXPL_X;
+				int nch = h.spg / L.KS;
+				L.grid = dim3((unsigned)((Gm.Nx + 31) / 32), (unsigned)(ng * nch * 2));
+				L.block = dim3(32, WS);
+				L.smem = (size_t)(4 * L.KS * WS * 32 + 2 * L.KS * 32) * sizeof(cx<R>);
+				launch(wood ? "wood_solve_y" : "expl_solve_y", bytes + fp * 2, [&] {
+					if(!launch_solve_ys<R>(L, Gm, slot0, nch, C, fy_cur, sc.plane_y, ly_cur, src, dst, acc_in, acc_out,
+							T3.as<cx<R>>()))
+						throw BackendError(E_INTERNAL, "no y-solve instance");
+				});
+				return;
 			}
 			L.M = sc.My; L.KS = sc.KSy; L.kind = sc.ymode == 1 ? ST_GIVEN : (wood ? ST_WOOD_Y : ST_EXPL_X);
 			int nch = h.spg / L.KS;
@@ -837,7 +1020,7 @@ struct Plan : PlanBase {
 		const double fp = (double)N * nsl;
 		const SolveCfg& cfg = scfg[h.index];
 		for(int dirn = 0; dirn < 2; dirn++) {
-			bool fused = (dirn == 0 ? cfg.Mx : cfg.My) > 0;
+			bool fused = dirn == 0 ? cfg.Mx > 0 : (cfg.My > 0 || cfg.ys);
 			if(fused) {
 				// t0 = solve(f + mu R f) written to T; Woodbury: t_k = solve(mu R' t_{k-1}),
 				// F = t0 + t1 + ... accumulated by the solves (the last t_k is not stored).
@@ -964,6 +1147,7 @@ struct Plan : PlanBase {
 		cs = stream;
 		rec_prologue(*S[0]);
 		sps = rec_pass_begin(*S[0], 0);
+		rec_bulk(*S[0], sps, 0, nullptr);
 	}
 	int step_advance(int nslabs) override {
 		CK(cudaSetDevice(opt.device));

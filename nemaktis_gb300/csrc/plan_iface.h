@@ -28,6 +28,8 @@ struct PlanBase {
 	virtual void upload() = 0;
 	virtual void execute(nbpm_timing* t) = 0;
 	virtual void download() = 0;
+	// Host-side outputs once the run has finished (bulk-output files); download() calls it.
+	virtual void host_finish() = 0;
 	virtual bool fields_view(int sample, PlanFieldsView& v) const = 0;
 	// Resumable execution of a one-sample plan with every wavelength in one pass (serving):
 	// step_begin records the entrance, step_advance up to n more slabs (returns the slabs

@@ -181,7 +181,10 @@ struct Server {
 				if(bad) continue;
 				try {
 					r->plan->sync();
-					if(r->finishing && r->plan->step_done()) done.push_back(r);
+					if(r->finishing && r->plan->step_done()) {
+						r->plan->host_finish();
+						done.push_back(r);
+					}
 				}
 				catch(BackendError& e) { failed.push_back({r, {e.code, e.what()}}); }
 			}

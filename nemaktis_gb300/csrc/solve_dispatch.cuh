@@ -25,6 +25,19 @@ bool launch_solve_yc(const SolveLaunch& L, Geom G, int slot0, int nch, const cx<
 template <typename R>
 bool launch_solve_xg(const SolveLaunch& L, Geom G, int slot0, const cx<R>* coef, const cx<R>* fac, size_t plane,
 	const cx<double>* lsc, const cx<R>* src, cx<R>* dst, const cx<R>* ai, cx<R>* ao);
+template <typename R>
+bool launch_solve_xw(const SolveLaunch& L, Geom G, int slot0, int nch, const cx<R>* coef, const cx<R>* fac,
+	size_t plane, const cx<double>* lsc, const cx<R>* src, cx<R>* dst, const cx<R>* ai, cx<R>* ao);
+void set_solve_smem_xw_f32(int bytes);
+void set_solve_smem_xw_f64(int bytes);
+template <typename R>
+bool launch_solve_xs(const SolveLaunch& L, Geom G, int slot0, int nch, const cx<R>* coef, const cx<R>* fac,
+	size_t plane, const cx<double>* lsc, const cx<R>* src, cx<R>* dst, const cx<R>* ai, cx<R>* ao);
+void set_solve_smem_xs_f32(int bytes);
+void set_solve_smem_xs_f64(int bytes);
+template <typename R>
+bool launch_solve_ys(const SolveLaunch& L, Geom G, int slot0, int nch, const cx<R>* coef, const cx<R>* fac,
+	size_t plane, const cx<double>* lsc, const cx<R>* src, cx<R>* dst, const cx<R>* ai, cx<R>* ao, cx<R>* vbuf);
 void set_solve_smem_xg_f32(int bytes);
 void set_solve_smem_xg_f64(int bytes);
 void set_solve_smem_x_f32(int bytes);

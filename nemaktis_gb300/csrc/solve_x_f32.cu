@@ -54,4 +54,48 @@ void set_solve_smem_xg_f32(int bytes) {
 	NBPM_XGA(2, ST_WOOD_X) NBPM_XGA(4, ST_WOOD_X) NBPM_XGA(8, ST_WOOD_X) NBPM_XGA(16, ST_WOOD_X) NBPM_XGA(32, ST_WOOD_X)
 }
 
+#define NBPM_XS(KK, KD) \
+	if(L.KS == KK && L.kind == KD) { \
+		k_solve_xs<float, KD, KK><<<L.grid, L.block, L.smem, L.stream>>>(G, slot0, nch, L.M, coef, fac, plane, lsc, \
+			src, dst, ai, ao); \
+		return true; \
+	}
+
+template <>
+bool launch_solve_xs<float>(const SolveLaunch& L, Geom G, int slot0, int nch, const cx<float>* coef,
+		const cx<float>* fac, size_t plane, const cx<double>* lsc, const cx<float>* src, cx<float>* dst,
+		const cx<float>* ai, cx<float>* ao) {
+	NBPM_XS(1, ST_EXPL_Y) NBPM_XS(2, ST_EXPL_Y) NBPM_XS(4, ST_EXPL_Y)
+	NBPM_XS(1, ST_WOOD_X) NBPM_XS(2, ST_WOOD_X) NBPM_XS(4, ST_WOOD_X)
+	return false;
+}
+
+void set_solve_smem_xs_f32(int bytes) {
+#define NBPM_XSA(KK, KD) cudaFuncSetAttribute(k_solve_xs<float, KD, KK>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+	NBPM_XSA(1, ST_EXPL_Y) NBPM_XSA(2, ST_EXPL_Y) NBPM_XSA(4, ST_EXPL_Y)
+	NBPM_XSA(1, ST_WOOD_X) NBPM_XSA(2, ST_WOOD_X) NBPM_XSA(4, ST_WOOD_X)
+}
+
+#define NBPM_XW(KK, KD) \
+	if(L.M == 8 && L.KS == KK && L.kind == KD) { \
+		k_solve_xw<float, 8, KD, KK><<<L.grid, L.block, L.smem, L.stream>>>(G, slot0, nch, coef, fac, plane, lsc, \
+			src, dst, ai, ao); \
+		return true; \
+	}
+
+template <>
+bool launch_solve_xw<float>(const SolveLaunch& L, Geom G, int slot0, int nch, const cx<float>* coef,
+		const cx<float>* fac, size_t plane, const cx<double>* lsc, const cx<float>* src, cx<float>* dst,
+		const cx<float>* ai, cx<float>* ao) {
+	NBPM_XW(1, ST_EXPL_Y) NBPM_XW(2, ST_EXPL_Y) NBPM_XW(4, ST_EXPL_Y)
+	NBPM_XW(1, ST_WOOD_X) NBPM_XW(2, ST_WOOD_X) NBPM_XW(4, ST_WOOD_X)
+	return false;
+}
+
+void set_solve_smem_xw_f32(int bytes) {
+#define NBPM_XWA(KK, KD) cudaFuncSetAttribute(k_solve_xw<float, 8, KD, KK>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+	NBPM_XWA(1, ST_EXPL_Y) NBPM_XWA(2, ST_EXPL_Y) NBPM_XWA(4, ST_EXPL_Y)
+	NBPM_XWA(1, ST_WOOD_X) NBPM_XWA(2, ST_WOOD_X) NBPM_XWA(4, ST_WOOD_X)
+}
+
 }  // namespace nbpm

@@ -35,4 +35,20 @@ void set_solve_smem_y_f32(int bytes) {
 	NBPM_YA_PAIRS(ST_GIVEN)
 }
 
+#define NBPM_YS(KK, KD) \
+	if(L.KS == KK && L.kind == KD) { \
+		k_solve_ys<float, KD, KK><<<L.grid, L.block, L.smem, L.stream>>>(G, slot0, nch, coef, fac, plane, lsc, src, \
+			dst, ai, ao, vbuf); \
+		return true; \
+	}
+
+template <>
+bool launch_solve_ys<float>(const SolveLaunch& L, Geom G, int slot0, int nch, const cx<float>* coef,
+		const cx<float>* fac, size_t plane, const cx<double>* lsc, const cx<float>* src, cx<float>* dst,
+		const cx<float>* ai, cx<float>* ao, cx<float>* vbuf) {
+	NBPM_YS(1, ST_EXPL_X) NBPM_YS(2, ST_EXPL_X) NBPM_YS(4, ST_EXPL_X)
+	NBPM_YS(1, ST_WOOD_Y) NBPM_YS(2, ST_WOOD_Y) NBPM_YS(4, ST_WOOD_Y)
+	return false;
+}
+
 }  // namespace nbpm

@@ -35,4 +35,20 @@ void set_solve_smem_y_f64(int bytes) {
 	NBPM_YA_PAIRS(ST_GIVEN)
 }
 
+#define NBPM_YS(KK, KD) \
+	if(L.KS == KK && L.kind == KD) { \
+		k_solve_ys<double, KD, KK><<<L.grid, L.block, L.smem, L.stream>>>(G, slot0, nch, coef, fac, plane, lsc, src, \
+			dst, ai, ao, vbuf); \
+		return true; \
+	}
+
+template <>
+bool launch_solve_ys<double>(const SolveLaunch& L, Geom G, int slot0, int nch, const cx<double>* coef,
+		const cx<double>* fac, size_t plane, const cx<double>* lsc, const cx<double>* src, cx<double>* dst,
+		const cx<double>* ai, cx<double>* ao, cx<double>* vbuf) {
+	NBPM_YS(1, ST_EXPL_X) NBPM_YS(2, ST_EXPL_X) NBPM_YS(4, ST_EXPL_X)
+	NBPM_YS(1, ST_WOOD_Y) NBPM_YS(2, ST_WOOD_Y) NBPM_YS(4, ST_WOOD_Y)
+	return false;
+}
+
 }  // namespace nbpm

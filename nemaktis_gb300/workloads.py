@@ -25,12 +25,13 @@ except Exception:  # pragma: no cover
 
 def settings_json(dims, spacings, wavelengths, wavevectors=(0.0, 0.0), no="1.5", ne="1.7", nhost="1.5",
                   nin="1", nout="1", ne_imag="0", n_woodbury=2, NA=1.0, beam="UniformBeam",
-                  lc_type="Director", iso_thick=(), iso_index=(), z_shift=0.0):
+                  lc_type="Director", iso_thick=(), iso_index=(), z_shift=0.0, bulk_name=None,
+                  results_folder=""):
     """JSON settings string in the layout of light_propagator.py:152-186."""
     wv = [float(v) for v in np.asarray(wavevectors, float).ravel()]
     return json.dumps({
         "Algorithm settings": {
-            "General": {"LC field type": lc_type, "Results folder name": ""},
+            "General": {"LC field type": lc_type, "Results folder name": results_folder},
             "Beam propagation": {"N Woodbury steps": int(n_woodbury), "Number of substeps per slab": 1}},
         "Physics settings": {
             "Initial conditions": {
@@ -42,7 +43,7 @@ def settings_json(dims, spacings, wavelengths, wavevectors=(0.0, 0.0), no="1.5",
                 "nin": str(nin), "nout": str(nout),
                 "Wavelengths": [float(w) for w in wavelengths], "Wavevectors": wv}},
         "Postprocessor settings": {
-            "Bulk output": {"Activate": False, "Base name": ""},
+            "Bulk output": {"Activate": bulk_name is not None, "Base name": bulk_name or ""},
             "Screen output": {
                 "Activate": True, "Base name": "",
                 "Isotropic layer thicknesses": [float(t) for t in iso_thick],

@@ -63,6 +63,9 @@ def _load():
         _lib.oracle_run.restype = ctypes.c_int
         _lib.oracle_run.argtypes = [ctypes.POINTER(_Params), ctypes.c_void_p, ctypes.c_void_p,
                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        _lib.oracle_run_bulk.restype = ctypes.c_int
+        _lib.oracle_run_bulk.argtypes = [ctypes.POINTER(_Params), ctypes.c_void_p, ctypes.c_void_p,
+                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
         _lib.oracle_fft1d.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
         _lib.oracle_num_threads.restype = ctypes.c_int
     return _lib
@@ -135,7 +138,7 @@ def mask_interp_weights(mask_vals, formula, dims, spacings):
     return m.astype(np.uint8), w
 
 
-def _run(json_str, lc_vals, E, mask_vals=None, mask_formula="", stages=3):
+def _run(json_str, lc_vals, E, mask_vals=None, mask_formula="", stages=3, bulk=None):
     s = _settings.parse(json_str)
     Nx, Ny, Nz = s["dims"]
     nv = Nx * Ny * Nz
@@ -169,17 +172,22 @@ def _run(json_str, lc_vals, E, mask_vals=None, mask_formula="", stages=3):
                 Nq, _dptr(q), len(s["iso_thick"]), _dptr(it), _dptr(ii),
                 s["z_foc"], s["NA"], s["nout_06"])
     lib = _load()
-    rc = lib.oracle_run(ctypes.byref(p), lc.ctypes.data,
-                        None if mask is None else mask.ctypes.data, w.ctypes.data,
-                        E.ctypes.data, stages)
+    if bulk is not None:
+        if not (bulk.dtype == np.complex128 and bulk.flags.c_contiguous and bulk.size == Nl * Nq * 2 * Nz * 2 * Nx * Ny):
+            raise ValueError("bulk must be a C-contiguous complex128 (Nl, Nq, 2, Nz, 2, Ny, Nx) array")
+    rc = lib.oracle_run_bulk(ctypes.byref(p), lc.ctypes.data,
+                             None if mask is None else mask.ctypes.data, w.ctypes.data,
+                             E.ctypes.data, stages, None if bulk is None else bulk.ctypes.data)
     if rc != 0:
         raise RuntimeError("oracle failed")
     return s
 
 
-def run_backend_without_mask(json_str, lc_vals, E, stages=3):
-    """In-place on E (complex128, (Nl,Nq,4,Ny,Nx)); stages bit0 = z-loop, bit1 = screen filter."""
-    return _run(json_str, lc_vals, E, stages=stages)
+def run_backend_without_mask(json_str, lc_vals, E, stages=3, bulk=None):
+    """In-place on E (complex128, (Nl,Nq,4,Ny,Nx)); stages bit0 = z-loop, bit1 = screen filter.
+    bulk: optional (Nl, Nq, 2, Nz, 2, Ny, Nx) complex128 array receiving every plane's fields
+    (the bulk output of BPMIteration.cpp:111-121, 153-168)."""
+    return _run(json_str, lc_vals, E, stages=stages, bulk=bulk)
 
 
 def run_backend_with_mask(json_str, mask_formula, lc_vals, mask_vals, E, stages=3):

@@ -847,8 +847,11 @@ void screen_output(const Params& P, cd* E) {
 	}
 }
 
-// BPMIteration::propagate_fields (BPMIteration.cpp:53-177).
-void propagate(const Params& P, const double* lc, const unsigned char* mask, const double* w, cd* E) {
+// BPMIteration::propagate_fields (BPMIteration.cpp:53-177). With bulk non-null, the fields of
+// every transverse plane are recorded as the bulk output does (BPMIteration.cpp:111-121,
+// 153-168: the entrance plane after the input Fresnel operator, then plane iz+1 after each
+// slab, before the output Fresnel operator), as bulk[slot][iz][comp][iy][ix].
+void propagate(const Params& P, const double* lc, const unsigned char* mask, const double* w, cd* E, cd* bulk) {
 	int Nx = P.Nx, Ny = P.Ny, N = Nx * Ny, Nq = P.n_q;
 	for(int wi = 0; wi < P.n_wavelengths; wi++) {
 		double lam = P.wavelengths[wi];
@@ -885,6 +888,16 @@ void propagate(const Params& P, const double* lc, const unsigned char* mask, con
 				fresnel_in(eps, P.nin[wi], f);
 			}
 		}
+		auto record = [&](int iz) {
+			if(!bulk) return;
+			for(int pol = 0; pol < 2; pol++)
+				for(int q = 0; q < Nq; q++) {
+					size_t slot = pol + 2 * (q + (size_t)Nq * wi);
+					Field f = field(q, pol);
+					std::copy(f.d, f.d + 2 * N, bulk + (slot * P.Nz + iz) * 2 * N);
+				}
+		};
+		record(0);
 		for(int iz = 0; iz < P.Nz - 1; iz++) {
 			prim.update(iz);
 			phase.update(iz);
@@ -898,6 +911,7 @@ void propagate(const Params& P, const double* lc, const unsigned char* mask, con
 					shifts[q]->apply(f);
 				}
 			}
+			record(iz + 1);
 		}
 		for(int pol = 0; pol < 2; pol++)
 			for(int q = 0; q < Nq; q++) {
@@ -940,14 +954,15 @@ struct oracle_params {
 };
 
 // stages: bit 0 = z-propagation (BPMIteration), bit 1 = screen filter (ScreenOutput).
-int oracle_run(const oracle_params* p, const double* lc, const unsigned char* mask,
-		const double* interp_w, double* E, int stages) {
+// bulk (nullable): (slots, Nz, 2, Ny, Nx) complex, the fields of every plane.
+int oracle_run_bulk(const oracle_params* p, const double* lc, const unsigned char* mask,
+		const double* interp_w, double* E, int stages, double* bulk) {
 	static_assert(sizeof(oracle_params) == sizeof(Params), "layout");
 	Params P;
 	std::memcpy(&P, p, sizeof(P));
 	cd* Ec = reinterpret_cast<cd*>(E);
 	try {
-		if(stages & 1) propagate(P, lc, mask, interp_w, Ec);
+		if(stages & 1) propagate(P, lc, mask, interp_w, Ec, reinterpret_cast<cd*>(bulk));
 		if(stages & 2) screen_output(P, Ec);
 	}
 	catch(std::exception& e) {
@@ -955,6 +970,11 @@ int oracle_run(const oracle_params* p, const double* lc, const unsigned char* ma
 		return 1;
 	}
 	return 0;
+}
+
+int oracle_run(const oracle_params* p, const double* lc, const unsigned char* mask,
+		const double* interp_w, double* E, int stages) {
+	return oracle_run_bulk(p, lc, mask, interp_w, E, stages, nullptr);
 }
 
 // Unnormalised 1-D DFT of a contiguous complex line (sign -1 forward), for tests of the

@@ -42,6 +42,10 @@ CASES = {
     "odd_sizes": dict(dims=(15, 11, 5), q=((0.07, 0.02),)),
     "nz1": dict(dims=(8, 8, 1)),
     "nin_nout": dict(dims=(12, 12, 6), nin="1.3", nout="1.2"),
+    # several warps per x-line (Nx - 1 > 256) and the long-y-line solve (Ny - 1 > 512)
+    "long_x_lines": dict(dims=(300, 10, 4), q=((0.0, 0.0), (0.1, -0.05))),
+    "long_x_lines_1030": dict(dims=(1030, 6, 3), q=((0.04, 0.02),)),
+    "long_y_lines": dict(dims=(10, 530, 4), q=((0.0, 0.0), (-0.06, 0.09))),
 }
 
 
@@ -107,7 +111,7 @@ def test_uniform_director_closed_form_gpu(gpu):
             assert np.allclose(E[0, 0, 2 * pol + comp], J[comp, pol], rtol=0, atol=1e-12)
 
 
-@pytest.mark.parametrize("name", ["random_tilted_q", "two_wavelengths_dispersion", "iso_layers_focus"])
+@pytest.mark.parametrize("name", ["random_tilted_q", "two_wavelengths_dispersion", "iso_layers_focus", "long_x_lines"])
 def test_fp32_error_budget(gpu, name):
     kw = dict(CASES[name])
     dims = kw.pop("dims")
