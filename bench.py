@@ -224,7 +224,11 @@ def run_ours(args):
     # DRAM bytes per launch of the dominant kernel from one ncu capture (dram__bytes_read.sum +
     # dram__bytes_write.sum), scaled to this workload's launch by the slots it processes; the
     # capture and its command are summarised under profiles/.
-    TRAFFIC = {("config3", "fp32", "wood_solve_x"): (2 * 723.8e6, "profiles/solve_xc_yc_koehler_256x256x8_fp32.md")}
+    PROF = "profiles/solve_kernels_koehler_256x256x8_fp32.md"
+    TRAFFIC = {("config3", "fp32", "wood_solve_y"): (2 * (782.5e6 + 724.6e6) / 2, PROF),
+               ("config3", "fp32", "expl_solve_y"): (2 * 536.2e6, PROF),
+               ("config3", "fp32", "wood_solve_x"): (2 * (827.8e6 + 749.6e6) / 2, PROF),
+               ("config3", "fp32", "expl_solve_x"): (2 * 591.7e6, PROF)}
     roof = None
     if prof:
         top = max(prof, key=lambda k: prof[k]["ms"])

@@ -1447,9 +1447,10 @@ __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_xc(Geom G, 
 // y-line solve fused with its right-hand side (KIND: explicit x half-step or y Woodbury term),
 // chunked parallel form: block = 32 adjacent columns (lanes, coalesced) x WY warps for KS
 // slots of one wavelength; warp w owns the rows [w*M, w*M+M) of the 32 lines for all KS
-// slots. Chunk maps are combined across warps through shared memory.
-template <typename R, int M, int KIND, int KS>
-__global__ void __launch_bounds__(512, NBPM_YC_MINB) k_solve_yc(Geom G, int slot0, int nch, const cx<R>* __restrict__ coef,
+// slots. Chunk maps are combined across warps through shared memory. MAXT: block size the
+// instance is compiled for (512, or 1024 for 32 warps of short chunks).
+template <typename R, int M, int KIND, int KS, int MAXT = 512>
+__global__ void __launch_bounds__(MAXT, NBPM_YC_MINB) k_solve_yc(Geom G, int slot0, int nch, const cx<R>* __restrict__ coef,
 		const cx<R>* __restrict__ fac, size_t plane, const cx<double>* __restrict__ lsc,
 		const cx<R>* __restrict__ src, cx<R>* __restrict__ dst, const cx<R>* acc_in, cx<R>* acc_out) {
 	extern __shared__ unsigned char smem_raw[];
@@ -2279,7 +2280,8 @@ __global__ void __launch_bounds__(256) k_shift_fused(Geom G, int slot0, const Sh
 		}
 		return;
 	}
-	// 1. input window, phase_A applied
+	// 1. input window, phase_A applied (unrolled so several rows' loads are in flight)
+#pragma unroll 4
 	for(int e = tid; e < wx * wy; e += blockDim.x) {
 		int u = e % wx, v = e / wx;
 		int xi = ax ? pmod(x0 + bx + u, Px) : x0 + u;
@@ -2329,6 +2331,7 @@ __global__ void __launch_bounds__(256) k_shift_fused(Geom G, int slot0, const Sh
 		}
 	}
 	// 4. phase factor, phase_B, store
+#pragma unroll 4
 	for(int e = tid; e < SHT * SHT; e += blockDim.x) {
 		int t = e % SHT, v = e / SHT;
 		int ix = x0 + t, iy = y0 + v;

@@ -174,6 +174,7 @@ struct Plan : PlanBase {
 	cudaStream_t streamB = nullptr;  // per-slab setup (eps planes, coefficients, factorisations)
 	cudaStream_t cs = nullptr;       // stream the next launch goes to
 	cudaEvent_t eFork = nullptr, eJoin = nullptr, eCoef = nullptr, eFac = nullptr, eTrans = nullptr, eAdi[2] = {nullptr, nullptr};
+	cudaEvent_t eNref = nullptr, eNrefFork = nullptr;
 	// double-buffered factor planes / line scalars: slab iz uses half iz & 1
 	size_t facx_half = 0, facy_half = 0, lsc_half = 0;
 	cx<R>* fx_cur = nullptr;
@@ -231,6 +232,7 @@ struct Plan : PlanBase {
 		bool ys = false;  // y-lines too long for k_solve_yc: k_solve_ys with scratch-held chunks
 		bool xs = false;  // x-lines with long chunks: k_solve_xs with the chunks in shared memory
 		int WPLx = 1;     // warps per x-line (k_solve_xw when > 1: 32*WPLx chunks of Mx points)
+		bool y1024w = false;  // Woodbury y-solves with 32 warps of 8-row chunks, 2 slots per thread
 		int ymode = 0;
 		size_t plane_x = 0, plane_y = 0, smem_xg = 0;
 	};
@@ -247,7 +249,7 @@ struct Plan : PlanBase {
 		for(auto e : evpool) cudaEventDestroy(e);
 		if(gexec) cudaGraphExecDestroy(gexec);
 		for(auto& e : ev) if(e) cudaEventDestroy(e);
-		for(cudaEvent_t e : {eFork, eJoin, eCoef, eFac, eTrans, eAdi[0], eAdi[1]}) if(e) cudaEventDestroy(e);
+		for(cudaEvent_t e : {eFork, eJoin, eCoef, eFac, eTrans, eAdi[0], eAdi[1], eNref, eNrefFork}) if(e) cudaEventDestroy(e);
 		if(streamB) cudaStreamDestroy(streamB);
 		if(stream) cudaStreamDestroy(stream);
 	}
@@ -365,7 +367,7 @@ struct Plan : PlanBase {
 		CK(cudaSetDevice(opt.device));
 		CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
 		CK(cudaStreamCreateWithFlags(&streamB, cudaStreamNonBlocking));
-		for(cudaEvent_t* e : {&eFork, &eJoin, &eCoef, &eFac, &eTrans, &eAdi[0], &eAdi[1]})
+		for(cudaEvent_t* e : {&eFork, &eJoin, &eCoef, &eFac, &eTrans, &eAdi[0], &eAdi[1], &eNref, &eNrefFork})
 			CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
 		cs = stream;
 		for(auto& e : ev) CK(cudaEventCreate(&e));
@@ -424,6 +426,12 @@ struct Plan : PlanBase {
 				if(const char* e = std::getenv("NBPM_YWMAX")) wmax = std::min(16, std::max(1, std::atoi(e)));
 				for(int M = 2; M <= 32; M *= 2) if((uy + M - 1) / M <= wmax) { sc.My = M; break; }
 				if(sc.My) sc.WY = (uy + sc.My - 1) / sc.My;
+				// Woodbury y-solves of 129-256-row lines: 32 warps of 8-row chunks, two slots per
+				// thread (1024-thread blocks), measured faster on GB300 than 16 warps of 16 rows;
+				// the explicit-step solve keeps the 16-warp form. NBPM_Y1024=0 disables.
+				const char* ey = std::getenv("NBPM_Y1024");
+				if(sizeof(R) == sizeof(float) && uy > 128 && uy <= 256 && !(ey && std::atoi(ey) == 0) && h.spg % 2 == 0)
+					sc.y1024w = true;
 			}
 			// slots per thread: largest KS dividing 2*Nq with a compiled (M, KS) instance
 			// per-thread chunk values (M*KS complex) kept within 32 FP32 / 16 FP64 complex registers
@@ -437,7 +445,8 @@ struct Plan : PlanBase {
 				return 0;
 			};
 			if(sc.Mx) { sc.KSx = pick_ks(sc.Mx, kmx); if(!sc.KSx) sc.Mx = 0; }
-			if(sc.My) { sc.KSy = pick_ks(sc.My, kmy); if(!sc.KSy) { sc.My = 0; sc.WY = 0; } }
+			if(sc.My) { sc.KSy = pick_ks(sc.My, kmy); if(!sc.KSy) { sc.My = 0; sc.WY = 0; sc.y1024w = false; } }
+			if(kmy < 2) sc.y1024w = false;
 			if(const char* e = std::getenv("NBPM_YS")) if(std::atoi(e) == 1 && h.s.Ny > 3) { sc.My = 0; sc.WY = 0; }
 			if(sc.WPLx == 1 && (sc.Mx >= 32 || (sc.Mx && std::getenv("NBPM_XS") && std::atoi(std::getenv("NBPM_XS")) == 1))) {
 				sc.xs = true;
@@ -618,9 +627,14 @@ struct Plan : PlanBase {
 		double eps_bytes = 0, field_pts = 0;
 	};
 
-	// nref of every group, then the shift parameters (device side).
+	// nref of every group, then the shift parameters (device side). Runs on the setup stream,
+	// overlapping the entrance of the first pass on the main stream; the first transition
+	// waits for it (eNref).
 	void rec_prologue(SampleHost& h) {
 		const uint8_t* mk_ = h.has_mask ? h.dmask.as<uint8_t>() : nullptr;
+		CK(cudaEventRecord(eNrefFork, stream));
+		CK(cudaStreamWaitEvent(streamB, eNrefFork, 0));
+		cs = streamB;
 		int nb = (int)std::min<size_t>(1024, (h.nvox + 255) / 256);
 		launch("neff_partial", (double)h.nvox * h.fd * 8 * h.G, [&] {
 			k_neff_partial<<<dim3(nb, h.G), 256, 0, cs>>>(h.dir.as<double>(), h.fd, mk_, h.nvox,
@@ -634,6 +648,8 @@ struct Plan : PlanBase {
 			k_shift_params<<<(h.G * h.Nq + 63) / 64, 64, 0, cs>>>(h.G, h.Nq, h.geom.Nx, h.geom.Ny,
 				h.gpsd.as<GroupParams>(), h.qv.as<double>(), h.shiftd.as<ShiftParams>());
 		});
+		CK(cudaEventRecord(eNref, streamB));
+		cs = stream;
 	}
 
 	// Entrance of a pass: eps plane 0 and the initial fields.
@@ -691,6 +707,7 @@ struct Plan : PlanBase {
 		const int ng = ps.ng, nsl = ps.nsl, slot0 = ps.slot0;
 		const GroupParams* gps = ps.gps;
 		if(ps.iz >= iz_end) return;
+		CK(cudaStreamWaitEvent(stream, eNref, 0));  // shift parameters
 		CK(cudaEventRecord(eFork, stream));
 		CK(cudaStreamWaitEvent(streamB, eFork, 0));
 		for(int iz = ps.iz; iz < iz_end; iz++) {
@@ -761,6 +778,7 @@ struct Plan : PlanBase {
 		const int N = Gm.N, Nz = Gm.Nz;
 		const double sc = sizeof(cx<R>);
 		cs = stream;
+		CK(cudaStreamWaitEvent(stream, eNref, 0));
 		if(Nz > 1) rec_transition(h, ps.slot0, ps.nsl, ps.Cprev, nullptr, ps.Fp, ps.Tb, ps.T2b, false);
 		const GroupParams* gps = ps.gps;
 		R* Qlast = ps.Qr[(Nz - 1) & 1];
@@ -907,13 +925,13 @@ struct Plan : PlanBase {
 		double bytes = (double)Gm.N * nsl * 2 * sz * (acc_out ? 4 : 2) + (double)Gm.N * ng * 2 * NFAC * sz;
 		if(dirn == 0)
 			launch("solve_x", bytes, [&] {
-				k_solve<R, 0><<<(nt + 127) / 128, 128, 0, cs>>>(Gm, slot0, nsl, facx.as<cx<R>>(), sc.plane_x,
-					lscx.as<cx<double>>(), src, dst, acc_in, acc_out);
+				k_solve<R, 0><<<(nt + 127) / 128, 128, 0, cs>>>(Gm, slot0, nsl, fx_cur, sc.plane_x, lx_cur, src, dst,
+					acc_in, acc_out);
 			});
 		else
 			launch("solve_y", bytes, [&] {
-				k_solve<R, 1><<<(nt + 127) / 128, 128, 0, cs>>>(Gm, slot0, nsl, facy.as<cx<R>>(), sc.plane_y,
-					lscy.as<cx<double>>(), src, dst, acc_in, acc_out);
+				k_solve<R, 1><<<(nt + 127) / 128, 128, 0, cs>>>(Gm, slot0, nsl, fy_cur, sc.plane_y, ly_cur, src, dst,
+					acc_in, acc_out);
 			});
 	}
 
@@ -999,10 +1017,15 @@ struct Plan : PlanBase {
 				return;
 			}
 			L.M = sc.My; L.KS = sc.KSy; L.kind = sc.ymode == 1 ? ST_GIVEN : (wood ? ST_WOOD_Y : ST_EXPL_X);
+			int WY = sc.WY;
+			if(wood && sc.y1024w && sc.ymode != 1) {
+				L.M = 8; L.KS = 2;
+				WY = (Gm.Ny - 1 + 7) / 8;
+			}
 			int nch = h.spg / L.KS;
 			L.grid = dim3((unsigned)((Gm.Nx + 31) / 32), (unsigned)(ng * nch * 2));
-			L.block = dim3(32, sc.WY);
-			L.smem = (size_t)(4 * L.KS * sc.WY * 32 + 2 * L.KS * 32) * sizeof(cx<R>);
+			L.block = dim3(32, WY);
+			L.smem = (size_t)(4 * L.KS * WY * 32 + 2 * L.KS * 32) * sizeof(cx<R>);
 			launch(wood ? "wood_solve_y" : "expl_solve_y", bytes, [&] {
 				if(!launch_solve_yc<R>(L, Gm, slot0, nch, C, fy_cur, sc.plane_y, ly_cur, rsrc,
 						dst, acc_in, acc_out))

@@ -17,6 +17,29 @@ template <>
 bool launch_solve_yc<double>(const SolveLaunch& L, Geom G, int slot0, int nch, const cx<double>* coef,
 		const cx<double>* fac, size_t plane, const cx<double>* lsc, const cx<double>* src, cx<double>* dst,
 		const cx<double>* ai, cx<double>* ao) {
+	if(L.block.y > 16) {  // 32 warps of 8-row chunks
+		if(L.M == 8 && L.KS == 1 && L.kind == ST_EXPL_X) {
+			k_solve_yc<double, 8, ST_EXPL_X, 1, 1024><<<L.grid, L.block, L.smem, L.stream>>>(G, slot0, nch, coef, fac, plane,
+				lsc, src, dst, ai, ao);
+			return true;
+		}
+		if(L.M == 8 && L.KS == 1 && L.kind == ST_WOOD_Y) {
+			k_solve_yc<double, 8, ST_WOOD_Y, 1, 1024><<<L.grid, L.block, L.smem, L.stream>>>(G, slot0, nch, coef, fac, plane,
+				lsc, src, dst, ai, ao);
+			return true;
+		}
+		if(L.M == 8 && L.KS == 2 && L.kind == ST_EXPL_X) {
+			k_solve_yc<double, 8, ST_EXPL_X, 2, 1024><<<L.grid, L.block, L.smem, L.stream>>>(G, slot0, nch, coef, fac, plane,
+				lsc, src, dst, ai, ao);
+			return true;
+		}
+		if(L.M == 8 && L.KS == 2 && L.kind == ST_WOOD_Y) {
+			k_solve_yc<double, 8, ST_WOOD_Y, 2, 1024><<<L.grid, L.block, L.smem, L.stream>>>(G, slot0, nch, coef, fac, plane,
+				lsc, src, dst, ai, ao);
+			return true;
+		}
+		return false;
+	}
 	NBPM_YC_PAIRS(ST_EXPL_X)
 	NBPM_YC_PAIRS(ST_WOOD_Y)
 	NBPM_YC_PAIRS(ST_GIVEN)
@@ -30,6 +53,10 @@ bool launch_solve_yc<double>(const SolveLaunch& L, Geom G, int slot0, int nch, c
 	NBPM_YA(8, 1, KIND) NBPM_YA(8, 2, KIND) NBPM_YA(8, 4, KIND) NBPM_YA(16, 1, KIND) NBPM_YA(16, 2, KIND) NBPM_YA(32, 1, KIND)
 
 void set_solve_smem_y_f64(int bytes) {
+	cudaFuncSetAttribute(k_solve_yc<double, 8, ST_EXPL_X, 1, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+	cudaFuncSetAttribute(k_solve_yc<double, 8, ST_WOOD_Y, 1, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+	cudaFuncSetAttribute(k_solve_yc<double, 8, ST_EXPL_X, 2, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+	cudaFuncSetAttribute(k_solve_yc<double, 8, ST_WOOD_Y, 2, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 	NBPM_YA_PAIRS(ST_EXPL_X)
 	NBPM_YA_PAIRS(ST_WOOD_Y)
 	NBPM_YA_PAIRS(ST_GIVEN)

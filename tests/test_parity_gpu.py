@@ -46,6 +46,8 @@ CASES = {
     "long_x_lines": dict(dims=(300, 10, 4), q=((0.0, 0.0), (0.1, -0.05))),
     "long_x_lines_1030": dict(dims=(1030, 6, 3), q=((0.04, 0.02),)),
     "long_y_lines": dict(dims=(10, 530, 4), q=((0.0, 0.0), (-0.06, 0.09))),
+    "sequential_x_lines": dict(dims=(2100, 5, 3), q=((0.03, 0.0),)),
+    "tall_mesh": dict(dims=(12, 200, 5), q=((0.0, 0.0), (0.05, 0.08))),
 }
 
 
@@ -111,7 +113,8 @@ def test_uniform_director_closed_form_gpu(gpu):
             assert np.allclose(E[0, 0, 2 * pol + comp], J[comp, pol], rtol=0, atol=1e-12)
 
 
-@pytest.mark.parametrize("name", ["random_tilted_q", "two_wavelengths_dispersion", "iso_layers_focus", "long_x_lines"])
+@pytest.mark.parametrize("name", ["random_tilted_q", "two_wavelengths_dispersion", "iso_layers_focus", "long_x_lines",
+                                  "tall_mesh"])
 def test_fp32_error_budget(gpu, name):
     kw = dict(CASES[name])
     dims = kw.pop("dims")
