@@ -93,6 +93,37 @@ __device__ __forceinline__ double neff_of(double xxtr, double yytr, double xytr)
 	return (sqrt(tr + r) + sqrt(tr - r)) / 2.;
 }
 
+// neff of one voxel in FP32 arithmetic (the same formulas as eps_voxel + neff_of), for the nref
+// mean of the FP32 mode.
+__device__ __forceinline__ float neff_voxel_f(const double* __restrict__ dir, int fd, bool m, float eps_perp,
+		float eps_a, float eps_host) {
+	float e0, e1, e2, e3, e4, e5;
+	if(!m) return sqrtf(eps_host);
+	if(fd == 3) {
+		float n0 = (float)dir[0], n1 = (float)dir[1], n2 = (float)dir[2];
+		e0 = eps_perp + eps_a * (n0 * n0);
+		e1 = eps_perp + eps_a * (n1 * n1);
+		e2 = eps_perp + eps_a * (n2 * n2);
+		e3 = eps_a * n0 * n1;
+		e4 = eps_a * n0 * n2;
+		e5 = eps_a * n1 * n2;
+	}
+	else {
+		float ea = 2 * eps_a / 3, ei = eps_perp + eps_a / 3.f;
+		e0 = ei + ea * (float)dir[0];
+		e1 = ei + ea * (float)dir[1];
+		e2 = ei + ea * (float)dir[2];
+		e3 = ea * (float)dir[3];
+		e4 = ea * (float)dir[4];
+		e5 = ea * (float)dir[5];
+	}
+	float xx = e0 - (e4 * e4) / e2, yy = e1 - (e5 * e5) / e2, xy = e3 - e4 * e5 / e2;
+	float det = xx * yy - xy * xy, tr = 0.5f * (xx + yy);
+	if(tr * tr - det < 1e-8f) return sqrtf(tr);
+	float r = sqrtf(tr * tr - det);
+	return (sqrtf(tr + r) + sqrtf(tr - r)) / 2.f;
+}
+
 // One transverse plane of derived quantities for every group of the pass, computed in FP64
 // and stored in the plan's precision Q.
 template <typename Q>
@@ -123,13 +154,20 @@ static __global__ void k_eps_plane(const double* __restrict__ dir, int fd, const
 
 // Partial sums of neff over the volume for nref (PermittivityTensorField.cpp:183-211),
 // in a fixed block order so the reduction is deterministic.
+// FP32 mode (F32 = true): neff in FP32 arithmetic, summed in FP64.
+template <bool F32>
 static __global__ void k_neff_partial(const double* __restrict__ dir, int fd, const uint8_t* __restrict__ mask,
 		size_t nvox, const GroupParams* __restrict__ gps, double* __restrict__ partial) {
 	__shared__ double sh[256];
 	int g = blockIdx.y;
 	GroupParams gp = gps[g];
 	double acc = 0;
+	const float ep = (float)(gp.no * gp.no), ea = (float)(gp.ne * gp.ne - gp.no * gp.no), eh = (float)(gp.nhost * gp.nhost);
 	for(size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvox; v += (size_t)gridDim.x * blockDim.x) {
+		if(F32) {
+			acc += (double)neff_voxel_f(dir + v * fd, fd, mask ? mask[v] != 0 : true, ep, ea, eh);
+			continue;
+		}
 		double e[6];
 		eps_voxel(dir + v * fd, fd, mask ? mask[v] != 0 : true, gp, e);
 		double xxtr = e[0] - (e[4] * e[4]) / e[2];
@@ -1444,6 +1482,60 @@ __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_xc(Geom G, 
 	}
 }
 
+// Column-parallel combine of the y-chunk maps of a block (32 columns x WY chunks, maps at
+// [j][chunk][column] in shared memory): warp w scans columns w, w + WY, ... with its lanes
+// indexing the chunks, so all warps work at once. sD receives, per chunk, the state entering
+// it from the line's start (reverse: from the line's end), starting from zero.
+template <typename R, int KS>
+__device__ __forceinline__ void ycol_scan(const cx<R>* sA, const cx<R>* sB, cx<R>* sD, int WY, int w, int lane,
+		bool reverse) {
+	const int SZ = WY * 32;
+	const cx<R> one = mk<R>(1, 0), zero = mk<R>(0, 0);
+	for(int col = w; col < 32; col += WY) {
+#pragma unroll
+		for(int j = 0; j < KS; j++) {
+			const int ch = lane;  // chunk handled by this lane
+			cx<R> A = one, B = zero;
+			if(ch < WY) { A = sA[j * SZ + ch * 32 + col]; B = sB[j * SZ + ch * 32 + col]; }
+			if(!reverse) {
+#pragma unroll
+				for(int o = 1; o < 32; o <<= 1) {
+					cx<R> Ap = shfl_up_c(A, o), Bp = shfl_up_c(B, o);
+					if(lane >= o) { B = A * Bp + B; A = A * Ap; }
+				}
+				cx<R> D = shfl_up_c(B, 1);
+				if(lane == 0) D = zero;
+				if(ch < WY) sD[j * SZ + ch * 32 + col] = D;
+			}
+			else {
+#pragma unroll
+				for(int o = 1; o < 32; o <<= 1) {
+					cx<R> An = shfl_down_c(A, o), Bn = shfl_down_c(B, o);
+					if(lane + o < 32) { B = A * Bn + B; A = A * An; }
+				}
+				cx<R> D = shfl_down_c(B, 1);
+				if(lane == 31) D = zero;
+				if(ch < WY) sD[j * SZ + ch * 32 + col] = D;
+			}
+		}
+	}
+}
+
+// Column totals of per-chunk values sP[j][chunk][column] into sF[j][column].
+template <typename R, int KS>
+__device__ __forceinline__ void ycol_sum(const cx<R>* sP, cx<R>* sF, int WY, int w, int lane) {
+	const int SZ = WY * 32;
+	for(int col = w; col < 32; col += WY) {
+#pragma unroll
+		for(int j = 0; j < KS; j++) {
+			cx<R> v = lane < WY ? sP[j * SZ + lane * 32 + col] : mk<R>(0, 0);
+#pragma unroll
+			for(int o = 16; o > 0; o >>= 1) v += shfl_xor_c(v, o);
+			if(lane == 0) sF[j * 32 + col] = v;
+		}
+	}
+}
+
 // y-line solve fused with its right-hand side (KIND: explicit x half-step or y Woodbury term),
 // chunked parallel form: block = 32 adjacent columns (lanes, coalesced) x WY warps for KS
 // slots of one wavelength; warp w owns the rows [w*M, w*M+M) of the 32 lines for all KS
@@ -1508,15 +1600,7 @@ __global__ void __launch_bounds__(MAXT, NBPM_YC_MINB) k_solve_yc(Geom G, int slo
 #pragma unroll
 	for(int j = 0; j < KS; j++) { sA[j * SZ + w * 32 + lane] = A[j]; sB[j * SZ + w * 32 + lane] = B[j]; }
 	__syncthreads();
-	if(w == 0) {
-		for(int j = 0; j < KS; j++) {
-			cx<R> D = zero;
-			for(int ww = 0; ww < WY; ww++) {
-				sD[j * SZ + ww * 32 + lane] = D;
-				D = sA[j * SZ + ww * 32 + lane] * D + sB[j * SZ + ww * 32 + lane];
-			}
-		}
-	}
+	ycol_scan<R, KS>(sA, sB, sD, WY, w, lane, false);
 	__syncthreads();
 	cx<R> d[KS], acc[KS];
 #pragma unroll
@@ -1539,12 +1623,11 @@ __global__ void __launch_bounds__(MAXT, NBPM_YC_MINB) k_solve_yc(Geom G, int slo
 #pragma unroll
 	for(int j = 0; j < KS; j++) sP[j * SZ + w * 32 + lane] = acc[j];
 	__syncthreads();
+	ycol_sum<R, KS>(sP, sF, WY, w, lane);  // sF = column totals
+	__syncthreads();
 	if(w == 0) {
-		for(int j = 0; j < KS; j++) {
-			cx<R> tot = zero;
-			for(int ww = 0; ww < WY; ww++) tot += sP[j * SZ + ww * 32 + lane];
-			sF[j * 32 + lane] = cvt<R>((cvt<double>(tot) - r0 * cvt<double>(sL[j * 32 + lane])) * rden);
-		}
+		for(int j = 0; j < KS; j++)
+			sF[j * 32 + lane] = cvt<R>((cvt<double>(sF[j * 32 + lane]) - r0 * cvt<double>(sL[j * 32 + lane])) * rden);
 	}
 #pragma unroll
 	for(int j = 0; j < KS; j++) { A[j] = one; B[j] = zero; }
@@ -1560,15 +1643,7 @@ __global__ void __launch_bounds__(MAXT, NBPM_YC_MINB) k_solve_yc(Geom G, int slo
 #pragma unroll
 	for(int j = 0; j < KS; j++) { sA[j * SZ + w * 32 + lane] = A[j]; sB[j * SZ + w * 32 + lane] = B[j]; }
 	__syncthreads();
-	if(w == 0) {
-		for(int j = 0; j < KS; j++) {
-			cx<R> D = zero;
-			for(int ww = WY - 1; ww >= 0; ww--) {
-				sD[j * SZ + ww * 32 + lane] = D;
-				D = sA[j * SZ + ww * 32 + lane] * D + sB[j * SZ + ww * 32 + lane];
-			}
-		}
-	}
+	ycol_scan<R, KS>(sA, sB, sD, WY, w, lane, true);
 	__syncthreads();
 	cx<R> fr[KS];
 #pragma unroll
@@ -2280,7 +2355,7 @@ __global__ void __launch_bounds__(256) k_shift_fused(Geom G, int slot0, const Sh
 		}
 		return;
 	}
-	// 1. input window, phase_A applied (unrolled so several rows' loads are in flight)
+	// 1. input window, phase_A applied (unrolled so several loads are in flight)
 #pragma unroll 4
 	for(int e = tid; e < wx * wy; e += blockDim.x) {
 		int u = e % wx, v = e / wx;

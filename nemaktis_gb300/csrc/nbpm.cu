@@ -376,7 +376,8 @@ struct Plan : PlanBase {
 		CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
 		smem_limit = (size_t)optin;
 		CK(cudaFuncSetAttribute(k_fft_lines<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit));
-		CK(cudaFuncSetAttribute(k_shift_fused<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit));
+		CK(cudaFuncSetAttribute(k_shift_fused<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			(int)((size_t)4 * (SHT + 6) * (SHT + 6) * sizeof(cx<R>))));
 		if(const char* e = std::getenv("NBPM_SHIFT_FUSED")) shift_fused = std::atoi(e) != 0;
 		if(const char* e = std::getenv("NBPM_FACTOR_SEQ")) factor_seq = std::atoi(e) != 0;
 		if(sizeof(R) == sizeof(float)) {
@@ -637,7 +638,7 @@ struct Plan : PlanBase {
 		cs = streamB;
 		int nb = (int)std::min<size_t>(1024, (h.nvox + 255) / 256);
 		launch("neff_partial", (double)h.nvox * h.fd * 8 * h.G, [&] {
-			k_neff_partial<<<dim3(nb, h.G), 256, 0, cs>>>(h.dir.as<double>(), h.fd, mk_, h.nvox,
+			k_neff_partial<sizeof(R) == sizeof(float)><<<dim3(nb, h.G), 256, 0, cs>>>(h.dir.as<double>(), h.fd, mk_, h.nvox,
 				h.gpsd.as<GroupParams>(), h.partial.as<double>());
 		});
 		launch("nref_final", 8.0 * nb * h.G, [&] {
