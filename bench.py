@@ -367,6 +367,12 @@ def cpu_baseline(samples, seconds):
                       % (c["Nz"] - 1, runs, el)}
 
 
+def workloads_voxel_steps(c):
+    """Voxel-steps of one sample of a workload (every slab of every propagation)."""
+    from nemaktis_gb300 import workloads
+    return workloads.voxel_steps(c["shape"], c["Nz"])
+
+
 def run_reference(args):
     world, rank, local = dist_env()
     if rank != 0:
@@ -380,8 +386,10 @@ def run_reference(args):
             ms.append(r)
             cpu = r
     v = float(np.median([r["value"] for r in ms]))
+    vs_step = sum(workloads_voxel_steps(c) for c in samples)
     line = {"impl": "reference", "metric": "voxel-steps/s FP32-batched vs FP64 plain, 1 GB300, <=1e-4 rel err; p50/p99 latency",
             "value": v, "unit": "voxel-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * vs_step / v if v > 0 else None,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "complex-f64",
             "data": "synthetic (seeded director fields, no dataset)",
             "config": {"workload": samples[0]["desc"], "precision": "fp64 CPU oracle (reference not buildable here)"},
