@@ -124,8 +124,8 @@ __device__ __forceinline__ float neff_voxel_f(const double* __restrict__ dir, in
 	return (sqrtf(tr + r) + sqrtf(tr - r)) / 2.f;
 }
 
-// One transverse plane of derived quantities for every group of the pass, computed in FP64
-// and stored in the plan's precision Q.
+// One transverse plane of derived quantities for every group of the pass, computed and
+// stored in the plan's precision Q (FP64 mode: FP64; FP32 mode: FP32).
 template <typename Q>
 static __global__ void k_eps_plane(const double* __restrict__ dir, int fd, const uint8_t* __restrict__ mask,
 		int N, int iz, const GroupParams* __restrict__ gps, Q* __restrict__ out) {
@@ -134,13 +134,46 @@ static __global__ void k_eps_plane(const double* __restrict__ dir, int fd, const
 	if(p >= N) return;
 	size_t v = (size_t)iz * N + p;
 	GroupParams gp = gps[g];
+	const bool m = mask ? mask[v] != 0 : true;
+	Q* o = out + (size_t)g * NQ * N + p;
+	if(sizeof(Q) == sizeof(float)) {
+		// FP32 mode: the same formulas in FP32 arithmetic
+		const float ep = (float)(gp.no * gp.no), ea = (float)(gp.ne * gp.ne - gp.no * gp.no);
+		const float eh = (float)(gp.nhost * gp.nhost);
+		const double* d = dir + v * fd;
+		float e0, e1, e2, e3, e4, e5;
+		if(!m) { e0 = e1 = e2 = eh; e3 = e4 = e5 = 0.f; }
+		else if(fd == 3) {
+			float n0 = (float)d[0], n1 = (float)d[1], n2 = (float)d[2];
+			e0 = ep + ea * (n0 * n0); e1 = ep + ea * (n1 * n1); e2 = ep + ea * (n2 * n2);
+			e3 = ea * n0 * n1; e4 = ea * n0 * n2; e5 = ea * n1 * n2;
+		}
+		else {
+			float a = 2 * ea / 3, ei = ep + ea / 3.f;
+			e0 = ei + a * (float)d[0]; e1 = ei + a * (float)d[1]; e2 = ei + a * (float)d[2];
+			e3 = a * (float)d[3]; e4 = a * (float)d[4]; e5 = a * (float)d[5];
+		}
+		float xx = e0 - (e4 * e4) / e2, yy = e1 - (e5 * e5) / e2, xy = e3 - e4 * e5 / e2;
+		float det = xx * yy - xy * xy, tr = 0.5f * (xx + yy), ne;
+		if(tr * tr - det < 1e-8f) ne = sqrtf(tr);
+		else { float r = sqrtf(tr * tr - det); ne = (sqrtf(tr + r) + sqrtf(tr - r)) / 2.f; }
+		o[Q_XXTR * N] = (Q)xx;
+		o[Q_YYTR * N] = (Q)yy;
+		o[Q_XYTR * N] = (Q)xy;
+		o[Q_XXS * N] = (Q)(ne + (xx - yy) / (4 * ne));
+		o[Q_YYS * N] = (Q)(ne + (yy - xx) / (4 * ne));
+		o[Q_XYS * N] = (Q)(xy / (2 * ne));
+		o[Q_VX * N] = (Q)(e4 / e2);
+		o[Q_VY * N] = (Q)(e5 / e2);
+		o[Q_IZZ * N] = (Q)(1.f / e2);
+		return;
+	}
 	double e[6];
-	eps_voxel(dir + v * fd, fd, mask ? mask[v] != 0 : true, gp, e);
+	eps_voxel(dir + v * fd, fd, m, gp, e);
 	double xxtr = e[0] - (e[4] * e[4]) / e[2];
 	double yytr = e[1] - (e[5] * e[5]) / e[2];
 	double xytr = e[3] - e[4] * e[5] / e[2];
 	double neff = neff_of(xxtr, yytr, xytr);
-	Q* o = out + (size_t)g * NQ * N + p;
 	o[Q_XXTR * N] = (Q)xxtr;
 	o[Q_YYTR * N] = (Q)yytr;
 	o[Q_XYTR * N] = (Q)xytr;
@@ -2355,12 +2388,19 @@ __global__ void __launch_bounds__(256) k_shift_fused(Geom G, int slot0, const Sh
 		}
 		return;
 	}
-	// 1. input window, phase_A applied (unrolled so several loads are in flight)
+	// 1. input window, phase_A applied. The wrapped source column and row of every window
+	// position are tabulated once; the loop runs over the fixed pitch PW so that its index
+	// arithmetic has compile-time divisors (positions beyond the window are zero and unused).
+	__shared__ int xcol[SHT + 6], yrow[SHT + 6];
+	for(int u = tid; u < PW; u += blockDim.x) {
+		xcol[u] = u < wx ? (ax ? pmod(x0 + bx + u, Px) : x0 + u) : Nx;
+		yrow[u] = u < wy ? (ay ? pmod(y0 + by + u, Py) : y0 + u) : Ny;
+	}
+	__syncthreads();
 #pragma unroll 4
-	for(int e = tid; e < wx * wy; e += blockDim.x) {
-		int u = e % wx, v = e / wx;
-		int xi = ax ? pmod(x0 + bx + u, Px) : x0 + u;
-		int yi = ay ? pmod(y0 + by + v, Py) : y0 + v;
+	for(int e = tid; e < PW * wy; e += blockDim.x) {
+		const int u = e % PW, v = e / PW;
+		const int xi = xcol[u], yi = yrow[v];
 		cx<R> a = mk<R>(0, 0), b = mk<R>(0, 0);
 		if(xi < Nx && yi < Ny) tap_in(f, Ca, N, xi + Nx * yi, a, b);
 		A[v * PW + u] = a;
@@ -2374,8 +2414,9 @@ __global__ void __launch_bounds__(256) k_shift_fused(Geom G, int slot0, const Sh
 	if(ax) {
 		for(int pass = 0; pass < nsh; pass++) {
 			int ow = cw - 3;
-			for(int e = tid; e < ow * wy; e += blockDim.x) {
-				int t = e % ow, v = e / ow;
+			for(int e = tid; e < PW * wy; e += blockDim.x) {
+				const int t = e % PW, v = e / PW;
+				if(t >= ow) continue;
 				for(int c = 0; c < 2; c++) {
 					const cx<R>* in = cur + c * PW * PW + v * PW + t;
 					nxt[c * PW * PW + v * PW + t] = (R)P.wx[0] * in[0] + (R)P.wx[1] * in[1] + (R)P.wx[2] * in[2] +
