@@ -2388,19 +2388,12 @@ __global__ void __launch_bounds__(256) k_shift_fused(Geom G, int slot0, const Sh
 		}
 		return;
 	}
-	// 1. input window, phase_A applied. The wrapped source column and row of every window
-	// position are tabulated once; the loop runs over the fixed pitch PW so that its index
-	// arithmetic has compile-time divisors (positions beyond the window are zero and unused).
-	__shared__ int xcol[SHT + 6], yrow[SHT + 6];
-	for(int u = tid; u < PW; u += blockDim.x) {
-		xcol[u] = u < wx ? (ax ? pmod(x0 + bx + u, Px) : x0 + u) : Nx;
-		yrow[u] = u < wy ? (ay ? pmod(y0 + by + u, Py) : y0 + u) : Ny;
-	}
-	__syncthreads();
+	// 1. input window, phase_A applied (unrolled so several loads are in flight)
 #pragma unroll 4
-	for(int e = tid; e < PW * wy; e += blockDim.x) {
-		const int u = e % PW, v = e / PW;
-		const int xi = xcol[u], yi = yrow[v];
+	for(int e = tid; e < wx * wy; e += blockDim.x) {
+		int u = e % wx, v = e / wx;
+		int xi = ax ? pmod(x0 + bx + u, Px) : x0 + u;
+		int yi = ay ? pmod(y0 + by + v, Py) : y0 + v;
 		cx<R> a = mk<R>(0, 0), b = mk<R>(0, 0);
 		if(xi < Nx && yi < Ny) tap_in(f, Ca, N, xi + Nx * yi, a, b);
 		A[v * PW + u] = a;
@@ -2414,9 +2407,8 @@ __global__ void __launch_bounds__(256) k_shift_fused(Geom G, int slot0, const Sh
 	if(ax) {
 		for(int pass = 0; pass < nsh; pass++) {
 			int ow = cw - 3;
-			for(int e = tid; e < PW * wy; e += blockDim.x) {
-				const int t = e % PW, v = e / PW;
-				if(t >= ow) continue;
+			for(int e = tid; e < ow * wy; e += blockDim.x) {
+				int t = e % ow, v = e / ow;
 				for(int c = 0; c < 2; c++) {
 					const cx<R>* in = cur + c * PW * PW + v * PW + t;
 					nxt[c * PW * PW + v * PW + t] = (R)P.wx[0] * in[0] + (R)P.wx[1] * in[1] + (R)P.wx[2] * in[2] +
