@@ -1370,6 +1370,63 @@ __global__ void __launch_bounds__(256) k_factor_chunked(Geom G, int ngroups, int
 	}
 }
 
+// One combine of the chunk maps of a line whose chunks sit on the 32 lanes of a warp (chunk =
+// lane; lanes past the line carry identity maps). Inputs per lane: forward map (P, d0[j]),
+// sum terms (S0[j], S1), backward terms (Cp, G0[j], G1). Outputs per lane: din = the forward
+// value entering the chunk, xin = the backward value entering it from the line's end, and
+// fr = (sum_i w_i d_i - r0 * d_last) * rden, the Sherman-Morrison factor (same on all lanes).
+template <typename R, int KS>
+__device__ __forceinline__ void line_combine(cx<R> P, const cx<R>* d0, const cx<R>* S0, cx<R> S1, const cx<R>* G0,
+		cx<R> G1, cx<R> Cp, cx<double> r0, cx<double> rden, int lane, cx<R>* din, cx<R>* xin, cx<R>* fr) {
+	const cx<R> zero = mk<R>(0, 0);
+	cx<R> B[KS];
+#pragma unroll
+	for(int j = 0; j < KS; j++) B[j] = d0[j];
+#pragma unroll
+	for(int o = 1; o < 32; o <<= 1) {
+		const cx<R> Pp = shfl_up_c(P, o);
+#pragma unroll
+		for(int j = 0; j < KS; j++) {
+			const cx<R> Bp = shfl_up_c(B[j], o);
+			if(lane >= o) B[j] = P * Bp + B[j];
+		}
+		if(lane >= o) P = P * Pp;
+	}
+	cx<R> G[KS];
+	cx<R> tsel = zero, dsel = zero;  // lane j < KS keeps slot j's sum and last value
+#pragma unroll
+	for(int j = 0; j < KS; j++) {
+		din[j] = shfl_up_c(B[j], 1);
+		if(lane == 0) din[j] = zero;
+		cx<R> t = S0[j] + S1 * din[j];
+#pragma unroll
+		for(int o = 16; o > 0; o >>= 1) t += shfl_xor_c(t, o);
+		const cx<R> dl = shfl_idx_c(B[j], 31);
+		if(lane == j) { tsel = t; dsel = dl; }
+		G[j] = G0[j] + G1 * din[j];
+	}
+	// the FP64 factor once per slot (lane j), then broadcast
+	cx<R> f = zero;
+	if(lane < KS) f = cvt<R>((cvt<double>(tsel) - r0 * cvt<double>(dsel)) * rden);
+#pragma unroll
+	for(int j = 0; j < KS; j++) fr[j] = shfl_idx_c(f, j);
+#pragma unroll
+	for(int o = 1; o < 32; o <<= 1) {
+		const cx<R> Cn = shfl_down_c(Cp, o);
+#pragma unroll
+		for(int j = 0; j < KS; j++) {
+			const cx<R> Gn = shfl_down_c(G[j], o);
+			if(lane + o < 32) G[j] = Cp * Gn + G[j];
+		}
+		if(lane + o < 32) Cp = Cp * Cn;
+	}
+#pragma unroll
+	for(int j = 0; j < KS; j++) {
+		xin[j] = shfl_down_c(G[j], 1);
+		if(lane == 31) xin[j] = zero;
+	}
+}
+
 template <typename R, int M, int KIND, int KS>
 // Resident blocks per SM requested from the compiler: 8 (64 registers) for the instances
 // whose chunk values fit, measured faster on GB300; the larger instances keep their registers.
@@ -1398,7 +1455,6 @@ __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_xc(Geom G, 
 	const cx<double>* ls = lsc + (((size_t)g * 2 + c) * Ny + iy) * 2;
 	const cx<double> r0 = ls[0], rden = ls[1];
 	const int i0 = lane * M;
-	const int last = n_unk - 1, lane_last = last / M, k_last = last % M;
 	const cx<R> one = mk<R>(1, 0), zero = mk<R>(0, 0);
 	const Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
 	const cx<R>* f0 = src + (size_t)s0 * 2 * N;
@@ -1409,97 +1465,59 @@ __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_xc(Geom G, 
 		for(int j = 0; j < KS; j++) buf[j * PITCH + (e / M) * (M + 1) + e % M] = r[j];
 	}
 	__syncwarp();
-	cx<R> v[KS][M];
-	cx<R> A[KS], B[KS];
+	// Local pass over the lane's chunk: the right-hand sides b (written back over the stencil
+	// values in buf), the zero-carry forward values d0 and the three maps that finish the line
+	// after one combine:
+	//   forward   D_out = P * D_in + d0_end                  (P = product of a)
+	//   sum       sum_i w_i d_i = S0 + S1 * D_in
+	//   backward  x_start = Cp * X_in + G0 + G1 * D_in       (Cp = product of c)
+	// P, S1, G1 and Cp do not depend on the slot. The chunk values live in shared memory, not
+	// in registers.
+	cx<R> d0[KS], S0[KS], G0[KS];
+	cx<R> P = one, S1 = zero, G1 = zero, Cp = one;
 #pragma unroll
-	for(int j = 0; j < KS; j++) { A[j] = one; B[j] = zero; }
-#pragma unroll
-	for(int k = 0; k < M; k++) {
-		bool ok = i0 + k < n_unk;
-		cx<R> a = zero, rb = zero;
-		if(ok) { a = Fc[F_A * plane + k * 32 + lane]; rb = Fc[F_RB * plane + k * 32 + lane]; }
-#pragma unroll
-		for(int j = 0; j < KS; j++) {
-			v[j][k] = zero;
-			if(ok) {
-				cx<R> b = buf[j * PITCH + lane * (M + 1) + k] * rb;
-				v[j][k] = b;
-				B[j] = a * B[j] + b;
-				A[j] = a * A[j];
-			}
-		}
-	}
-#pragma unroll
-	for(int o = 1; o < 32; o <<= 1) {
-#pragma unroll
-		for(int j = 0; j < KS; j++) {
-			cx<R> Ap = shfl_up_c(A[j], o), Bp = shfl_up_c(B[j], o);
-			if(lane >= o) { B[j] = A[j] * Bp + B[j]; A[j] = A[j] * Ap; }
-		}
-	}
-	cx<R> d[KS], acc[KS], dl[KS];
-#pragma unroll
-	for(int j = 0; j < KS; j++) {
-		d[j] = shfl_up_c(B[j], 1);
-		if(lane == 0) d[j] = zero;
-		acc[j] = zero;
-		dl[j] = zero;
-	}
+	for(int j = 0; j < KS; j++) { d0[j] = zero; S0[j] = zero; G0[j] = zero; }
+	cx<R>* vb = buf + lane * (M + 1);
 #pragma unroll
 	for(int k = 0; k < M; k++) {
 		if(i0 + k < n_unk) {
-			cx<R> a = Fc[F_A * plane + k * 32 + lane], w = Fc[F_W * plane + k * 32 + lane];
+			const cx<R> a = Fc[F_A * plane + k * 32 + lane], rb = Fc[F_RB * plane + k * 32 + lane];
+			const cx<R> w = Fc[F_W * plane + k * 32 + lane], cc = Fc[F_C * plane + k * 32 + lane];
+			P = a * P;
+			S1 += w * P;
+			G1 += Cp * P;
 #pragma unroll
 			for(int j = 0; j < KS; j++) {
-				d[j] = a * d[j] + v[j][k];
-				v[j][k] = d[j];
-				acc[j] += w * d[j];
+				const cx<R> b = vb[j * PITCH + k] * rb;
+				vb[j * PITCH + k] = b;
+				d0[j] = a * d0[j] + b;
+				S0[j] += w * d0[j];
+				G0[j] += Cp * d0[j];
 			}
-		}
-		if(k == k_last) {
-#pragma unroll
-			for(int j = 0; j < KS; j++) dl[j] = d[j];
+			Cp = Cp * cc;
 		}
 	}
-	cx<R> fr[KS];
+	// One combine across the chunks (lanes): forward carries, Sherman-Morrison factor,
+	// backward carries.
+	cx<R> din[KS], xin[KS], fr[KS];
+	line_combine<R, KS>(P, d0, S0, S1, G0, G1, Cp, r0, rden, lane, din, xin, fr);
+	// Finish: forward values from the carry, then the backward sweep with the correction.
 #pragma unroll
-	for(int j = 0; j < KS; j++) {
+	for(int k = 0; k < M; k++) {
+		if(i0 + k < n_unk) {
+			const cx<R> a = Fc[F_A * plane + k * 32 + lane];
 #pragma unroll
-		for(int o = 16; o > 0; o >>= 1) acc[j] += shfl_xor_c(acc[j], o);
-		dl[j] = shfl_idx_c(dl[j], lane_last);
-		fr[j] = cvt<R>((cvt<double>(acc[j]) - r0 * cvt<double>(dl[j])) * rden);
-		A[j] = one;
-		B[j] = zero;
+			for(int j = 0; j < KS; j++) { din[j] = a * din[j] + vb[j * PITCH + k]; vb[j * PITCH + k] = din[j]; }
+		}
 	}
 #pragma unroll
 	for(int k = M - 1; k >= 0; k--) {
 		if(i0 + k < n_unk) {
-			cx<R> cc = Fc[F_C * plane + k * 32 + lane];
-#pragma unroll
-			for(int j = 0; j < KS; j++) { B[j] = cc * B[j] + v[j][k]; A[j] = cc * A[j]; }
-		}
-	}
-#pragma unroll
-	for(int o = 1; o < 32; o <<= 1) {
-#pragma unroll
-		for(int j = 0; j < KS; j++) {
-			cx<R> An = shfl_down_c(A[j], o), Bn = shfl_down_c(B[j], o);
-			if(lane + o < 32) { B[j] = A[j] * Bn + B[j]; A[j] = A[j] * An; }
-		}
-	}
-#pragma unroll
-	for(int j = 0; j < KS; j++) {
-		d[j] = shfl_down_c(B[j], 1);
-		if(lane == 31) d[j] = zero;
-	}
-#pragma unroll
-	for(int k = M - 1; k >= 0; k--) {
-		if(i0 + k < n_unk) {
-			cx<R> cc = Fc[F_C * plane + k * 32 + lane], cr = Fc[F_COR * plane + k * 32 + lane];
+			const cx<R> cc = Fc[F_C * plane + k * 32 + lane], cr = Fc[F_COR * plane + k * 32 + lane];
 #pragma unroll
 			for(int j = 0; j < KS; j++) {
-				d[j] = cc * d[j] + v[j][k];
-				buf[j * PITCH + lane * (M + 1) + k] = d[j] - fr[j] * cr;
+				xin[j] = cc * xin[j] + vb[j * PITCH + k];
+				vb[j * PITCH + k] = xin[j] - fr[j] * cr;
 			}
 		}
 	}
@@ -1515,56 +1533,44 @@ __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_xc(Geom G, 
 	}
 }
 
-// Column-parallel combine of the y-chunk maps of a block (32 columns x WY chunks, maps at
-// [j][chunk][column] in shared memory): warp w scans columns w, w + WY, ... with its lanes
-// indexing the chunks, so all warps work at once. sD receives, per chunk, the state entering
-// it from the line's start (reverse: from the line's end), starting from zero.
+// Whether k_solve_yc<M, KS, MAXT> keeps its chunk values in shared memory: the values
+// (KS*M*MAXT complex) and the combine arrays ((4 + 3 KS)*MAXT + 32 KS complex) within 224 KiB.
+__host__ __device__ constexpr bool yc_values_in_smem(int M, int KS, int MAXT, int csize) {
+	return ((long)KS * M * MAXT + (4L + 3L * KS) * MAXT + 32L * KS) * csize <= 224L * 1024;
+}
+
+// Combine of the y-chunk maps of a block (32 columns x WY chunks; shared arrays at
+// [chunk][column], per-slot arrays at [slot][chunk][column]): warp w combines columns
+// w, w + WY, ... with its lanes indexing the chunks (line_combine), and leaves per chunk the
+// forward and backward entering values in sD0 / sG0 and per column the Sherman-Morrison
+// factor in sF.
 template <typename R, int KS>
-__device__ __forceinline__ void ycol_scan(const cx<R>* sA, const cx<R>* sB, cx<R>* sD, int WY, int w, int lane,
-		bool reverse) {
+__device__ __forceinline__ void ycol_combine(const cx<R>* sP, const cx<R>* sS1, const cx<R>* sG1, const cx<R>* sCp,
+		cx<R>* sD0, const cx<R>* sS0, cx<R>* sG0, cx<R>* sF, int WY, int w, int lane, int ix0, int Nx,
+		const cx<double>* ls) {
 	const int SZ = WY * 32;
 	const cx<R> one = mk<R>(1, 0), zero = mk<R>(0, 0);
 	for(int col = w; col < 32; col += WY) {
+		if(ix0 + col >= Nx) continue;  // uniform across the warp
+		const bool ok = lane < WY;
+		const int e = lane * 32 + col;
+		const cx<R> P = ok ? sP[e] : one, S1 = ok ? sS1[e] : zero, G1 = ok ? sG1[e] : zero, Cp = ok ? sCp[e] : one;
+		cx<R> d0[KS], S0[KS], G0[KS], din[KS], xin[KS], fr[KS];
 #pragma unroll
 		for(int j = 0; j < KS; j++) {
-			const int ch = lane;  // chunk handled by this lane
-			cx<R> A = one, B = zero;
-			if(ch < WY) { A = sA[j * SZ + ch * 32 + col]; B = sB[j * SZ + ch * 32 + col]; }
-			if(!reverse) {
-#pragma unroll
-				for(int o = 1; o < 32; o <<= 1) {
-					cx<R> Ap = shfl_up_c(A, o), Bp = shfl_up_c(B, o);
-					if(lane >= o) { B = A * Bp + B; A = A * Ap; }
-				}
-				cx<R> D = shfl_up_c(B, 1);
-				if(lane == 0) D = zero;
-				if(ch < WY) sD[j * SZ + ch * 32 + col] = D;
-			}
-			else {
-#pragma unroll
-				for(int o = 1; o < 32; o <<= 1) {
-					cx<R> An = shfl_down_c(A, o), Bn = shfl_down_c(B, o);
-					if(lane + o < 32) { B = A * Bn + B; A = A * An; }
-				}
-				cx<R> D = shfl_down_c(B, 1);
-				if(lane == 31) D = zero;
-				if(ch < WY) sD[j * SZ + ch * 32 + col] = D;
-			}
+			d0[j] = ok ? sD0[j * SZ + e] : zero;
+			S0[j] = ok ? sS0[j * SZ + e] : zero;
+			G0[j] = ok ? sG0[j * SZ + e] : zero;
 		}
-	}
-}
-
-// Column totals of per-chunk values sP[j][chunk][column] into sF[j][column].
-template <typename R, int KS>
-__device__ __forceinline__ void ycol_sum(const cx<R>* sP, cx<R>* sF, int WY, int w, int lane) {
-	const int SZ = WY * 32;
-	for(int col = w; col < 32; col += WY) {
+		const cx<double> r0 = ls[(size_t)(ix0 + col) * 2], rden = ls[(size_t)(ix0 + col) * 2 + 1];
+		line_combine<R, KS>(P, d0, S0, S1, G0, G1, Cp, r0, rden, lane, din, xin, fr);
+		if(ok) {
 #pragma unroll
-		for(int j = 0; j < KS; j++) {
-			cx<R> v = lane < WY ? sP[j * SZ + lane * 32 + col] : mk<R>(0, 0);
+			for(int j = 0; j < KS; j++) { sD0[j * SZ + e] = din[j]; sG0[j * SZ + e] = xin[j]; }
+		}
+		if(lane == 0) {
 #pragma unroll
-			for(int o = 16; o > 0; o >>= 1) v += shfl_xor_c(v, o);
-			if(lane == 0) sF[j * 32 + col] = v;
+			for(int j = 0; j < KS; j++) sF[j * 32 + col] = fr[j];
 		}
 	}
 }
@@ -1572,8 +1578,9 @@ __device__ __forceinline__ void ycol_sum(const cx<R>* sP, cx<R>* sF, int WY, int
 // y-line solve fused with its right-hand side (KIND: explicit x half-step or y Woodbury term),
 // chunked parallel form: block = 32 adjacent columns (lanes, coalesced) x WY warps for KS
 // slots of one wavelength; warp w owns the rows [w*M, w*M+M) of the 32 lines for all KS
-// slots. Chunk maps are combined across warps through shared memory. MAXT: block size the
-// instance is compiled for (512, or 1024 for 32 warps of short chunks).
+// slots. One pass builds the chunk maps, one combine (ycol_combine) joins them across the
+// warps, one pass finishes the lines. MAXT: block size the instance is compiled for (512, or
+// 1024 for 32 warps of short chunks).
 template <typename R, int M, int KIND, int KS, int MAXT = 512>
 __global__ void __launch_bounds__(MAXT, NBPM_YC_MINB) k_solve_yc(Geom G, int slot0, int nch, const cx<R>* __restrict__ coef,
 		const cx<R>* __restrict__ fac, size_t plane, const cx<double>* __restrict__ lsc,
@@ -1589,115 +1596,99 @@ __global__ void __launch_bounds__(MAXT, NBPM_YC_MINB) k_solve_yc(Geom G, int slo
 	const int s0 = g * G.spg + ch * KS;
 	const int n_unk = Ny - 1;
 	const int SZ = WY * 32;
-	cx<R>* sA = reinterpret_cast<cx<R>*>(smem_raw);  // [KS][WY][32]
-	cx<R>* sB = sA + KS * SZ;
-	cx<R>* sD = sB + KS * SZ;
-	cx<R>* sP = sD + KS * SZ;
-	cx<R>* sL = sP + KS * SZ;                         // [KS][32]
-	cx<R>* sF = sL + KS * 32;                         // [KS][32]
+	cx<R>* sP = reinterpret_cast<cx<R>*>(smem_raw);  // [WY][32] each
+	cx<R>* sS1 = sP + SZ;
+	cx<R>* sG1 = sS1 + SZ;
+	cx<R>* sCp = sG1 + SZ;
+	cx<R>* sD0 = sCp + SZ;                            // [KS][WY][32] each
+	cx<R>* sS0 = sD0 + KS * SZ;
+	cx<R>* sG0 = sS0 + KS * SZ;
+	cx<R>* sF = sG0 + KS * SZ;                        // [KS][32]
+	// chunk values in shared memory ([KS][M][WY][32]) when they fit beside the combine arrays,
+	// else in registers
+	constexpr bool VS = yc_values_in_smem(M, KS, MAXT, (int)sizeof(cx<R>));
+	cx<R>* sV = sF + KS * 32;
 	const cx<R>* Fc = fac + ((size_t)g * 2 + c) * NFAC * plane;
 	const int i0 = w * M;
 	const cx<R> one = mk<R>(1, 0), zero = mk<R>(0, 0);
-	cx<double> r0 = mk(0.0, 0.0), rden = mk(0.0, 0.0);
-	if(col) {
-		const cx<double>* ls = lsc + (((size_t)g * 2 + c) * Nx + ix) * 2;
-		r0 = ls[0];
-		rden = ls[1];
-	}
 	const Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
 	const cx<R>* f0 = src + (size_t)s0 * 2 * N;
-	cx<R> v[KS][M];
-	cx<R> A[KS], B[KS];
+	// chunk pass: right-hand sides b (kept in v) and the chunk maps of line_combine
+	cx<R> v[VS ? 1 : KS][VS ? 1 : M];
+	auto V = [&](int j, int k) -> cx<R>& { return VS ? sV[((j * M + k) * WY + w) * 32 + lane] : v[VS ? 0 : j][VS ? 0 : k]; };
+	cx<R> d0[KS], S0[KS], G0[KS];
+	cx<R> P = one, S1 = zero, G1 = zero, Cp = one;
 #pragma unroll
-	for(int j = 0; j < KS; j++) { A[j] = one; B[j] = zero; }
+	for(int j = 0; j < KS; j++) { d0[j] = zero; S0[j] = zero; G0[j] = zero; }
 #pragma unroll
 	for(int k = 0; k < M; k++) {
-		int i = i0 + k;
-		bool ok = col && i < n_unk;
+		const int i = i0 + k;
 #pragma unroll
-		for(int j = 0; j < KS; j++) v[j][k] = zero;
-		if(ok) {
-			size_t q = (size_t)ix + (size_t)Nx * i;
-			cx<R> a = Fc[F_A * plane + q], rb = Fc[F_RB * plane + q];
+		for(int j = 0; j < KS; j++) V(j, k) = zero;
+		if(col && i < n_unk) {
+			const size_t q = (size_t)ix + (size_t)Nx * i;
+			const cx<R> a = Fc[F_A * plane + q], rb = Fc[F_RB * plane + q];
+			const cx<R> wv = Fc[F_W * plane + q], cc = Fc[F_C * plane + q];
 			cx<R> r[KS];
 			composite_m<R, KIND, KS>(st, c, ix, i, f0, r);
+			P = a * P;
+			S1 += wv * P;
+			G1 += Cp * P;
 #pragma unroll
 			for(int j = 0; j < KS; j++) {
-				cx<R> b = r[j] * rb;
-				v[j][k] = b;
-				B[j] = a * B[j] + b;
-				A[j] = a * A[j];
+				const cx<R> b = r[j] * rb;
+				V(j, k) = b;
+				d0[j] = a * d0[j] + b;
+				S0[j] += wv * d0[j];
+				G0[j] += Cp * d0[j];
 			}
+			Cp = Cp * cc;
 		}
 	}
+	{
+		const int e = w * 32 + lane;
+		sP[e] = P; sS1[e] = S1; sG1[e] = G1; sCp[e] = Cp;
 #pragma unroll
-	for(int j = 0; j < KS; j++) { sA[j * SZ + w * 32 + lane] = A[j]; sB[j * SZ + w * 32 + lane] = B[j]; }
+		for(int j = 0; j < KS; j++) { sD0[j * SZ + e] = d0[j]; sS0[j * SZ + e] = S0[j]; sG0[j * SZ + e] = G0[j]; }
+	}
 	__syncthreads();
-	ycol_scan<R, KS>(sA, sB, sD, WY, w, lane, false);
+	ycol_combine<R, KS>(sP, sS1, sG1, sCp, sD0, sS0, sG0, sF, WY, w, lane, blockIdx.x * 32, Nx,
+		lsc + ((size_t)g * 2 + c) * Nx * 2);
 	__syncthreads();
-	cx<R> d[KS], acc[KS];
+	if(!col) return;
+	cx<R> d[KS], x[KS], fr[KS];
 #pragma unroll
-	for(int j = 0; j < KS; j++) { d[j] = sD[j * SZ + w * 32 + lane]; acc[j] = zero; }
+	for(int j = 0; j < KS; j++) {
+		d[j] = sD0[j * SZ + w * 32 + lane];
+		x[j] = sG0[j * SZ + w * 32 + lane];
+		fr[j] = sF[j * 32 + lane];
+	}
 #pragma unroll
 	for(int k = 0; k < M; k++) {
-		int i = i0 + k;
-		if(col && i < n_unk) {
-			size_t q = (size_t)ix + (size_t)Nx * i;
-			cx<R> a = Fc[F_A * plane + q], wv = Fc[F_W * plane + q];
+		const int i = i0 + k;
+		if(i < n_unk) {
+			const cx<R> a = Fc[F_A * plane + (size_t)ix + (size_t)Nx * i];
 #pragma unroll
-			for(int j = 0; j < KS; j++) {
-				d[j] = a * d[j] + v[j][k];
-				v[j][k] = d[j];
-				acc[j] += wv * d[j];
-				if(i == n_unk - 1) sL[j * 32 + lane] = d[j];
-			}
+			for(int j = 0; j < KS; j++) { d[j] = a * d[j] + V(j, k); V(j, k) = d[j]; }
 		}
 	}
 #pragma unroll
-	for(int j = 0; j < KS; j++) sP[j * SZ + w * 32 + lane] = acc[j];
-	__syncthreads();
-	ycol_sum<R, KS>(sP, sF, WY, w, lane);  // sF = column totals
-	__syncthreads();
-	if(w == 0) {
-		for(int j = 0; j < KS; j++)
-			sF[j * 32 + lane] = cvt<R>((cvt<double>(sF[j * 32 + lane]) - r0 * cvt<double>(sL[j * 32 + lane])) * rden);
-	}
-#pragma unroll
-	for(int j = 0; j < KS; j++) { A[j] = one; B[j] = zero; }
-#pragma unroll
 	for(int k = M - 1; k >= 0; k--) {
-		int i = i0 + k;
-		if(col && i < n_unk) {
-			cx<R> cc = Fc[F_C * plane + (size_t)ix + (size_t)Nx * i];
-#pragma unroll
-			for(int j = 0; j < KS; j++) { B[j] = cc * B[j] + v[j][k]; A[j] = cc * A[j]; }
-		}
-	}
-#pragma unroll
-	for(int j = 0; j < KS; j++) { sA[j * SZ + w * 32 + lane] = A[j]; sB[j * SZ + w * 32 + lane] = B[j]; }
-	__syncthreads();
-	ycol_scan<R, KS>(sA, sB, sD, WY, w, lane, true);
-	__syncthreads();
-	cx<R> fr[KS];
-#pragma unroll
-	for(int j = 0; j < KS; j++) { fr[j] = sF[j * 32 + lane]; d[j] = sD[j * SZ + w * 32 + lane]; }
-#pragma unroll
-	for(int k = M - 1; k >= 0; k--) {
-		int i = i0 + k;
-		if(col && i < n_unk) {
-			size_t q = (size_t)ix + (size_t)Nx * i;
-			cx<R> cc = Fc[F_C * plane + q], cr = Fc[F_COR * plane + q];
+		const int i = i0 + k;
+		if(i < n_unk) {
+			const size_t q = (size_t)ix + (size_t)Nx * i;
+			const cx<R> cc = Fc[F_C * plane + q], cr = Fc[F_COR * plane + q];
 #pragma unroll
 			for(int j = 0; j < KS; j++) {
-				d[j] = cc * d[j] + v[j][k];
-				cx<R> x = d[j] - fr[j] * cr;
-				size_t off = (size_t)(s0 + j) * 2 * N + (size_t)c * N;
-				if(dst) dst[off + q] = x;
-				if(acc_out) acc_out[off + q] = acc_in[off + q] + x;
+				x[j] = cc * x[j] + V(j, k);
+				const cx<R> y = x[j] - fr[j] * cr;
+				const size_t off = (size_t)(s0 + j) * 2 * N + (size_t)c * N;
+				if(dst) dst[off + q] = y;
+				if(acc_out) acc_out[off + q] = acc_in[off + q] + y;
 				if(i == 0) {
-					size_t qe = (size_t)ix + (size_t)Nx * (Ny - 1);
-					if(dst) dst[off + qe] = x;
-					if(acc_out) acc_out[off + qe] = acc_in[off + qe] + x;
+					const size_t qe = (size_t)ix + (size_t)Nx * (Ny - 1);
+					if(dst) dst[off + qe] = y;
+					if(acc_out) acc_out[off + qe] = acc_in[off + qe] + y;
 				}
 			}
 		}

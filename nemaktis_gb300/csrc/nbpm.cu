@@ -1026,7 +1026,9 @@ struct Plan : PlanBase {
 			int nch = h.spg / L.KS;
 			L.grid = dim3((unsigned)((Gm.Nx + 31) / 32), (unsigned)(ng * nch * 2));
 			L.block = dim3(32, WY);
-			L.smem = (size_t)(4 * L.KS * WY * 32 + 2 * L.KS * 32) * sizeof(cx<R>);
+			L.smem = (size_t)((4 + 3 * L.KS) * WY * 32 + L.KS * 32) * sizeof(cx<R>);
+			if(yc_values_in_smem(L.M, L.KS, WY > 16 ? 1024 : 512, (int)sizeof(cx<R>)))
+				L.smem += (size_t)L.KS * L.M * WY * 32 * sizeof(cx<R>);  // chunk values
 			launch(wood ? "wood_solve_y" : "expl_solve_y", bytes, [&] {
 				if(!launch_solve_yc<R>(L, Gm, slot0, nch, C, fy_cur, sc.plane_y, ly_cur, rsrc,
 						dst, acc_in, acc_out))
