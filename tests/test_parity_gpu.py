@@ -48,6 +48,10 @@ CASES = {
     "long_y_lines": dict(dims=(10, 530, 4), q=((0.0, 0.0), (-0.06, 0.09))),
     "sequential_x_lines": dict(dims=(2100, 5, 3), q=((0.03, 0.0),)),
     "tall_mesh": dict(dims=(12, 200, 5), q=((0.0, 0.0), (0.05, 0.08))),
+    # many slots per wavelength (>= 4 chunks of two slots), Ny <= 3 with them
+    "many_slots": dict(dims=(40, 24, 6), q=((0.0, 0.0), (0.1, 0.0), (0.0, 0.1), (-0.07, 0.05), (0.05, -0.12))),
+    "many_slots_256": dict(dims=(256, 6, 4), q=((0.0, 0.0), (0.08, 0.0), (0.0, -0.08), (0.06, 0.06))),
+    "many_slots_ny3": dict(dims=(40, 3, 4), q=((0.0, 0.0), (0.1, 0.0), (0.0, 0.1), (-0.07, 0.05))),
 }
 
 
@@ -114,7 +118,7 @@ def test_uniform_director_closed_form_gpu(gpu):
 
 
 @pytest.mark.parametrize("name", ["random_tilted_q", "two_wavelengths_dispersion", "iso_layers_focus", "long_x_lines",
-                                  "tall_mesh"])
+                                  "tall_mesh", "many_slots", "many_slots_256", "many_slots_ny3"])
 def test_fp32_error_budget(gpu, name):
     kw = dict(CASES[name])
     dims = kw.pop("dims")
