@@ -1630,7 +1630,10 @@ __global__ void __launch_bounds__(MAXT, NBPM_YC_MINB) k_solve_yc(Geom G, int slo
 	cx<R> P = one, S1 = zero, G1 = zero, Cp = one;
 #pragma unroll
 	for(int j = 0; j < KS; j++) { d0[j] = zero; S0[j] = zero; G0[j] = zero; }
-#pragma unroll
+	// chunk values in shared memory need no compile-time row index: unroll by 2 in the 16-warp
+	// blocks (measured faster on GB300), fully in the 32-warp ones
+	constexpr int U1 = (VS && MAXT <= 512 && M >= 2) ? 2 : M;
+#pragma unroll U1
 	for(int k = 0; k < M; k++) {
 		const int i = i0 + k;
 #pragma unroll
@@ -1738,11 +1741,15 @@ __global__ void __launch_bounds__(256) k_solve_xw(Geom G, int slot0, int nch, co
 	const cx<R> one = mk<R>(1, 0), zero = mk<R>(0, 0);
 	const Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
 	const cx<R>* f0 = src + (size_t)s0 * 2 * N;
-	for(int e = threadIdx.x; e < n_unk; e += blockDim.x) {
-		cx<R> r[KS];
-		composite_m<R, KIND, KS>(st, c, e, iy, f0, r);
+#pragma unroll 1
+	for(int t = 0; t < M; t++) {  // fixed trip count: CH * M >= n_unk
+		const int e = threadIdx.x + CH * t;
+		if(e < n_unk) {
+			cx<R> r[KS];
+			composite_m<R, KIND, KS>(st, c, e, iy, f0, r);
 #pragma unroll
-		for(int j = 0; j < KS; j++) buf[j * PITCH + (e / M) * (M + 1) + e % M] = r[j];
+			for(int j = 0; j < KS; j++) buf[j * PITCH + (e / M) * (M + 1) + e % M] = r[j];
+		}
 	}
 	__syncthreads();
 	cx<R> v[KS][M];
@@ -1881,11 +1888,15 @@ __global__ void __launch_bounds__(256) k_solve_xw(Geom G, int slot0, int nch, co
 	__syncthreads();
 	for(int j = 0; j < KS; j++) {
 		const size_t off = (size_t)(s0 + j) * 2 * N + (size_t)c * N + (size_t)iy * Nx;
-		for(int e = threadIdx.x; e < Nx; e += blockDim.x) {
-			int ee = e == Nx - 1 ? 0 : e;
-			cx<R> x = buf[j * PITCH + (ee / M) * (M + 1) + ee % M];
-			if(dst) dst[off + e] = x;
-			if(acc_out) acc_out[off + e] = acc_in[off + e] + x;
+#pragma unroll 1
+		for(int t = 0; t <= M; t++) {
+			const int e = threadIdx.x + CH * t;
+			if(e < Nx) {
+				int ee = e == Nx - 1 ? 0 : e;
+				cx<R> x = buf[j * PITCH + (ee / M) * (M + 1) + ee % M];
+				if(dst) dst[off + e] = x;
+				if(acc_out) acc_out[off + e] = acc_in[off + e] + x;
+			}
 		}
 	}
 }
