@@ -225,11 +225,11 @@ def run_ours(args):
     # dram__bytes_write.sum), scaled to this workload's launch by the slots it processes; the
     # capture and its command are summarised under profiles/.
     PROF = "profiles/slab_main_stream_koehler_256x256x8_fp32.md"
-    TRAFFIC = {("config3", "fp32", "wood_solve_y"): (2 * (844.2e6 + 759.3e6) / 2, PROF),
-               ("config3", "fp32", "expl_solve_y"): (2 * 546.8e6, PROF),
-               ("config3", "fp32", "wood_solve_x"): (2 * (797.9e6 + 735.9e6) / 2, PROF),
-               ("config3", "fp32", "expl_solve_x"): (2 * 582.7e6, PROF),
-               ("config3", "fp32", "shift_fused"): (2 * 431.9e6, PROF)}
+    TRAFFIC = {("config3", "fp32", "wood_solve_y"): (2 * (738.6e6 + 724.1e6) / 2, PROF),
+               ("config3", "fp32", "expl_solve_y"): (2 * 532.2e6, PROF),
+               ("config3", "fp32", "wood_solve_x"): (2 * (735.3e6 + 723.1e6) / 2, PROF),
+               ("config3", "fp32", "expl_solve_x"): (2 * 534.5e6, PROF),
+               ("config3", "fp32", "shift_fused"): (2 * 432.4e6, PROF)}
     roof = None
     if prof:
         top = max(prof, key=lambda k: prof[k]["ms"])

@@ -102,8 +102,9 @@ int nbpm_plan_download(nbpm_plan* plan);
 int nbpm_plan_slab_ms(nbpm_plan* plan, double* ms);
 int nbpm_plan_destroy(nbpm_plan* plan);
 
-/* Runs the plan once without a graph, timing every kernel launch with CUDA events on the
- * plan's stream. Fills up to *n entries (kernel name, total ms, launches, algorithmic bytes
+/* Runs the plan once without a graph, timing every kernel launch with CUDA events, each
+ * kernel alone on the device (the device is synchronised before every launch, so the setup
+ * and main streams do not overlap as they do in execute). Fills up to *n entries (kernel name, total ms, launches, algorithmic bytes
  * moved by those launches) and sets *n to the number of entries written. */
 int nbpm_plan_profile(nbpm_plan* plan, char (*names)[48], double* ms, int* launches, double* bytes, int* n);
 

@@ -1741,15 +1741,11 @@ __global__ void __launch_bounds__(256) k_solve_xw(Geom G, int slot0, int nch, co
 	const cx<R> one = mk<R>(1, 0), zero = mk<R>(0, 0);
 	const Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
 	const cx<R>* f0 = src + (size_t)s0 * 2 * N;
-#pragma unroll 1
-	for(int t = 0; t < M; t++) {  // fixed trip count: CH * M >= n_unk
-		const int e = threadIdx.x + CH * t;
-		if(e < n_unk) {
-			cx<R> r[KS];
-			composite_m<R, KIND, KS>(st, c, e, iy, f0, r);
+	for(int e = threadIdx.x; e < n_unk; e += blockDim.x) {
+		cx<R> r[KS];
+		composite_m<R, KIND, KS>(st, c, e, iy, f0, r);
 #pragma unroll
-			for(int j = 0; j < KS; j++) buf[j * PITCH + (e / M) * (M + 1) + e % M] = r[j];
-		}
+		for(int j = 0; j < KS; j++) buf[j * PITCH + (e / M) * (M + 1) + e % M] = r[j];
 	}
 	__syncthreads();
 	cx<R> v[KS][M];
@@ -1888,15 +1884,11 @@ __global__ void __launch_bounds__(256) k_solve_xw(Geom G, int slot0, int nch, co
 	__syncthreads();
 	for(int j = 0; j < KS; j++) {
 		const size_t off = (size_t)(s0 + j) * 2 * N + (size_t)c * N + (size_t)iy * Nx;
-#pragma unroll 1
-		for(int t = 0; t <= M; t++) {
-			const int e = threadIdx.x + CH * t;
-			if(e < Nx) {
-				int ee = e == Nx - 1 ? 0 : e;
-				cx<R> x = buf[j * PITCH + (ee / M) * (M + 1) + ee % M];
-				if(dst) dst[off + e] = x;
-				if(acc_out) acc_out[off + e] = acc_in[off + e] + x;
-			}
+		for(int e = threadIdx.x; e < Nx; e += blockDim.x) {
+			int ee = e == Nx - 1 ? 0 : e;
+			cx<R> x = buf[j * PITCH + (ee / M) * (M + 1) + ee % M];
+			if(dst) dst[off + e] = x;
+			if(acc_out) acc_out[off + e] = acc_in[off + e] + x;
 		}
 	}
 }

@@ -207,6 +207,9 @@ struct Plan : PlanBase {
 	template <typename F>
 	void launch(const char* name, double bytes, F&& fn) {
 		if(profiling) {
+			// each kernel alone on the device: the launches before it (on either stream) have
+			// finished, so the events time this kernel without the overlap of the two streams
+			CK(cudaDeviceSynchronize());
 			ProfRec r{name, bytes, pool_event(), pool_event()};
 			CK(cudaEventRecord(r.a, cs));
 			fn();
@@ -219,6 +222,7 @@ struct Plan : PlanBase {
 	}
 	double last_slab_ms = 0;
 	size_t smem_limit = 0;
+	int nsm = 152;  // streaming multiprocessors of the device (queried at setup)
 	bool shift_fused = true;  // one-pass transition kernel (NBPM_SHIFT_FUSED=0: four passes)
 	bool factor_seq = false;  // one thread per line factorisation (NBPM_FACTOR_SEQ=1)
 	// line-solve configuration per sample (chunk sizes of the parallel kernels; 0 = sequential)
@@ -375,6 +379,7 @@ struct Plan : PlanBase {
 		int optin = 0;
 		CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
 		smem_limit = (size_t)optin;
+		CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
 		CK(cudaFuncSetAttribute(k_fft_lines<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit));
 		CK(cudaFuncSetAttribute(k_shift_fused<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 			(int)((size_t)4 * (SHT + 6) * (SHT + 6) * sizeof(cx<R>))));
@@ -447,6 +452,24 @@ struct Plan : PlanBase {
 			};
 			if(sc.Mx) { sc.KSx = pick_ks(sc.Mx, kmx); if(!sc.KSx) sc.Mx = 0; }
 			if(sc.My) { sc.KSy = pick_ks(sc.My, kmy); if(!sc.KSy) { sc.My = 0; sc.WY = 0; sc.y1024w = false; } }
+			// small grids leave SMs idle: fewer slots per thread, more blocks (unless the slots
+			// per thread are set through NBPM_KSX / NBPM_KSY)
+			{
+				const size_t want = 2 * (size_t)nsm;
+				auto xblocks = [&](int ks) { return (size_t)((h.s.Ny + 3) / 4) * 2 * ng * (h.spg / ks); };
+				auto yblocks = [&](int ks) { return (size_t)((h.s.Nx + 31) / 32) * 2 * ng * (h.spg / ks); };
+				if(sc.Mx && sc.WPLx == 1 && !std::getenv("NBPM_KSX"))
+					while(sc.KSx > 1 && xblocks(sc.KSx) < want && solve_pair_ok(sc.Mx, sc.KSx / 2)) sc.KSx /= 2;
+				if(sc.My && !std::getenv("NBPM_KSY"))
+					while(sc.KSy > 1 && yblocks(sc.KSy) < want && solve_pair_ok(sc.My, sc.KSy / 2)) sc.KSy /= 2;
+				if(sc.KSy < 2) sc.y1024w = false;
+				// FP64 (bound by the FP64 pipe) with short y-lines on few blocks: k_solve_ys with one
+				// slot per thread, measured 2x faster on GB300 for 64x64 meshes
+				if(sizeof(R) == sizeof(double) && sc.My && sc.My <= 4 && yblocks(1) < (size_t)nsm &&
+						!std::getenv("NBPM_YS")) {
+					sc.My = 0; sc.WY = 0; sc.ys = true; sc.KSy = 1;
+				}
+			}
 			if(kmy < 2) sc.y1024w = false;
 			if(const char* e = std::getenv("NBPM_YS")) if(std::atoi(e) == 1 && h.s.Ny > 3) { sc.My = 0; sc.WY = 0; }
 			if(sc.WPLx == 1 && (sc.Mx >= 32 || (sc.Mx && std::getenv("NBPM_XS") && std::atoi(std::getenv("NBPM_XS")) == 1))) {

@@ -48,7 +48,7 @@ void set_solve_smem_y_f64(int bytes);
 // (M, KS) pairs with compiled instances.
 inline bool solve_pair_ok(int M, int KS) {
 	switch(M) {
-		case 2: case 4: return KS == 2 || KS == 4;
+		case 2: case 4: return KS == 1 || KS == 2 || KS == 4;
 		case 8: return KS == 1 || KS == 2 || KS == 4;
 		case 16: return KS == 1 || KS == 2;
 		case 32: return KS == 1;

@@ -10,7 +10,7 @@ namespace nbpm {
 		return true; \
 	}
 #define NBPM_XC_PAIRS(KIND) \
-	NBPM_XC(2, 2, KIND) NBPM_XC(2, 4, KIND) NBPM_XC(4, 2, KIND) NBPM_XC(4, 4, KIND) \
+	NBPM_XC(2, 1, KIND) NBPM_XC(2, 2, KIND) NBPM_XC(2, 4, KIND) NBPM_XC(4, 1, KIND) NBPM_XC(4, 2, KIND) NBPM_XC(4, 4, KIND) \
 	NBPM_XC(8, 1, KIND) NBPM_XC(8, 2, KIND) NBPM_XC(8, 4, KIND) NBPM_XC(16, 1, KIND) NBPM_XC(16, 2, KIND) NBPM_XC(32, 1, KIND)
 
 template <>
@@ -25,7 +25,7 @@ bool launch_solve_xc<float>(const SolveLaunch& L, Geom G, int slot0, int nch, co
 #define NBPM_XA(MM, KK, KD) \
 	cudaFuncSetAttribute(k_solve_xc<float, MM, KD, KK>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 #define NBPM_XA_PAIRS(KIND) \
-	NBPM_XA(2, 2, KIND) NBPM_XA(2, 4, KIND) NBPM_XA(4, 2, KIND) NBPM_XA(4, 4, KIND) \
+	NBPM_XA(2, 1, KIND) NBPM_XA(2, 2, KIND) NBPM_XA(2, 4, KIND) NBPM_XA(4, 1, KIND) NBPM_XA(4, 2, KIND) NBPM_XA(4, 4, KIND) \
 	NBPM_XA(8, 1, KIND) NBPM_XA(8, 2, KIND) NBPM_XA(8, 4, KIND) NBPM_XA(16, 1, KIND) NBPM_XA(16, 2, KIND) NBPM_XA(32, 1, KIND)
 
 void set_solve_smem_x_f32(int bytes) {

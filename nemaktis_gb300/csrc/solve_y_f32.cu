@@ -10,7 +10,7 @@ namespace nbpm {
 		return true; \
 	}
 #define NBPM_YC_PAIRS(KIND) \
-	NBPM_YC(2, 2, KIND) NBPM_YC(2, 4, KIND) NBPM_YC(4, 2, KIND) NBPM_YC(4, 4, KIND) \
+	NBPM_YC(2, 1, KIND) NBPM_YC(2, 2, KIND) NBPM_YC(2, 4, KIND) NBPM_YC(4, 1, KIND) NBPM_YC(4, 2, KIND) NBPM_YC(4, 4, KIND) \
 	NBPM_YC(8, 1, KIND) NBPM_YC(8, 2, KIND) NBPM_YC(8, 4, KIND) NBPM_YC(16, 1, KIND) NBPM_YC(16, 2, KIND) NBPM_YC(32, 1, KIND)
 
 template <>
@@ -49,7 +49,7 @@ bool launch_solve_yc<float>(const SolveLaunch& L, Geom G, int slot0, int nch, co
 #define NBPM_YA(MM, KK, KD) \
 	cudaFuncSetAttribute(k_solve_yc<float, MM, KD, KK>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 #define NBPM_YA_PAIRS(KIND) \
-	NBPM_YA(2, 2, KIND) NBPM_YA(2, 4, KIND) NBPM_YA(4, 2, KIND) NBPM_YA(4, 4, KIND) \
+	NBPM_YA(2, 1, KIND) NBPM_YA(2, 2, KIND) NBPM_YA(2, 4, KIND) NBPM_YA(4, 1, KIND) NBPM_YA(4, 2, KIND) NBPM_YA(4, 4, KIND) \
 	NBPM_YA(8, 1, KIND) NBPM_YA(8, 2, KIND) NBPM_YA(8, 4, KIND) NBPM_YA(16, 1, KIND) NBPM_YA(16, 2, KIND) NBPM_YA(32, 1, KIND)
 
 void set_solve_smem_y_f32(int bytes) {
