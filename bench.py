@@ -48,6 +48,19 @@ def dist_env():
     return world, rank, local
 
 
+def replica_aggregate(vs, steps, dev_ms, world, device):
+    """Replicas (one process per GPU, the same workload on each): the step time is the slowest
+    rank's (max over ranks), and the value is the voxel-steps of all ranks over that time.
+    Returns (max ms, voxel-steps/s). With world == 1 no collective is made."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        tt = torch.tensor([dev_ms], dtype=torch.float64, device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        dev_ms = float(tt.item())
+    return dev_ms, vs * steps * world / (dev_ms / 1e3)
+
+
 class Clocks:
     """nvidia-smi sampling during the timed region."""
 
@@ -178,13 +191,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     clocks = clk.stop()
-    dev_ms = float(np.sum(ms))
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([dev_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        dev_ms = float(tt.item())
-    value = vs * args.steps * world / (dev_ms / 1e3)
+    dev_ms, value = replica_aggregate(vs, args.steps, float(np.sum(ms)), world, "cuda")
     plan.download()
     out32 = [b["E"].copy() for b in bufs]
     if args.only_value:
