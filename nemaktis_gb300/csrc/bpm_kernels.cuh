@@ -2494,7 +2494,9 @@ __global__ void k_phase_sync(Geom G, int slot0, const cx<R>* __restrict__ CA, co
 // built on sqrt(eps_tr) at iz = 0.
 template <typename R>
 __global__ void k_init_fields(Geom G, int slot0, const GroupParams* __restrict__ gps, const R* __restrict__ Q0,
-		int beam_type, double waist, double dx, double dy, cx<R>* F) {
+		int beam_type, double waist, double dx, double dy, double cpol1, double spol1, cx<R>* F) {
+	// arithmetic in the plan's precision (FP32 mode: FP32, within its error budget)
+	using T = R;
 	int p = blockIdx.x * blockDim.x + threadIdx.x;
 	if(p >= G.N) return;
 	int s = blockIdx.y;
@@ -2502,39 +2504,43 @@ __global__ void k_init_fields(Geom G, int slot0, const GroupParams* __restrict__
 	int gs = slot0 + s;
 	int g = gs / G.spg - slot0 / G.spg;
 	int pol = gs % 2;
-	const double PI_REF = 3.1415926535897932;
-	double th = 0.5 * PI_REF * pol;
-	double x = ((p % Nx) - (Nx - 1) / 2.) * dx, y = ((p / Nx) - (Ny - 1) / 2.) * dy;
-	double amp = beam_type == 1 ? exp(-(x * x + y * y) / (2 * waist * waist)) : 1.0;
-	double ex = cos(th) * amp, ey = sin(th) * amp;
+	// polarisation (cos, sin)(pi/2 * pol); the pol = 1 values come from the host's libm
+	const T cth = pol ? (T)cpol1 : (T)1, sth = pol ? (T)spol1 : (T)0;
+	T amp = 1;
+	if(beam_type == 1) {
+		const T x = (T)(((p % Nx) - (Nx - 1) / 2.) * dx), y = (T)(((p / Nx) - (Ny - 1) / 2.) * dy), w = (T)waist;
+		amp = exp(-(x * x + y * y) / (2 * w * w));
+	}
+	const T ex = cth * amp, ey = sth * amp;
 	const R* Q = Q0 + (size_t)g * NQ * N;
-	double nxx = Q[Q_XXS * N + p], nyy = Q[Q_YYS * N + p], nxy = Q[Q_XYS * N + p];
-	double n = gps[g].nin;
-	double det = (n + nxx) * (n + nyy) - nxy * nxy;
-	double a = 2 * n * (n + nyy) / det * ex - 2 * n * nxy / det * ey;
-	double b = -2 * n * nxy / det * ex + 2 * n * (n + nxx) / det * ey;
+	const T nxx = Q[Q_XXS * N + p], nyy = Q[Q_YYS * N + p], nxy = Q[Q_XYS * N + p];
+	const T n = (T)gps[g].nin;
+	const T det = (n + nxx) * (n + nyy) - nxy * nxy;
+	const T a = 2 * n * (n + nyy) / det * ex - 2 * n * nxy / det * ey;
+	const T b = -2 * n * nxy / det * ex + 2 * n * (n + nxx) / det * ey;
 	F[(size_t)s * 2 * N + p] = mk<R>((R)a, 0);
 	F[(size_t)s * 2 * N + N + p] = mk<R>((R)b, 0);
 }
 
-// Output Fresnel operator at iz = Nz-1 (FresnelOperator.cpp:45-69).
+// Output Fresnel operator at iz = Nz-1 (FresnelOperator.cpp:45-69), in the plan's precision.
 template <typename R>
 __global__ void k_fresnel_out(Geom G, int slot0, const GroupParams* __restrict__ gps, const R* __restrict__ QL,
 		cx<R>* F) {
+	using T = R;
 	int p = blockIdx.x * blockDim.x + threadIdx.x;
 	if(p >= G.N) return;
 	int s = blockIdx.y;
 	int N = G.N;
 	int g = (slot0 + s) / G.spg - slot0 / G.spg;
 	const R* Q = QL + (size_t)g * NQ * N;
-	double nxx = Q[Q_XXS * N + p], nyy = Q[Q_YYS * N + p], nxy = Q[Q_XYS * N + p];
-	double n = gps[g].nout_fresnel;
-	double det = (n + nxx) * (n + nyy) - nxy * nxy;
-	double axx = 2. * (1. - n * (n + nyy) / det), ayy = 2. * (1. - n * (n + nxx) / det), axy = 2. * (n * nxy / det);
+	const T nxx = Q[Q_XXS * N + p], nyy = Q[Q_YYS * N + p], nxy = Q[Q_XYS * N + p];
+	const T n = (T)gps[g].nout_fresnel;
+	const T det = (n + nxx) * (n + nyy) - nxy * nxy;
+	const T axx = 2 * (1 - n * (n + nyy) / det), ayy = 2 * (1 - n * (n + nxx) / det), axy = 2 * (n * nxy / det);
 	cx<R>* f = F + (size_t)s * 2 * N + p;
-	cx<double> a = cvt<double>(f[0]), b = cvt<double>(f[N]);
-	f[0] = cvt<R>(axx * a + axy * b);
-	f[N] = cvt<R>(ayy * b + axy * a);
+	const cx<R> a = f[0], b = f[N];
+	f[0] = axx * a + axy * b;
+	f[N] = ayy * b + axy * a;
 }
 
 template <typename R>

@@ -705,8 +705,9 @@ struct Plan : PlanBase {
 		});
 		if(h.s.beam_type != 2) {
 			launch("init_fields", ps.field_pts * 2 * sc + (double)N * ng * 3 * 8, [&] {
+				const double th1 = 0.5 * 3.1415926535897932;  // polarisation angle of pol = 1 (BPMIteration.cpp:87-109)
 				k_init_fields<R><<<pgrid(N, nsl), 256, 0, cs>>>(Gm, slot0, gps, ps.Qr[0], h.s.beam_type,
-					h.s.waist, h.s.dx, h.s.dy, ps.Fp);
+					h.s.waist, h.s.dx, h.s.dy, std::cos(th1), std::sin(th1), ps.Fp);
 			});
 		}
 		else {
