@@ -175,6 +175,8 @@ struct ScreenParams {
 template <typename R>
 __global__ void k_screen_filter(cx<R>* F, ScreenParams sp, int g0, const double* __restrict__ wl,
 		const double* __restrict__ nout, const double* __restrict__ qv) {
+	// transfer matrices in the plan's precision (FP32 mode: FP32, within its error budget)
+	using T = R;
 	int p = blockIdx.x * blockDim.x + threadIdx.x;
 	int Nx = sp.Nx, Ny = sp.Ny, N = Nx * Ny;
 	if(p >= N) return;
@@ -182,67 +184,71 @@ __global__ void k_screen_filter(cx<R>* F, ScreenParams sp, int g0, const double*
 	int g = gq / sp.Nq, q = gq % sp.Nq;
 	int ix = p % Nx, iy = p / Nx;
 	const double PI_REF = 3.1415926535897932;
-	double lam = wl[g0 + g];
-	double k0 = 2 * PI_REF / lam;
-	double kx = (ix < double(Nx / 2.)) ? 2 * PI_REF * ix / (sp.dx * Nx) : -2 * PI_REF * (Nx - ix) / (sp.dx * Nx);
-	double ky = (iy < double(Ny / 2.)) ? 2 * PI_REF * iy / (sp.dy * Ny) : -2 * PI_REF * (Ny - iy) / (sp.dy * Ny);
-	double qx0 = qv[2 * q], qy0 = qv[2 * q + 1];
-	double q0 = kx / k0 + qx0, q1 = ky / k0 + qy0;
-	double qn = sqrt(q0 * q0 + q1 * q1);
-	double qn2 = qn * qn;
-	double q0s = sqrt(qx0 * qx0 + qy0 * qy0);
-	cx<double> M[2][2] = {{mk(0.0, 0.0), mk(0.0, 0.0)}, {mk(0.0, 0.0), mk(0.0, 0.0)}};
-	if(qn < sp.NA) {
-		double n_out = nout[g0 + g];
-		cx<double> T[4][4];
-		for(int a = 0; a < 4; a++) for(int b = 0; b < 4; b++) T[a][b] = mk(a == b ? 1.0 : 0.0, 0.0);
+	const T k0 = (T)(2 * PI_REF / wl[g0 + g]);
+	const double kx = (ix < double(Nx / 2.)) ? 2 * PI_REF * ix / (sp.dx * Nx) : -2 * PI_REF * (Nx - ix) / (sp.dx * Nx);
+	const double ky = (iy < double(Ny / 2.)) ? 2 * PI_REF * iy / (sp.dy * Ny) : -2 * PI_REF * (Ny - iy) / (sp.dy * Ny);
+	// the aperture test in FP64 in both modes, so that no mode near |q| = NA flips in or out
+	const double k0d = 2 * PI_REF / wl[g0 + g];
+	const double q0d = (double)kx / k0d + qv[2 * q], q1d = (double)ky / k0d + qv[2 * q + 1];
+	const double qnd = sqrt(q0d * q0d + q1d * q1d);
+	const T qx0 = (T)qv[2 * q], qy0 = (T)qv[2 * q + 1];
+	const T q0 = (T)q0d, q1 = (T)q1d;
+	const T qn = (T)qnd;
+	const T qn2 = qn * qn;
+	const T q0s = sqrt(qx0 * qx0 + qy0 * qy0);
+	const cx<T> zero = mk<T>(0, 0);
+	cx<T> M[2][2] = {{zero, zero}, {zero, zero}};
+	if(qnd < sp.NA) {
+		const T n_out = (T)nout[g0 + g];
+		cx<T> TM[4][4];
+		for(int a = 0; a < 4; a++) for(int b = 0; b < 4; b++) TM[a][b] = mk<T>(a == b ? 1 : 0, 0);
 		for(int l = 0; l < sp.n_iso; l++) {
-			double np = sp.index[l];
-			double nn = (l + 1 < sp.n_iso) ? sp.index[l + 1] : n_out;
-			double neff = sqrt(np * np - qn2), nneff = sqrt(nn * nn - qn2);
-			double im[2][2] = {{neff + q0 * q0 / neff, q0 * q1 / neff}, {q0 * q1 / neff, neff + q1 * q1 / neff}};
-			double ni[2][2] = {{(1 - (q0 / nn) * (q0 / nn)) / nneff, -q0 * q1 / (nn * nn * nneff)},
+			const T np = (T)sp.index[l];
+			const T nn = (l + 1 < sp.n_iso) ? (T)sp.index[l + 1] : n_out;
+			const T neff = sqrt(np * np - qn2), nneff = sqrt(nn * nn - qn2);
+			const T im[2][2] = {{neff + q0 * q0 / neff, q0 * q1 / neff}, {q0 * q1 / neff, neff + q1 * q1 / neff}};
+			const T ni[2][2] = {{(1 - (q0 / nn) * (q0 / nn)) / nneff, -q0 * q1 / (nn * nn * nneff)},
 				{-q0 * q1 / (nn * nn * nneff), (1 - (q1 / nn) * (q1 / nn)) / nneff}};
-			double tp[2][2], tm[2][2];
+			T tp[2][2], tm[2][2];
 			for(int a = 0; a < 2; a++) for(int b = 0; b < 2; b++)
-				tp[a][b] = 0.5 * ((a == b ? 1. : 0.) + ni[a][0] * im[0][b] + ni[a][1] * im[1][b]);
-			for(int a = 0; a < 2; a++) for(int b = 0; b < 2; b++) tm[a][b] = (a == b ? 1. : 0.) - tp[a][b];
-			double ph = (neff - sqrt(np * np - q0s)) * k0 * sp.thick[l];
-			cx<double> gg = mk(cos(ph), sin(ph)), gc = conj(gg);
-			cx<double> Lm[4][4];
+				tp[a][b] = (T)0.5 * ((a == b ? (T)1 : (T)0) + ni[a][0] * im[0][b] + ni[a][1] * im[1][b]);
+			for(int a = 0; a < 2; a++) for(int b = 0; b < 2; b++) tm[a][b] = (a == b ? (T)1 : (T)0) - tp[a][b];
+			const T ph = (neff - sqrt(np * np - q0s)) * k0 * (T)sp.thick[l];
+			const cx<T> gg = mk<T>(cos(ph), sin(ph)), gc = conj(gg);
+			cx<T> Lm[4][4];
 			for(int a = 0; a < 2; a++) for(int b = 0; b < 2; b++) {
 				Lm[a][b] = tp[a][b] * gg;
 				Lm[a][b + 2] = tm[a][b] * gc;
 				Lm[a + 2][b] = tm[a][b] * gg;
 				Lm[a + 2][b + 2] = tp[a][b] * gc;
 			}
-			cx<double> T2[4][4];
+			cx<T> T2[4][4];
 			for(int a = 0; a < 4; a++) for(int b = 0; b < 4; b++) {
-				cx<double> s = mk(0.0, 0.0);
-				for(int c = 0; c < 4; c++) s += Lm[a][c] * T[c][b];
+				cx<T> s = zero;
+				for(int c = 0; c < 4; c++) s += Lm[a][c] * TM[c][b];
 				T2[a][b] = s;
 			}
-			for(int a = 0; a < 4; a++) for(int b = 0; b < 4; b++) T[a][b] = T2[a][b];
+			for(int a = 0; a < 4; a++) for(int b = 0; b < 4; b++) TM[a][b] = T2[a][b];
 		}
-		cx<double> det = T[2][2] * T[3][3] - T[2][3] * T[3][2];
-		cx<double> tmp[2][2] = {{cdiv(T[3][3], det), cdiv(-T[2][3], det)}, {cdiv(-T[3][2], det), cdiv(T[2][2], det)}};
-		double ph = (sqrt(n_out * n_out - qn2) - sqrt(n_out * n_out - q0s)) * k0 * sp.z_foc;
-		cx<double> e = mk(cos(ph), sin(ph));
+		const cx<T> det = TM[2][2] * TM[3][3] - TM[2][3] * TM[3][2];
+		const cx<T> tmp[2][2] = {{cdiv(TM[3][3], det), cdiv(-TM[2][3], det)}, {cdiv(-TM[3][2], det), cdiv(TM[2][2], det)}};
+		const T ph = (sqrt(n_out * n_out - qn2) - sqrt(n_out * n_out - q0s)) * k0 * (T)sp.z_foc;
+		const cx<T> e = mk<T>(cos(ph), sin(ph));
 		for(int a = 0; a < 2; a++) for(int b = 0; b < 2; b++) {
-			cx<double> s = mk(0.0, 0.0);
-			for(int c = 0; c < 2; c++) for(int d = 0; d < 2; d++) s += T[a][c + 2] * tmp[c][d] * T[d + 2][b];
-			M[a][b] = (T[a][b] - s) * e;
+			cx<T> s = zero;
+			for(int c = 0; c < 2; c++) for(int d = 0; d < 2; d++) s += TM[a][c + 2] * tmp[c][d] * TM[d + 2][b];
+			M[a][b] = (TM[a][b] - s) * e;
 		}
 	}
-	double inv = 1.0 / double(N);
+	const T inv = (T)(1.0 / double(N));
 	for(int pol = 0; pol < 2; pol++) {
 		size_t slot = (size_t)pol + 2 * ((size_t)q + (size_t)sp.Nq * g);
 		cx<R>* f = F + slot * 2 * N + p;
-		cx<double> a = cvt<double>(f[0]), b = cvt<double>(f[N]);
-		cx<double> t0 = M[0][0] * a + M[0][1] * b;
-		cx<double> t1 = M[1][0] * a + M[1][1] * b;
-		f[0] = cvt<R>(t0 * inv);
-		f[N] = cvt<R>(t1 * inv);
+		const cx<T> a = f[0], b = f[N];
+		const cx<T> t0 = M[0][0] * a + M[0][1] * b;
+		const cx<T> t1 = M[1][0] * a + M[1][1] * b;
+		f[0] = t0 * inv;
+		f[N] = t1 * inv;
 	}
 }
 
