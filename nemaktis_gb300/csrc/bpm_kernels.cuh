@@ -1132,7 +1132,7 @@ template <typename T>
 __device__ __forceinline__ Aff<T> shfl_down_a(const Aff<T>& X, int o) { return Aff<T>{shfl_down_c(X.A, o), shfl_down_c(X.B, o)}; }
 
 template <typename S, int DIRN>
-__global__ void __launch_bounds__(256) k_factor_chunked(Geom G, int ngroups, int chunkMx, int chunksX, int W,
+__global__ void __launch_bounds__(DIRN == 1 ? 512 : 256) k_factor_chunked(Geom G, int ngroups, int chunkMx, int chunksX, int W,
 		const cx<S>* __restrict__ diag, cx<S>* __restrict__ fac, size_t plane, cx<double>* __restrict__ lsc) {
 	typedef S T;
 	const int Nx = G.Nx, Ny = G.Ny, N = G.N;

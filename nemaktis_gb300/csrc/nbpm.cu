@@ -381,6 +381,8 @@ struct Plan : PlanBase {
 		smem_limit = (size_t)optin;
 		CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
 		CK(cudaFuncSetAttribute(k_fft_lines<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit));
+		CK(cudaFuncSetAttribute(k_factor_chunked<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			(int)((size_t)16 * 32 * 8 * sizeof(cx<R>) + 64 * sizeof(cx<R>))));
 		CK(cudaFuncSetAttribute(k_shift_fused<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 			(int)((size_t)4 * (SHT + 6) * (SHT + 6) * sizeof(cx<R>))));
 		if(const char* e = std::getenv("NBPM_SHIFT_FUSED")) shift_fused = std::atoi(e) != 0;
@@ -766,7 +768,8 @@ struct Plan : PlanBase {
 				});
 			}
 			else {
-				const int LT = 4, WF = 8;
+				// y factorisation: 8 chunk warps per 32 columns, 16 when the grid leaves SMs idle
+				const int LT = 4, WF = ((Nx + 31) / 32) * 2 * ng < nsm && Ny - 1 >= 256 ? 16 : 8;
 				launch("factor_x", fb, [&] {
 					k_factor_chunked<R, 0><<<dim3((unsigned)((Ny + LT - 1) / LT), (unsigned)(ng * 2)), dim3(32, LT), 0, cs>>>(
 						Gm, ng, scf.Mx, 32 * scf.WPLx, 1, ps.Dg, fx, scf.plane_x, lx);
