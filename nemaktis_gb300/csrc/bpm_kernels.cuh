@@ -1438,7 +1438,8 @@ template <typename R, int M, int KIND, int KS>
 #endif
 __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_xc(Geom G, int slot0, int nch, const cx<R>* __restrict__ coef,
 		const cx<R>* __restrict__ fac, size_t plane, const cx<double>* __restrict__ lsc,
-		const cx<R>* __restrict__ src, cx<R>* __restrict__ dst, const cx<R>* acc_in, cx<R>* acc_out) {
+		const cx<R>* __restrict__ src, cx<R>* __restrict__ dst, const cx<R>* acc_in, cx<R>* acc_out,
+		const cx<R>* acc_in2) {
 	extern __shared__ unsigned char smem_raw[];
 	const int LT = blockDim.x / 32;
 	const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
@@ -1537,7 +1538,7 @@ __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_xc(Geom G, 
 				int ee = e == Nx - 1 ? 0 : e;
 				cx<R> x = buf[j * PITCH + (ee / M) * (M + 1) + ee % M];
 				if(dst) dst[off + e] = x;
-				if(acc_out) acc_out[off + e] = acc_in[off + e] + x;
+				if(acc_out) acc_out[off + e] = (acc_in2 ? acc_in[off + e] + acc_in2[off + e] : acc_in[off + e]) + x;
 			}
 		}
 	}
@@ -1594,7 +1595,8 @@ __device__ __forceinline__ void ycol_combine(const cx<R>* sP, const cx<R>* sS1, 
 template <typename R, int M, int KIND, int KS, int MAXT = 512>
 __global__ void __launch_bounds__(MAXT, NBPM_YC_MINB) k_solve_yc(Geom G, int slot0, int nch, const cx<R>* __restrict__ coef,
 		const cx<R>* __restrict__ fac, size_t plane, const cx<double>* __restrict__ lsc,
-		const cx<R>* __restrict__ src, cx<R>* __restrict__ dst, const cx<R>* acc_in, cx<R>* acc_out) {
+		const cx<R>* __restrict__ src, cx<R>* __restrict__ dst, const cx<R>* acc_in, cx<R>* acc_out,
+		const cx<R>* acc_in2) {
 	extern __shared__ unsigned char smem_raw[];
 	const int WY = blockDim.y;
 	const int lane = threadIdx.x, w = threadIdx.y;
@@ -1697,11 +1699,11 @@ __global__ void __launch_bounds__(MAXT, NBPM_YC_MINB) k_solve_yc(Geom G, int slo
 				const cx<R> y = x[j] - fr[j] * cr;
 				const size_t off = (size_t)(s0 + j) * 2 * N + (size_t)c * N;
 				if(dst) dst[off + q] = y;
-				if(acc_out) acc_out[off + q] = acc_in[off + q] + y;
+				if(acc_out) acc_out[off + q] = (acc_in2 ? acc_in[off + q] + acc_in2[off + q] : acc_in[off + q]) + y;
 				if(i == 0) {
 					const size_t qe = (size_t)ix + (size_t)Nx * (Ny - 1);
 					if(dst) dst[off + qe] = y;
-					if(acc_out) acc_out[off + qe] = acc_in[off + qe] + y;
+					if(acc_out) acc_out[off + qe] = (acc_in2 ? acc_in[off + qe] + acc_in2[off + qe] : acc_in[off + qe]) + y;
 				}
 			}
 		}

@@ -965,8 +965,15 @@ struct Plan : PlanBase {
 
 	// Fused right-hand side + chunked line solve. wood = false: explicit half-step of the other
 	// direction; wood = true: Woodbury term. dst may be null (t not needed afterwards).
+	// Whether the fused solve of direction dirn runs k_solve_xc / k_solve_yc, the kernels that take
+	// a second accumulator input.
+	bool solve_takes_acc2(const SolveCfg& sc, int dirn) const {
+		return dirn == 0 ? (sc.Mx > 0 && !sc.xg && sc.WPLx == 1 && !sc.xs) : (sc.My > 0 && !sc.ys);
+	}
+
 	void rec_solve_fused(int dirn, bool wood, SampleHost& h, const Geom& Gm, int slot0, int nsl, int ng,
-			const cx<R>* C, const cx<R>* src, cx<R>* dst, const cx<R>* acc_in, cx<R>* acc_out) {
+			const cx<R>* C, const cx<R>* src, cx<R>* dst, const cx<R>* acc_in, cx<R>* acc_out,
+			const cx<R>* acc_in2 = nullptr) {
 		const SolveCfg& sc = scfg[h.index];
 		const double sz = sizeof(cx<R>);
 		double fp = (double)Gm.N * nsl * 2 * sz;
@@ -1014,7 +1021,7 @@ struct Plan : PlanBase {
 			L.smem = (size_t)LT * L.KS * 32 * (L.M + 1) * sizeof(cx<R>);
 			launch(wood ? "wood_solve_x" : "expl_solve_x", bytes, [&] {
 				if(!launch_solve_xc<R>(L, Gm, slot0, nch, C, fx_cur, sc.plane_x, lx_cur, src,
-						dst, acc_in, acc_out))
+						dst, acc_in, acc_out, acc_in2))
 					throw BackendError(E_INTERNAL, "no x-solve instance");
 			});
 		}
@@ -1058,7 +1065,7 @@ struct Plan : PlanBase {
 				L.smem += (size_t)L.KS * L.M * WY * 32 * sizeof(cx<R>);  // chunk values
 			launch(wood ? "wood_solve_y" : "expl_solve_y", bytes, [&] {
 				if(!launch_solve_yc<R>(L, Gm, slot0, nch, C, fy_cur, sc.plane_y, ly_cur, rsrc,
-						dst, acc_in, acc_out))
+						dst, acc_in, acc_out, acc_in2))
 					throw BackendError(E_INTERNAL, "no y-solve instance");
 			});
 		}
@@ -1098,9 +1105,17 @@ struct Plan : PlanBase {
 					k_copy<R><<<(unsigned)((n + 255) / 256), 256, 0, cs>>>(n, Tb, Fp);
 				});
 			}
+			// Two Woodbury iterates with k_solve_xc / k_solve_yc: the first writes t1 only and the
+			// second forms F = (t0 + t1) + t2, the same sums in the same order as accumulating after
+			// each iterate, without the first pass over F.
+			const bool acc2 = fused && Nw == 2 && solve_takes_acc2(cfg, dirn);
 			for(int it = 1; it <= Nw; it++) {
 				const cx<R>* ai = it == 1 ? Tb : Fp;
-				if(fused) {
+				if(acc2) {
+					if(it == 1) rec_solve_fused(dirn, true, h, Gm, slot0, nsl, ng, C, cur, oth, nullptr, nullptr);
+					else rec_solve_fused(dirn, true, h, Gm, slot0, nsl, ng, C, cur, nullptr, Tb, Fp, cur);
+				}
+				else if(fused) {
 					rec_solve_fused(dirn, true, h, Gm, slot0, nsl, ng, C, cur, it == Nw ? nullptr : oth, ai, Fp);
 				}
 				else {

@@ -15,13 +15,16 @@ struct SolveLaunch {
 	cudaStream_t stream;
 };
 
-// Returns false if (M, KS) has no compiled instance.
+// Returns false if (M, KS) has no compiled instance. ai2 (xc / yc only): a second accumulator
+// input, ao = (ai + ai2) + x.
 template <typename R>
 bool launch_solve_xc(const SolveLaunch& L, Geom G, int slot0, int nch, const cx<R>* coef, const cx<R>* fac,
-	size_t plane, const cx<double>* lsc, const cx<R>* src, cx<R>* dst, const cx<R>* ai, cx<R>* ao);
+	size_t plane, const cx<double>* lsc, const cx<R>* src, cx<R>* dst, const cx<R>* ai, cx<R>* ao,
+	const cx<R>* ai2 = nullptr);
 template <typename R>
 bool launch_solve_yc(const SolveLaunch& L, Geom G, int slot0, int nch, const cx<R>* coef, const cx<R>* fac,
-	size_t plane, const cx<double>* lsc, const cx<R>* src, cx<R>* dst, const cx<R>* ai, cx<R>* ao);
+	size_t plane, const cx<double>* lsc, const cx<R>* src, cx<R>* dst, const cx<R>* ai, cx<R>* ao,
+	const cx<R>* ai2 = nullptr);
 template <typename R>
 bool launch_solve_xg(const SolveLaunch& L, Geom G, int slot0, const cx<R>* coef, const cx<R>* fac, size_t plane,
 	const cx<double>* lsc, const cx<R>* src, cx<R>* dst, const cx<R>* ai, cx<R>* ao);

@@ -6,7 +6,7 @@ namespace nbpm {
 #define NBPM_XC(MM, KK, KD) \
 	if(L.M == MM && L.KS == KK && L.kind == KD) { \
 		k_solve_xc<float, MM, KD, KK><<<L.grid, L.block, L.smem, L.stream>>>(G, slot0, nch, coef, fac, plane, lsc, \
-			src, dst, ai, ao); \
+			src, dst, ai, ao, ai2); \
 		return true; \
 	}
 #define NBPM_XC_PAIRS(KIND) \
@@ -16,7 +16,7 @@ namespace nbpm {
 template <>
 bool launch_solve_xc<float>(const SolveLaunch& L, Geom G, int slot0, int nch, const cx<float>* coef,
 		const cx<float>* fac, size_t plane, const cx<double>* lsc, const cx<float>* src, cx<float>* dst,
-		const cx<float>* ai, cx<float>* ao) {
+		const cx<float>* ai, cx<float>* ao, const cx<float>* ai2) {
 	NBPM_XC_PAIRS(ST_EXPL_Y)
 	NBPM_XC_PAIRS(ST_WOOD_X)
 	return false;

@@ -6,7 +6,7 @@ namespace nbpm {
 #define NBPM_YC(MM, KK, KD) \
 	if(L.M == MM && L.KS == KK && L.kind == KD) { \
 		k_solve_yc<float, MM, KD, KK><<<L.grid, L.block, L.smem, L.stream>>>(G, slot0, nch, coef, fac, plane, lsc, \
-			src, dst, ai, ao); \
+			src, dst, ai, ao, ai2); \
 		return true; \
 	}
 #define NBPM_YC_PAIRS(KIND) \
@@ -16,26 +16,26 @@ namespace nbpm {
 template <>
 bool launch_solve_yc<float>(const SolveLaunch& L, Geom G, int slot0, int nch, const cx<float>* coef,
 		const cx<float>* fac, size_t plane, const cx<double>* lsc, const cx<float>* src, cx<float>* dst,
-		const cx<float>* ai, cx<float>* ao) {
+		const cx<float>* ai, cx<float>* ao, const cx<float>* ai2) {
 	if(L.block.y > 16) {  // 32 warps of 8-row chunks
 		if(L.M == 8 && L.KS == 1 && L.kind == ST_EXPL_X) {
 			k_solve_yc<float, 8, ST_EXPL_X, 1, 1024><<<L.grid, L.block, L.smem, L.stream>>>(G, slot0, nch, coef, fac, plane,
-				lsc, src, dst, ai, ao);
+				lsc, src, dst, ai, ao, ai2);
 			return true;
 		}
 		if(L.M == 8 && L.KS == 1 && L.kind == ST_WOOD_Y) {
 			k_solve_yc<float, 8, ST_WOOD_Y, 1, 1024><<<L.grid, L.block, L.smem, L.stream>>>(G, slot0, nch, coef, fac, plane,
-				lsc, src, dst, ai, ao);
+				lsc, src, dst, ai, ao, ai2);
 			return true;
 		}
 		if(L.M == 8 && L.KS == 2 && L.kind == ST_EXPL_X) {
 			k_solve_yc<float, 8, ST_EXPL_X, 2, 1024><<<L.grid, L.block, L.smem, L.stream>>>(G, slot0, nch, coef, fac, plane,
-				lsc, src, dst, ai, ao);
+				lsc, src, dst, ai, ao, ai2);
 			return true;
 		}
 		if(L.M == 8 && L.KS == 2 && L.kind == ST_WOOD_Y) {
 			k_solve_yc<float, 8, ST_WOOD_Y, 2, 1024><<<L.grid, L.block, L.smem, L.stream>>>(G, slot0, nch, coef, fac, plane,
-				lsc, src, dst, ai, ao);
+				lsc, src, dst, ai, ao, ai2);
 			return true;
 		}
 		return false;
