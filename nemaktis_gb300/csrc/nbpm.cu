@@ -977,7 +977,7 @@ struct Plan : PlanBase {
 		const SolveCfg& sc = scfg[h.index];
 		const double sz = sizeof(cx<R>);
 		double fp = (double)Gm.N * nsl * 2 * sz;
-		double bytes = fp * (1 + (dst ? 1 : 0) + (acc_out ? 2 : 0)) + (double)Gm.N * ng * (2 * NFAC + (wood ? 14 : 20)) * sz;
+		double bytes = fp * (1 + (dst ? 1 : 0) + (acc_out ? 2 : 0) + (acc_in2 ? 1 : 0)) + (double)Gm.N * ng * (2 * NFAC + (wood ? 14 : 20)) * sz;
 		SolveLaunch L;
 		L.stream = cs;
 		if(dirn == 0) {
