@@ -1538,7 +1538,9 @@ __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_xc(Geom G, 
 				int ee = e == Nx - 1 ? 0 : e;
 				cx<R> x = buf[j * PITCH + (ee / M) * (M + 1) + ee % M];
 				if(dst) dst[off + e] = x;
-				if(acc_out) acc_out[off + e] = (acc_in2 ? acc_in[off + e] + acc_in2[off + e] : acc_in[off + e]) + x;
+				// the explicit-step solves never accumulate
+				if(KIND != ST_EXPL_Y && acc_out)
+					acc_out[off + e] = (acc_in2 ? acc_in[off + e] + acc_in2[off + e] : acc_in[off + e]) + x;
 			}
 		}
 	}
@@ -1699,11 +1701,14 @@ __global__ void __launch_bounds__(MAXT, NBPM_YC_MINB) k_solve_yc(Geom G, int slo
 				const cx<R> y = x[j] - fr[j] * cr;
 				const size_t off = (size_t)(s0 + j) * 2 * N + (size_t)c * N;
 				if(dst) dst[off + q] = y;
-				if(acc_out) acc_out[off + q] = (acc_in2 ? acc_in[off + q] + acc_in2[off + q] : acc_in[off + q]) + y;
+				// the explicit-step solves never accumulate
+				if(KIND != ST_EXPL_X && acc_out)
+					acc_out[off + q] = (acc_in2 ? acc_in[off + q] + acc_in2[off + q] : acc_in[off + q]) + y;
 				if(i == 0) {
 					const size_t qe = (size_t)ix + (size_t)Nx * (Ny - 1);
 					if(dst) dst[off + qe] = y;
-					if(acc_out) acc_out[off + qe] = (acc_in2 ? acc_in[off + qe] + acc_in2[off + qe] : acc_in[off + qe]) + y;
+					if(KIND != ST_EXPL_X && acc_out)
+						acc_out[off + qe] = (acc_in2 ? acc_in[off + qe] + acc_in2[off + qe] : acc_in[off + qe]) + y;
 				}
 			}
 		}
