@@ -232,11 +232,11 @@ def run_ours(args):
     # dram__bytes_write.sum), scaled to this workload's launch by the slots it processes; the
     # capture and its command are summarised under profiles/.
     PROF = "profiles/slab_main_stream_koehler_256x256x8_fp32.md"
-    TRAFFIC = {("config3", "fp32", "wood_solve_y"): (2 * (738.6e6 + 724.1e6) / 2, PROF),
-               ("config3", "fp32", "expl_solve_y"): (2 * 532.2e6, PROF),
-               ("config3", "fp32", "wood_solve_x"): (2 * (735.3e6 + 723.1e6) / 2, PROF),
-               ("config3", "fp32", "expl_solve_x"): (2 * 534.5e6, PROF),
-               ("config3", "fp32", "shift_fused"): (2 * 432.4e6, PROF)}
+    TRAFFIC = {("config3", "fp32", "wood_solve_y"): (2 * (505.1e6 + 762.8e6) / 2, PROF),
+               ("config3", "fp32", "expl_solve_y"): (2 * 532.3e6, PROF),
+               ("config3", "fp32", "wood_solve_x"): (2 * (504.0e6 + 753.7e6) / 2, PROF),
+               ("config3", "fp32", "expl_solve_x"): (2 * 545.6e6, PROF),
+               ("config3", "fp32", "shift_fused"): (2 * 432.0e6, PROF)}
     roof = None
     if prof:
         top = max(prof, key=lambda k: prof[k]["ms"])
