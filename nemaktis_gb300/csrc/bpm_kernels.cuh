@@ -1427,6 +1427,11 @@ __device__ __forceinline__ void line_combine(cx<R> P, const cx<R>* d0, const cx<
 	}
 }
 
+// x-line solve fused with its right-hand side (KIND: explicit y half-step or x Woodbury term):
+// a warp per line (4 lines per block) for KS slots of one wavelength. The right-hand sides are
+// computed with coalesced loads into the warp's shared buffer in the lane-chunk layout (lane l
+// holds points [l M, l M + M)), one pass builds the chunk maps, line_combine joins them by
+// shuffles, and a last pass finishes the line, which goes back out coalesced.
 template <typename R, int M, int KIND, int KS>
 // Resident blocks per SM requested from the compiler: 8 (64 registers) for the instances
 // whose chunk values fit, measured faster on GB300; the larger instances keep their registers.
