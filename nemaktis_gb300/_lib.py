@@ -73,6 +73,7 @@ WAVEPLATES = {"No": 0, "Quarter-wave": 1, "Half-wave": 2, "Tint-sensitive": 3}
 
 EXPORTS = {
     "nbpm_default_options": (None, [ctypes.POINTER(Options)]),
+    "nbpm_release_plan_cache": (c_int, []),
     "nbpm_run_backend_without_mask": (c_int, [c_char_p, c_void_p, c_int, c_void_p, c_int]),
     "nbpm_run_backend_with_mask": (c_int, [c_char_p, c_char_p, c_void_p, c_int, c_void_p, c_int, c_void_p, c_int]),
     "nbpm_run_backend_ex": (c_int, [c_char_p, c_char_p, c_void_p, c_int, c_void_p, c_int, c_void_p, c_int,

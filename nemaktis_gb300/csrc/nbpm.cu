@@ -18,6 +18,7 @@
 #include <deque>
 #include <memory>
 #include <stdexcept>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -591,6 +592,24 @@ struct Plan : PlanBase {
 		}
 		CK(cudaStreamSynchronize(stream));
 		host_finish();
+	}
+
+	bool reusable() const override {
+		for(auto& hp : S)
+			if(hp->has_mask || hp->bulk) return false;
+		return true;
+	}
+	void rebind(int ns, const nbpm_sample* samples) override {
+		if(ns != (int)S.size()) throw BackendError(E_INTERNAL, "plan reuse with another sample count");
+		for(int i = 0; i < ns; i++) {
+			SampleHost& h = *S[i];
+			if(!samples[i].lc_field_vals || !samples[i].E_field_vals) throw BackendError(E_ARG, "null pointer argument");
+			if((size_t)samples[i].n_lc_vals != h.nvox * (size_t)h.fd ||
+					(long long)samples[i].n_E_vals != (long long)h.slots * 2 * h.geom.N || samples[i].mask_vals)
+				throw BackendError(E_INTERNAL, "plan reuse with other sizes");
+			h.lc = samples[i].lc_field_vals;
+			h.E = samples[i].E_field_vals;
+		}
 	}
 
 	// Host-side outputs of a finished run: the bulk-output files.
@@ -1427,12 +1446,44 @@ int nbpm_plan_destroy(nbpm_plan* p) {
 	return 0;
 }
 
-int nbpm_run_batch(int n_samples, const nbpm_sample* samples, const nbpm_options* opts, nbpm_timing* timing) {
-	g_last_error.clear();
-	nbpm_plan* p = nullptr;
-	int rc = nbpm_plan_create(n_samples, samples, opts, &p);
-	if(rc) return rc;
-	std::unique_ptr<nbpm_plan> guard(p);
+}  // extern "C"
+
+namespace {
+// One kept plan: a call with the same settings, sizes and options as the previous one (no mask,
+// no bulk output) reuses its device buffers and recorded graph; only the inputs are uploaded
+// again. NBPM_PLAN_CACHE=0 disables it; nbpm_release_plan_cache frees it.
+struct PlanCache {
+	std::mutex m;
+	std::string key;
+	std::unique_ptr<nbpm_plan> plan;
+};
+// never destroyed: a kept plan is released with the process, not by a static destructor that
+// could run after the CUDA runtime has shut down
+PlanCache& plan_cache() {
+	static PlanCache* c = new PlanCache();
+	return *c;
+}
+
+std::string plan_key(int n, const nbpm_sample* s, const nbpm_options* opts) {
+	nbpm_options o;
+	nbpm_default_options(&o);
+	if(opts) o = *opts;
+	std::string k = std::to_string(o.precision) + "/" + std::to_string(o.groups_per_pass) + "/" +
+		std::to_string(o.use_graph) + "/" + std::to_string(o.device) + "/" + std::to_string(o.verbose);
+	for(int i = 0; i < n; i++) {
+		if(!s[i].json_str || s[i].mask_vals) return std::string();
+		k += "|" + std::to_string(s[i].n_lc_vals) + "/" + std::to_string(s[i].n_E_vals) + "/" + s[i].json_str;
+	}
+	return k;
+}
+
+bool plan_cache_on() {
+	const char* e = std::getenv("NBPM_PLAN_CACHE");
+	return !(e && std::atoi(e) == 0);
+}
+
+// Upload, execute, download of one plan with the timing breakdown.
+static int run_plan_once(nbpm_plan* p, nbpm_timing* timing) {
 	API_GUARD({
 		auto t0 = std::chrono::steady_clock::now();
 		p->impl->upload();
@@ -1450,6 +1501,48 @@ int nbpm_run_batch(int n_samples, const nbpm_sample* samples, const nbpm_options
 		}
 		return 0;
 	})
+}
+}  // namespace
+
+extern "C" {
+
+int nbpm_release_plan_cache(void) {
+	std::lock_guard<std::mutex> lk(plan_cache().m);
+	plan_cache().plan.reset();
+	plan_cache().key.clear();
+	return 0;
+}
+
+int nbpm_run_batch(int n_samples, const nbpm_sample* samples, const nbpm_options* opts, nbpm_timing* timing) {
+	g_last_error.clear();
+	if(n_samples <= 0 || !samples) return fail(E_ARG, "invalid plan arguments");
+	// the kept plan, if this call matches it and no other call holds it
+	std::unique_lock<std::mutex> lk(plan_cache().m, std::defer_lock);
+	const std::string key = plan_cache_on() ? plan_key(n_samples, samples, opts) : std::string();
+	if(!key.empty()) lk.try_lock();
+	nbpm_plan* p = nullptr;
+	std::unique_ptr<nbpm_plan> guard;
+	if(lk.owns_lock() && plan_cache().plan && plan_cache().key == key) {
+		p = plan_cache().plan.get();
+		int rc = [&]() -> int { API_GUARD({ p->impl->rebind(n_samples, samples); return 0; }) }();
+		if(rc) { plan_cache().plan.reset(); plan_cache().key.clear(); return rc; }
+	}
+	else {
+		if(lk.owns_lock()) { plan_cache().plan.reset(); plan_cache().key.clear(); }
+		int rc = nbpm_plan_create(n_samples, samples, opts, &p);
+		if(rc) return rc;
+		guard.reset(p);
+	}
+	int rc = run_plan_once(p, timing);
+	if(rc) {
+		if(!guard) { plan_cache().plan.reset(); plan_cache().key.clear(); }
+		return rc;
+	}
+	if(guard && lk.owns_lock() && p->impl->reusable()) {
+		plan_cache().plan = std::move(guard);
+		plan_cache().key = key;
+	}
+	return 0;
 }
 
 int nbpm_run_backend_ex(const char* json_str, const char* mask_formula, const double* lc_field_vals,

@@ -1,0 +1,46 @@
+"""The plan kept between blocking calls (nbpm_run_batch and the reference-shaped entries): a
+call that reuses it gives the bits of a call that builds its plan afresh."""
+import numpy as np
+import pytest
+
+from nemaktis_gb300 import _lib, api, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def _case(seed, wl=(0.5, 0.6)):
+    dims = (24, 20, 7)
+    js = workloads.settings_json(dims, (0.25, 0.25, 0.25), list(wl), [(0.0, 0.0), (0.06, -0.03)], no="1.5", ne="1.7")
+    lc = workloads.random_smooth(dims, seed=seed)
+    return js, lc, (len(wl), 2, 4, dims[1], dims[0])
+
+
+def _fresh(js, lc, shape, precision, monkeypatch, mask=None):
+    monkeypatch.setenv("NBPM_PLAN_CACHE", "0")
+    E = np.zeros(shape, np.complex128)
+    api.run(js, lc, E, mask=mask, precision=precision)
+    monkeypatch.delenv("NBPM_PLAN_CACHE")
+    return E
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_reused_plan_gives_fresh_results(gpu, monkeypatch, precision):
+    lib = _lib.load()
+    monkeypatch.delenv("NBPM_PLAN_CACHE", raising=False)
+    assert lib.nbpm_release_plan_cache() == 0
+    runs = [_case(1), _case(2), _case(2, wl=(0.55, 0.6)), _case(3)]
+    for js, lc, shape in runs:  # second call reuses the first's plan; the third has other settings
+        E = np.zeros(shape, np.complex128)
+        api.run(js, lc, E, precision=precision)
+        np.testing.assert_array_equal(E, _fresh(js, lc, shape, precision, monkeypatch))
+    # a call with a mask between two reusing calls
+    js, lc, shape = runs[-1]
+    mask = np.ones(lc.shape[:3])
+    mask[:, :5, :] = -1.0
+    E = np.zeros(shape, np.complex128)
+    api.run(js, lc, E, mask=mask, precision=precision)
+    np.testing.assert_array_equal(E, _fresh(js, lc, shape, precision, monkeypatch, mask=mask))
+    E = np.zeros(shape, np.complex128)
+    api.run(js, lc[::-1].copy(), E, precision=precision)
+    np.testing.assert_array_equal(E, _fresh(js, lc[::-1].copy(), shape, precision, monkeypatch))
+    assert lib.nbpm_release_plan_cache() == 0
