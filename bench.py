@@ -3,9 +3,11 @@
 Metric: voxel-steps/s (one transverse point advanced one z-slab for one (wavelength,
 wave vector, polarisation) propagation). A "step" is one full run of the workload: every
 slab of every propagation plus the screen filter, with inputs resident in HBM (``value``).
-``e2e`` is the same metric through the reference-facing C ABI call
-(nbpm_run_backend_ex) with pinned host buffers: director upload, the run and the
-complex128 field download inside the timed region.
+``e2e`` is the same metric through the reference-facing C ABI call (nbpm_run_batch, the
+entry behind nbpm_run_backend_ex) with pinned host buffers: director upload, the run and the
+complex128 field download inside the timed region of every step; the device plan of the
+untimed first call is kept and reused by the timed calls, as for any repeated call with the
+same settings.
 
 Default workload: batched Koehler micrograph, 256x256x64 mesh, 16 wavelengths x 13 wave
 vectors x 2 polarisations = 416 propagations, FP32 batched mode. The FP64 plain mode (one
