@@ -184,3 +184,22 @@ def test_cli_matches_backend_call(gpu, tmp_path, basis):
                 im_ = d["point"]["E_imag_%s%d_%d" % (tag, w, q)]
                 got = (re_[:, :2] + 1j * im_[:, :2]).T.reshape(2, odims[1], odims[0])
                 np.testing.assert_array_equal(got, E[w, q, 2 * pol: 2 * pol + 2])
+
+
+def test_cli_failures_print_the_reference_frame(tmp_path, capsys):
+    """bpm-solver -x on a missing settings file, or on an LC field that is not a .vti file,
+    exits with status 1 and the reference's framed message on stderr (main.cpp:169-257)."""
+    from nemaktis_gb300 import cli
+    assert cli.main(["-x", str(tmp_path / "missing.json")]) == 1
+    err = capsys.readouterr().err
+    assert "Could not open the specified setting file" in err and "Aborting!" in err
+    js = json.loads(workloads.settings_json((4, 4, 4), (1, 1, 1), [0.5], [(0.0, 0.0)]))
+    js["Physics settings"]["Initial conditions"]["LC field file"] = str(tmp_path / "lc.dat")
+    p = tmp_path / "s.json"
+    p.write_text(json.dumps(js))
+    assert cli.main(["-x", str(p)]) == 1
+    assert "must be a path to a vti file" in capsys.readouterr().err
+    js["Physics settings"]["Initial conditions"]["LC field file"] = str(tmp_path / "absent.vti")
+    p.write_text(json.dumps(js))
+    assert cli.main(["-x", str(p)]) == 1
+    assert "does not exists" in capsys.readouterr().err
