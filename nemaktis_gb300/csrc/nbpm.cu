@@ -577,12 +577,26 @@ struct Plan : PlanBase {
 		CK(cudaStreamSynchronize(stream));
 	}
 
+	// Device address of a page-locked, mapped host buffer (the caller's result array), or null.
+	static void* mapped_host(void* p) {
+		const char* e = std::getenv("NBPM_ZEROCOPY");
+		if(e && std::atoi(e) == 0) return nullptr;
+		cudaPointerAttributes a;
+		if(cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+		return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+	}
+
 	void download() override {
 		for(auto& hp : S) {
 			SampleHost& h = *hp;
 			size_t n = (size_t)h.slots * 2 * h.geom.N;
 			if(sizeof(R) == sizeof(double)) {
 				CK(cudaMemcpyAsync(h.E, h.F.p, n * sizeof(cx<double>), cudaMemcpyDeviceToHost, stream));
+			}
+			else if(void* dE = mapped_host(h.E)) {
+				// page-locked result array: the widening kernel writes it directly
+				k_widen<R><<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, h.F.as<cx<R>>(), static_cast<cx<double>*>(dE));
+				CK(cudaGetLastError());
 			}
 			else {
 				k_widen<R><<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, h.F.as<cx<R>>(), stage.as<cx<double>>());

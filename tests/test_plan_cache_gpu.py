@@ -44,3 +44,19 @@ def test_reused_plan_gives_fresh_results(gpu, monkeypatch, precision):
     api.run(js, lc[::-1].copy(), E, precision=precision)
     np.testing.assert_array_equal(E, _fresh(js, lc[::-1].copy(), shape, precision, monkeypatch))
     assert lib.nbpm_release_plan_cache() == 0
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_page_locked_result_array(gpu, precision):
+    """A page-locked result array (written by the widening kernel directly in FP32 mode) holds
+    the same bits as an ordinary one."""
+    torch = pytest.importorskip("torch")
+    js, lc, shape = _case(5)
+    n = int(np.prod(shape)) * 16
+    t = torch.empty(n, dtype=torch.uint8, pin_memory=True)
+    E_pinned = t.numpy().view(np.complex128).reshape(shape)
+    E_pinned[...] = 0
+    E = np.zeros(shape, np.complex128)
+    api.run(js, lc, E_pinned, precision=precision)
+    api.run(js, lc, E, precision=precision)
+    np.testing.assert_array_equal(E_pinned, E)
