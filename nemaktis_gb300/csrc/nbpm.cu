@@ -590,10 +590,16 @@ struct Plan : PlanBase {
 		for(auto& hp : S) {
 			SampleHost& h = *hp;
 			size_t n = (size_t)h.slots * 2 * h.geom.N;
-			if(sizeof(R) == sizeof(double)) {
+			void* dE = mapped_host(h.E);
+			if(sizeof(R) == sizeof(double) && dE) {
+				// page-locked result array: copied by a kernel through the mapping
+				k_copy<R><<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, h.F.as<cx<R>>(), static_cast<cx<R>*>(dE));
+				CK(cudaGetLastError());
+			}
+			else if(sizeof(R) == sizeof(double)) {
 				CK(cudaMemcpyAsync(h.E, h.F.p, n * sizeof(cx<double>), cudaMemcpyDeviceToHost, stream));
 			}
-			else if(void* dE = mapped_host(h.E)) {
+			else if(dE) {
 				// page-locked result array: the widening kernel writes it directly
 				k_widen<R><<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, h.F.as<cx<R>>(), static_cast<cx<double>*>(dE));
 				CK(cudaGetLastError());
