@@ -214,8 +214,12 @@ inline void mask_weights(const BackendSettings& s, const double* mask_vals, cons
 	int Nx = s.Nx, Ny = s.Ny, Nz = s.Nz;
 	size_t nv = (size_t)Nx * Ny * Nz;
 	mask_out.resize(nv);
-	for(size_t i = 0; i < nv; i++) mask_out[i] = mask_vals[i] >= 0;
-	w_out.assign(2 * (size_t)Nx * Ny * (Nz > 1 ? Nz - 1 : 0), 0.5);
+	#pragma omp parallel for schedule(static)
+	for(long long i = 0; i < (long long)nv; i++) mask_out[i] = mask_vals[i] >= 0;
+	const size_t nw = 2 * (size_t)Nx * Ny * (Nz > 1 ? Nz - 1 : 0);
+	w_out.resize(nw);
+	#pragma omp parallel for schedule(static)
+	for(long long i = 0; i < (long long)nw; i++) w_out[i] = 0.5;
 	if(formula.empty() || Nz < 2) return;
 	Expr ex;
 	try { ex = Expr(formula, {"x", "y", "z"}); }
@@ -225,12 +229,18 @@ inline void mask_weights(const BackendSettings& s, const double* mask_vals, cons
 	for(long long iperp = 0; iperp < (long long)Nx * Ny; iperp++) {
 		int ix = (int)(iperp % Nx), iy = (int)(iperp / Nx);
 		double v[3] = {(ix - 0.5 * (Nx - 1)) * s.dx, (iy - 0.5 * (Ny - 1)) * s.dy, 0};
+		// the formula at the upper plane of a cell is the one at the lower plane of the next
+		// (the same z), so each plane is evaluated once
+		double f_next = 0;
 		for(int iz = 0; iz < Nz - 1; iz++) {
 			size_t i = iperp + (size_t)Nx * Ny * iz;
 			double zi = (iz - 0.5 * (Nz - 1)) * s.dz, zm = zi, zp = (iz + 1 - 0.5 * (Nz - 1)) * s.dz;
 			double& z = v[2];
-			z = zm; double fm = ex.eval(v);
+			double fm;
+			if(iz == 0) { z = zm; fm = ex.eval(v); }
+			else fm = f_next;
 			z = zp; double fp = ex.eval(v);
+			f_next = fp;
 			if(fm * fp <= 0) {
 				if(mask_out[i] == mask_out[i + (size_t)Nx * Ny]) failed = 1;
 				while(std::abs(zp - zm) >= 1e-3 * s.dz) {
