@@ -85,10 +85,10 @@ typedef struct nbpm_sample {
 /* Propagates several samples of possibly different mesh sizes in one run (each slab step
  * advances every sample that still has slabs left). Results are identical to separate
  * nbpm_run_backend_ex calls. This entry and the ones built on it (nbpm_run_backend_ex,
- * nbpm_run_backend_with/without_mask) keep the device plan of a call without a mask and without
- * bulk output, and reuse it when the next call has the same settings, sizes and options: its
- * device buffers and recorded CUDA graph stay, the inputs are uploaded again and the results
- * are the same. The kept plan holds its device memory until another call replaces it or
+ * nbpm_run_backend_with/without_mask) keep the device plan of a call without bulk output and
+ * reuse it when the next call has the same settings, sizes, mask formula and options: its
+ * device buffers and recorded CUDA graph stay, the inputs (director, mask and its z weights)
+ * are prepared and uploaded again and the results are the same. The kept plan holds its device memory until another call replaces it or
  * nbpm_release_plan_cache is called; the environment variable NBPM_PLAN_CACHE=0 turns the reuse
  * off. Concurrent calls do not share it. */
 int nbpm_run_batch(int n_samples, const nbpm_sample* samples, const nbpm_options* opts,

@@ -616,20 +616,37 @@ struct Plan : PlanBase {
 
 	bool reusable() const override {
 		for(auto& hp : S)
-			if(hp->has_mask || hp->bulk) return false;
+			if(hp->bulk) return false;
 		return true;
 	}
-	void rebind(int ns, const nbpm_sample* samples) override {
-		if(ns != (int)S.size()) throw BackendError(E_INTERNAL, "plan reuse with another sample count");
+	// Returns false (nothing changed) when the call needs another recording: other sizes, or
+	// mask weights that switch between uniform and formula-derived.
+	bool rebind(int ns, const nbpm_sample* samples) override {
+		if(ns != (int)S.size()) return false;
+		std::vector<std::vector<unsigned char>> masks(ns);
+		std::vector<std::vector<double>> wts(ns);
 		for(int i = 0; i < ns; i++) {
 			SampleHost& h = *S[i];
-			if(!samples[i].lc_field_vals || !samples[i].E_field_vals) throw BackendError(E_ARG, "null pointer argument");
-			if((size_t)samples[i].n_lc_vals != h.nvox * (size_t)h.fd ||
-					(long long)samples[i].n_E_vals != (long long)h.slots * 2 * h.geom.N || samples[i].mask_vals)
-				throw BackendError(E_INTERNAL, "plan reuse with other sizes");
+			const nbpm_sample& in = samples[i];
+			if(!in.lc_field_vals || !in.E_field_vals) throw BackendError(E_ARG, "null pointer argument");
+			if((size_t)in.n_lc_vals != h.nvox * (size_t)h.fd || (long long)in.n_E_vals != (long long)h.slots * 2 * h.geom.N ||
+					(in.mask_vals != nullptr) != h.has_mask)
+				return false;
+			if(in.mask_vals) {
+				if((size_t)in.n_mask_vals != h.nvox) return false;
+				mask_weights(h.s, in.mask_vals, in.mask_formula ? std::string(in.mask_formula) : std::string(), masks[i], wts[i]);
+				bool nonuniform = false;
+				for(double w : wts[i]) if(w != 0.5) { nonuniform = true; break; }
+				if(nonuniform != h.has_wts) return false;
+			}
+		}
+		for(int i = 0; i < ns; i++) {
+			SampleHost& h = *S[i];
 			h.lc = samples[i].lc_field_vals;
 			h.E = samples[i].E_field_vals;
+			if(h.has_mask) { h.mask.swap(masks[i]); h.wts.swap(wts[i]); }
 		}
+		return true;
 	}
 
 	// Host-side outputs of a finished run: the bulk-output files.
@@ -1491,8 +1508,10 @@ std::string plan_key(int n, const nbpm_sample* s, const nbpm_options* opts) {
 	std::string k = std::to_string(o.precision) + "/" + std::to_string(o.groups_per_pass) + "/" +
 		std::to_string(o.use_graph) + "/" + std::to_string(o.device) + "/" + std::to_string(o.verbose);
 	for(int i = 0; i < n; i++) {
-		if(!s[i].json_str || s[i].mask_vals) return std::string();
-		k += "|" + std::to_string(s[i].n_lc_vals) + "/" + std::to_string(s[i].n_E_vals) + "/" + s[i].json_str;
+		if(!s[i].json_str) return std::string();
+		k += "|" + std::to_string(s[i].n_lc_vals) + "/" + std::to_string(s[i].n_E_vals) + "/" +
+			std::to_string(s[i].mask_vals ? s[i].n_mask_vals : -1) + "/" + (s[i].mask_formula ? s[i].mask_formula : "") +
+			"/" + s[i].json_str;
 	}
 	return k;
 }
@@ -1542,12 +1561,14 @@ int nbpm_run_batch(int n_samples, const nbpm_sample* samples, const nbpm_options
 	if(!key.empty()) lk.try_lock();
 	nbpm_plan* p = nullptr;
 	std::unique_ptr<nbpm_plan> guard;
+	bool reused = false;
 	if(lk.owns_lock() && plan_cache().plan && plan_cache().key == key) {
 		p = plan_cache().plan.get();
-		int rc = [&]() -> int { API_GUARD({ p->impl->rebind(n_samples, samples); return 0; }) }();
-		if(rc) { plan_cache().plan.reset(); plan_cache().key.clear(); return rc; }
+		int rc = [&]() -> int { API_GUARD({ return p->impl->rebind(n_samples, samples) ? 0 : -1; }) }();
+		if(rc > 0) { plan_cache().plan.reset(); plan_cache().key.clear(); return rc; }
+		reused = rc == 0;
 	}
-	else {
+	if(!reused) {
 		if(lk.owns_lock()) { plan_cache().plan.reset(); plan_cache().key.clear(); }
 		int rc = nbpm_plan_create(n_samples, samples, opts, &p);
 		if(rc) return rc;

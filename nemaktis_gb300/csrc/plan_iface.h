@@ -30,10 +30,10 @@ struct PlanBase {
 	virtual void download() = 0;
 	// Host-side outputs once the run has finished (bulk-output files); download() calls it.
 	virtual void host_finish() = 0;
-	// Whether the plan may be kept for a later call with the same settings (no mask, no bulk
-	// output), and pointing a kept plan at a new call's host arrays (same sizes).
+	// Whether the plan may be kept for a later call with the same settings (no bulk output), and
+	// pointing a kept plan at a new call's host arrays (false: the call needs a new plan).
 	virtual bool reusable() const = 0;
-	virtual void rebind(int n_samples, const nbpm_sample* samples) = 0;
+	virtual bool rebind(int n_samples, const nbpm_sample* samples) = 0;
 	virtual bool fields_view(int sample, PlanFieldsView& v) const = 0;
 	// Resumable execution of a one-sample plan with every wavelength in one pass (serving):
 	// step_begin records the entrance, step_advance up to n more slabs (returns the slabs

@@ -33,13 +33,27 @@ def test_reused_plan_gives_fresh_results(gpu, monkeypatch, precision):
         E = np.zeros(shape, np.complex128)
         api.run(js, lc, E, precision=precision)
         np.testing.assert_array_equal(E, _fresh(js, lc, shape, precision, monkeypatch))
-    # a call with a mask between two reusing calls
+    # masked calls: the same formula-free mask twice with other values, then a mask formula
     js, lc, shape = runs[-1]
-    mask = np.ones(lc.shape[:3])
-    mask[:, :5, :] = -1.0
-    E = np.zeros(shape, np.complex128)
-    api.run(js, lc, E, mask=mask, precision=precision)
-    np.testing.assert_array_equal(E, _fresh(js, lc, shape, precision, monkeypatch, mask=mask))
+    for cut in (5, 9):
+        mask = np.ones(lc.shape[:3])
+        mask[:, :cut, :] = -1.0
+        E = np.zeros(shape, np.complex128)
+        api.run(js, lc, E, mask=mask, precision=precision)
+        np.testing.assert_array_equal(E, _fresh(js, lc, shape, precision, monkeypatch, mask=mask))
+    Nz, Ny, Nx = lc.shape[:3]
+    z, y, x = np.meshgrid((np.arange(Nz) - (Nz - 1) / 2) * 0.25, (np.arange(Ny) - (Ny - 1) / 2) * 0.25,
+                          (np.arange(Nx) - (Nx - 1) / 2) * 0.25, indexing="ij")
+    formula = "4-x^2-y^2-z^2"
+    for r2 in (4.0, 3.0):  # the second mask disagrees with the formula: uniform weights
+        mask = r2 - x ** 2 - y ** 2 - z ** 2
+        E = np.zeros(shape, np.complex128)
+        api.run(js, lc, E, mask=mask, formula=formula, precision=precision)
+        monkeypatch.setenv("NBPM_PLAN_CACHE", "0")
+        ref = np.zeros(shape, np.complex128)
+        api.run(js, lc, ref, mask=mask, formula=formula, precision=precision)
+        monkeypatch.delenv("NBPM_PLAN_CACHE")
+        np.testing.assert_array_equal(E, ref)
     E = np.zeros(shape, np.complex128)
     api.run(js, lc[::-1].copy(), E, precision=precision)
     np.testing.assert_array_equal(E, _fresh(js, lc[::-1].copy(), shape, precision, monkeypatch))
