@@ -243,12 +243,12 @@ inline void mask_weights(const BackendSettings& s, const double* mask_vals, cons
 			f_next = fp;
 			if(fm * fp <= 0) {
 				if(mask_out[i] == mask_out[i + (size_t)Nx * Ny]) failed = 1;
+				// bisection to 1e-3 dz; fm always holds the formula at zm
 				while(std::abs(zp - zm) >= 1e-3 * s.dz) {
-					z = zm; fm = ex.eval(v);
 					z = 0.5 * (zp + zm); double f = ex.eval(v);
 					if(f == 0) break;
 					else if(f * fm < 0) zp = z;
-					else zm = z;
+					else { zm = z; fm = f; }
 				}
 				w_out[2 * i] = (z - zi) / s.dz;
 				w_out[2 * i + 1] = 1 - w_out[2 * i];
