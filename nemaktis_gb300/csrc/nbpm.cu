@@ -623,6 +623,14 @@ struct Plan : PlanBase {
 	// mask weights that switch between uniform and formula-derived.
 	bool rebind(int ns, const nbpm_sample* samples) override {
 		if(ns != (int)S.size()) return false;
+		// a device reset since the plan was made leaves its buffers unknown to the runtime
+		{
+			cudaPointerAttributes a;
+			if(cudaPointerGetAttributes(&a, S[0]->F.p) != cudaSuccess || a.type != cudaMemoryTypeDevice) {
+				cudaGetLastError();
+				return false;
+			}
+		}
 		std::vector<std::vector<unsigned char>> masks(ns);
 		std::vector<std::vector<double>> wts(ns);
 		for(int i = 0; i < ns; i++) {
