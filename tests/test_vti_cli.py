@@ -203,3 +203,23 @@ def test_cli_failures_print_the_reference_frame(tmp_path, capsys):
     p.write_text(json.dumps(js))
     assert cli.main(["-x", str(p)]) == 1
     assert "does not exists" in capsys.readouterr().err
+
+
+def test_reader_big_endian_and_integer_arrays(tmp_path):
+    """Big-endian files and integer/single-precision arrays, as VTK writes them on other hosts."""
+    dims = (3, 2, 2)
+    n = _director(dims, 8).astype(">f4")
+    ids = np.arange(12, dtype=">i4")
+    raw_n, raw_i = n.tobytes(), ids.tobytes()
+    blob_n = struct.pack(">Q", len(raw_n)) + raw_n
+    blob_i = struct.pack(">Q", len(raw_i)) + raw_i
+    ext = "0 2 0 1 0 1"
+    x = ('<?xml version="1.0"?>\n<VTKFile type="ImageData" version="1.0" byte_order="BigEndian" header_type="UInt64">\n'
+         '<ImageData WholeExtent="%s" Origin="0 0 0" Spacing="1 1 1"><Piece Extent="%s"><PointData>'
+         '<DataArray type="Float32" Name="n" NumberOfComponents="3" format="appended" offset="0"/>'
+         '<DataArray type="Int32" Name="id" NumberOfComponents="1" format="appended" offset="%d"/>'
+         '</PointData></Piece></ImageData>\n<AppendedData encoding="raw">\n_' % (ext, ext, len(blob_n)))
+    (tmp_path / "b.vti").write_bytes(x.encode() + blob_n + blob_i + b"\n</AppendedData>\n</VTKFile>\n")
+    d = vti_io.read_vti(str(tmp_path / "b.vti"))
+    np.testing.assert_array_equal(d["point"]["n"], n.astype(np.float64))
+    np.testing.assert_array_equal(d["point"]["id"], ids.astype(np.float64))
