@@ -255,9 +255,9 @@ def run_ours(args):
         from nemaktis_gb300 import _lib
         lib = _lib.load()
         peaks_meas = {}
-        for name, prec in (("fp32_tflops", _lib.FP32), ("fp64_tflops", _lib.FP64)):
+        for name, peak_prec in (("fp32_tflops", _lib.FP32), ("fp64_tflops", _lib.FP64)):
             t = ctypes.c_double()
-            if lib.nbpm_fma_peak(prec, ctypes.byref(t)) == 0:
+            if lib.nbpm_fma_peak(peak_prec, ctypes.byref(t)) == 0:
                 peaks_meas[name] = t.value
     cpu = None
     if rank == 0 and not args.skip_cpu:
@@ -266,7 +266,7 @@ def run_ours(args):
         "metric": "voxel-steps/s FP32-batched vs FP64 plain, 1 GB300, <=1e-4 rel err; p50/p99 latency",
         "value": value, "unit": "voxel-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak" if world > 1 else "weak",
-        "vs_baseline": None, "dtype": "complex-f32 (f64 phase argument, Sherman-Morrison scalar, coefficients)"
+        "vs_baseline": None, "dtype": "complex-f32 (f64 phase argument and Sherman-Morrison scalars)"
         if prec == "fp32" else "complex-f64",
         "data": "synthetic (seeded director fields, no dataset)",
         "config": {"workload": samples[0]["desc"], "precision": prec, "voxel_steps_per_step": vs,
