@@ -182,11 +182,27 @@ def run_ours(args):
         dist.barrier()
     torch.cuda.synchronize()
     clk = Clocks(local)
+    # A step's working set (fields and director) larger than the 126 MB L2 cannot be served from
+    # it; a smaller one is flushed by a 512 MB write before each timed step (outside the step's
+    # CUDA-event window).
+    ws = sum(np.prod(c["shape"]) * (8 if prec == "fp32" else 16) + c["lc"].size * 8 for c in samples)
+    flush = None
+    if ws < 4 * 126e6:
+        try:
+            flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device="cuda")
+        except Exception:
+            flush = None
+    l2_note = ("inputs larger than L2 (fields and director %.0f MB per step)" % (ws / 1e6) if flush is None and ws >= 4 * 126e6
+               else "L2 flushed before every timed step (512 MB write; working set %.0f MB)" % (ws / 1e6)
+               if flush is not None else "working set %.0f MB, not flushed" % (ws / 1e6))
     clk.start()
     t0 = time.perf_counter()
     ms = []
     launches = 0
     for _ in range(args.steps):
+        if flush is not None:
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
         t = plan.execute()
         ms.append(t["compute_ms"])
         launches += t["kernel_launches"]
@@ -270,8 +286,7 @@ def run_ours(args):
         if prec == "fp32" else "complex-f64",
         "data": "synthetic (seeded director fields, no dataset)",
         "config": {"workload": samples[0]["desc"], "precision": prec, "voxel_steps_per_step": vs,
-                   "l2": "inputs larger than L2 (field planes %.0f MB per step)" %
-                         (sum(np.prod(c["shape"]) for c in samples) * (8 if prec == "fp32" else 16) / 1e6),
+                   "l2": l2_note,
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "clocks": clocks, "gpu_launches": launches, "wall_s": wall,
         "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "fp64_plain": fp64, "fma_peaks_measured": peaks_meas,
