@@ -90,3 +90,23 @@ def test_energy_without_absorption():
     oracle.run_backend_without_mask(js, lc, E, stages=1)
     e = np.mean(np.abs(E[0, 0, 0]) ** 2 + np.abs(E[0, 0, 1]) ** 2)
     assert 0.95 < e < 1.05
+
+
+def test_qtensor_of_a_director_gives_the_director_fields():
+    """The Q-tensor permittivity eps = (eps_perp + eps_a/3) I + (2 eps_a / 3) Q
+    (PermittivityTensorField.cpp:3-99) with Q = 3/2 (n n - I/3) is the director's
+    eps_perp I + eps_a n n: both inputs give the same fields."""
+    from tests.helpers import case, rand_director
+    dims = (10, 9, 6)
+    n = rand_director(dims, 4)
+    Q = np.empty(n.shape[:-1] + (6,))
+    for k, (a, b) in enumerate([(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]):
+        Q[..., k] = 1.5 * n[..., a] * n[..., b] - 0.5 * (a == b)
+    q = ((0.0, 0.0), (0.08, -0.05))
+    js_n, _, shape = case(dims, lc=n, q=q)
+    js_q, _, _ = case(dims, lc=Q, lc_type="Q-tensor", q=q)
+    En = np.zeros(shape, np.complex128)
+    Eq = np.zeros(shape, np.complex128)
+    oracle.run_backend_without_mask(js_n, n, En)
+    oracle.run_backend_without_mask(js_q, Q, Eq)
+    assert np.linalg.norm(Eq - En) / np.linalg.norm(En) < 1e-12
