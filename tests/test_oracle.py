@@ -110,3 +110,25 @@ def test_qtensor_of_a_director_gives_the_director_fields():
     oracle.run_backend_without_mask(js_n, n, En)
     oracle.run_backend_without_mask(js_q, Q, Eq)
     assert np.linalg.norm(Eq - En) / np.linalg.norm(En) < 1e-12
+
+
+def test_isotropic_uniform_medium_leaves_the_beam_unchanged():
+    """ne = no (to 1e-10) = nhost = nin = nout: the Fresnel operators, the phase operator and the
+    diffraction step are the identity on a uniform beam, so the screen field equals the input
+    polarisation at every point. With ne exactly equal to no the absorption factor
+    ne_imag / (ne - no) is 0/0 and the fields are NaN, as in the reference
+    (PhaseEvolutionOperator.cpp:12)."""
+    from tests.helpers import case, rand_director
+    dims = (12, 10, 7)
+    n = rand_director(dims, 6)
+    js, _, shape = case(dims, lc=n, no="1.5", ne="1.5000000001", nhost="1.5", nin="1.5", nout="1.5")
+    E = np.zeros(shape, np.complex128)
+    oracle.run_backend_without_mask(js, n, E)
+    np.testing.assert_allclose(E[0, 0, 0], 1.0, atol=1e-8)   # x input, Ex
+    np.testing.assert_allclose(E[0, 0, 1], 0.0, atol=1e-8)   # x input, Ey
+    np.testing.assert_allclose(E[0, 0, 2], 0.0, atol=1e-8)   # y input, Ex (cos(pi/2))
+    np.testing.assert_allclose(E[0, 0, 3], 1.0, atol=1e-8)   # y input, Ey
+    js, _, shape = case(dims, lc=n, no="1.5", ne="1.5", nhost="1.5", nin="1.5", nout="1.5")
+    E = np.zeros(shape, np.complex128)
+    oracle.run_backend_without_mask(js, n, E)
+    assert np.isnan(E).all()
