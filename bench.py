@@ -32,6 +32,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
 MEASURED = os.path.join(HERE, "MEASURED_PEAKS.json")
+L2_BYTES = 126e6
+NO_FLUSH_BYTES = 4 * L2_BYTES  # working sets at least this large are not flushed between steps
 
 
 def peaks():
@@ -182,19 +184,20 @@ def run_ours(args):
         dist.barrier()
     torch.cuda.synchronize()
     clk = Clocks(local)
-    # A step's working set (fields and director) larger than the 126 MB L2 cannot be served from
-    # it; a smaller one is flushed by a 512 MB write before each timed step (outside the step's
-    # CUDA-event window).
+    # A step's working set (fields and director) of at least NO_FLUSH_BYTES (four times the 126 MB
+    # L2) cannot be served from it; a smaller one is flushed by a 512 MB write before each timed
+    # step (outside the step's CUDA-event window).
     ws = sum(np.prod(c["shape"]) * (8 if prec == "fp32" else 16) + c["lc"].size * 8 for c in samples)
     flush = None
-    if ws < 4 * 126e6:
+    if ws < NO_FLUSH_BYTES:
         try:
             flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device="cuda")
         except Exception:
             flush = None
-    l2_note = ("inputs larger than L2 (fields and director %.0f MB per step)" % (ws / 1e6) if flush is None and ws >= 4 * 126e6
-               else "L2 flushed before every timed step (512 MB write; working set %.0f MB)" % (ws / 1e6)
-               if flush is not None else "working set %.0f MB, not flushed" % (ws / 1e6))
+    l2_note = ("inputs larger than L2 (fields and director %.0f MB per step, >= 4x L2: not flushed)" % (ws / 1e6)
+               if ws >= NO_FLUSH_BYTES
+               else "L2 flushed before every timed step (512 MB write; working set %.0f MB < 4x L2)" % (ws / 1e6)
+               if flush is not None else "working set %.0f MB < 4x L2, flush buffer unavailable" % (ws / 1e6))
     clk.start()
     t0 = time.perf_counter()
     ms = []
@@ -268,13 +271,10 @@ def run_ours(args):
                 "algorithmic_bytes_per_launch": r["bytes"] / max(1, r["launches"])}
     peaks_meas = None
     if not args.only_value:
-        from nemaktis_gb300 import _lib
-        lib = _lib.load()
-        peaks_meas = {}
-        for name, peak_prec in (("fp32_tflops", _lib.FP32), ("fp64_tflops", _lib.FP64)):
-            t = ctypes.c_double()
-            if lib.nbpm_fma_peak(peak_prec, ctypes.byref(t)) == 0:
-                peaks_meas[name] = t.value
+        peaks_meas = fma_peaks()
+    c4 = None
+    if rank == 0 and args.workload == "config3" and not args.skip_config4:
+        c4 = config4_record()
     cpu = None
     if rank == 0 and not args.skip_cpu:
         cpu = cpu_baseline(samples, args.cpu_seconds)
@@ -290,10 +290,59 @@ def run_ours(args):
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "clocks": clocks, "gpu_launches": launches, "wall_s": wall,
         "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "fp64_plain": fp64, "fma_peaks_measured": peaks_meas,
+        "config4": c4,
         "kernel_profile": {k: {"ms_per_step": v["ms"], "launches_per_step": v["launches"]} for k, v in (prof or {}).items()},
     }
     if rank == 0:
         print(json.dumps(line))
+
+
+def config4_record(steps=2):
+    """Sub-record for the largest single-GPU configuration (four uneven samples 1024^2x200,
+    768^2x160, 512^2x96, 256^2x48, FP32 batched, one plan): device-resident value over `steps`
+    timed executions after one warm-up, e2e through nbpm_run_batch with pinned host buffers (one
+    warm-up call, one timed call), and the FP32 relative L2 error of the 512^2x96 sample against
+    an FP64 plain run of that sample alone."""
+    import torch
+    from nemaktis_gb300 import api
+    samples = workload("config4")
+    vs = voxel_steps(samples)
+    bufs = [{"json": c["json"], "lc": c["lc"], "E": np.zeros(c["shape"], np.complex128)} for c in samples]
+    plan = api.Plan(bufs, precision="fp32", groups_per_pass=0)
+    plan.upload()
+    plan.execute()
+    torch.cuda.synchronize()
+    ms = [plan.execute()["compute_ms"] for _ in range(steps)]
+    launches = plan.execute()["kernel_launches"]
+    plan.download()
+    plan.close()
+    k = 2  # the 512^2x96 sample
+    E64 = np.zeros(samples[k]["shape"], np.complex128)
+    api.run(samples[k]["json"], samples[k]["lc"], E64, precision="fp64", groups_per_pass=1)
+    err = float(np.linalg.norm(bufs[k]["E"] - E64) / np.linalg.norm(E64))
+    e2e = e2e_measure(samples, "fp32", 1)
+    return {"workload": samples[0]["desc"], "voxel_steps_per_step": vs, "precision": "fp32",
+            "value": vs * steps / (float(np.sum(ms)) / 1e3), "unit": "voxel-steps/s",
+            "ms_per_step": float(np.mean(ms)), "steps": steps, "warmup": 1, "gpu_launches_per_step": launches,
+            "e2e": e2e, "fp32_rel_l2_vs_fp64": {"sample": "512x512x96", "value": err}}
+
+
+def fma_peaks():
+    """FP32/FP64 FMA throughput of the device, from the bench-only probe library."""
+    try:
+        from nemaktis_gb300 import build as nb
+        lib = ctypes.CDLL(nb.build_bench())
+    except Exception as e:  # the probe is a reported extra, never a reason to fail the bench
+        return {"unavailable": str(e)[:200]}
+    f = lib.nbpm_bench_fma_peak
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    out = {}
+    for name, prec in (("fp32_tflops", 1), ("fp64_tflops", 0)):
+        t = ctypes.c_double()
+        if f(prec, ctypes.byref(t)) == 0:
+            out[name] = t.value
+    return out
 
 
 def profile_kernels(plan, lib):
@@ -362,20 +411,27 @@ def e2e_measure(samples, prec, steps):
                              "total": t.total_ms}}
 
 
-def cpu_baseline(samples, seconds):
-    """Oracle (FP64 C++/OpenMP) on a bounded sample: the first wavelength and the first
-    wave vector of the first sample (2 polarisations), every slab, plus its screen filter."""
+def cpu_sample(samples):
+    """The CPU baseline's bounded sample of a workload: the first wavelength with every wave vector
+    and both polarisations (2*Nq propagations sharing that wavelength's permittivity, operators and
+    factorisations, as in BPMIteration.cpp:127-146), every slab, plus the screen filter, of the
+    workload's smallest sample. Returns (json, sample dict, shape, voxel-steps of one run)."""
     import json as _json
-    import oracle
-    c = samples[0]
+    c = min(samples, key=lambda c: int(np.prod(c["shape"][-2:])) * c["Nz"])
     j = _json.loads(c["json"])
     co = j["Physics settings"]["Coefficients"]
     co["Wavelengths"] = co["Wavelengths"][:1]
-    co["Wavevectors"] = co["Wavevectors"][:2]
-    js = _json.dumps(j)
     Nl, Nq, _, Ny, Nx = c["shape"]
-    shape = (1, 1, 4, Ny, Nx)
-    vs = Nx * Ny * (c["Nz"] - 1) * 2
+    shape = (1, Nq, 4, Ny, Nx)
+    vs = Nx * Ny * (c["Nz"] - 1) * 2 * Nq
+    return _json.dumps(j), c, shape, vs
+
+
+def cpu_baseline(samples, seconds, max_runs=50):
+    """Oracle (FP64 C++/OpenMP, all host threads) on the bounded sample of cpu_sample(), repeated
+    until `seconds` have elapsed (at least one run)."""
+    import oracle
+    js, c, shape, vs = cpu_sample(samples)
     runs, t0 = 0, time.perf_counter()
     while True:
         E = np.zeros(shape, np.complex128)
@@ -385,39 +441,41 @@ def cpu_baseline(samples, seconds):
             oracle.run_backend_without_mask(js, c["lc"], E)
         runs += 1
         el = time.perf_counter() - t0
-        if el > seconds or runs >= 50:
+        if el > seconds or runs >= max_runs:
             break
+    Ny, Nx = shape[-2:]
     return {"value": vs * runs / el, "unit": "voxel-steps/s", "cores": oracle.num_threads(), "kind": "port",
-            "sample": "1 wavelength x 1 q x 2 pol of the workload's first sample, all %d slabs, %d run(s), %.1f s"
-                      % (c["Nz"] - 1, runs, el)}
-
-
-def workloads_voxel_steps(c):
-    """Voxel-steps of one sample of a workload (every slab of every propagation)."""
-    from nemaktis_gb300 import workloads
-    return workloads.voxel_steps(c["shape"], c["Nz"])
+            "seconds": el, "runs": runs, "voxel_steps_per_run": vs,
+            "sample": "1 wavelength x %d q x 2 pol (%d propagations sharing the wavelength's operators) of the "
+                      "%dx%dx%d sample, all %d slabs + screen filter, %d run(s) in %.1f s"
+                      % (shape[1], 2 * shape[1], Nx, Ny, c["Nz"], c["Nz"] - 1, runs, el)}
 
 
 def run_reference(args):
+    """The reference arm: the CPU oracle (the reference's algorithm restated in FP64 C++/OpenMP;
+    the reference itself cannot be built here) on all host threads. Each step is one timed run
+    of the bounded sample of cpu_sample(); value = its voxel-steps / its time."""
     world, rank, local = dist_env()
     if rank != 0:
         return
     samples = workload(args.workload)
-    ms = []
-    cpu = None
+    recs = []
     for i in range(args.warmup + args.steps):
-        r = cpu_baseline(samples, args.cpu_seconds / max(1, args.steps))
+        r = cpu_baseline(samples, 0.0, max_runs=1)
         if i >= args.warmup:
-            ms.append(r)
-            cpu = r
-    v = float(np.median([r["value"] for r in ms]))
-    vs_step = sum(workloads_voxel_steps(c) for c in samples)
+            recs.append(r)
+    secs = [r["seconds"] for r in recs]
+    vs_run = recs[0]["voxel_steps_per_run"]
+    v = vs_run * len(recs) / float(np.sum(secs))
+    cpu = recs[-1]
     line = {"impl": "reference", "metric": "voxel-steps/s FP32-batched vs FP64 plain, 1 GB300, <=1e-4 rel err; p50/p99 latency",
             "value": v, "unit": "voxel-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * vs_step / v if v > 0 else None,
+            "ms_per_step": 1e3 * float(np.mean(secs)),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "complex-f64",
             "data": "synthetic (seeded director fields, no dataset)",
-            "config": {"workload": samples[0]["desc"], "precision": "fp64 CPU oracle (reference not buildable here)"},
+            "config": {"workload": samples[0]["desc"], "precision": "fp64 CPU oracle (reference not buildable here)",
+                       "step": "one run of the bounded sample: " + cpu["sample"].split(", %d run" % cpu["runs"])[0],
+                       "voxel_steps_per_step": vs_run},
             "cpu_baseline": {"value": v, "unit": "voxel-steps/s", "cores": cpu["cores"], "kind": "port",
                              "sample": cpu["sample"]},
             "e2e": {"value": v, "unit": "voxel-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -500,6 +558,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-config4", action="store_true", help="no config-4 sub-record in the default line")
     ap.add_argument("--only-value", action="store_true", help="time the device-resident run only")
     ap.add_argument("--serve-requests", type=int, default=12, help="requests in the serving trace")
     args = ap.parse_args()

@@ -1,15 +1,13 @@
-// FMA throughput of the GPU in FP32 and FP64 (the denominators of the compute rooflines of
-// the FP64 plain path and of the compute-heavy kernels). Each thread runs independent FMA
-// chains in registers; the result is written so the compiler keeps the work.
+// Bench-only probe (not part of libnbpm): FMA throughput of the GPU in FP32 and FP64, the
+// compute ceilings the benchmark reports beside the HBM roofline. Each thread runs independent
+// FMA chains in registers; the result is written so the compiler keeps the work. Built into
+// its own library (nemaktis_gb300/_build/libnbpm_bench.so) by nemaktis_gb300/build.py.
 #include <cuda_runtime.h>
 
-#include <string>
+namespace nbpm_bench {
 
-#include "../../include/nbpm.h"
-
-namespace nbpm {
-
-void set_last_error(const std::string& m);
+static const char* g_err = "";
+static void set_last_error(const char* m) { g_err = m; }
 
 template <typename T, int CHAINS>
 __global__ void __launch_bounds__(256) k_fma_peak(int iters, T a, T b, T* out) {
@@ -50,18 +48,21 @@ static int run_peak(double* tflops) {
 	if(a) cudaEventDestroy(a);
 	if(b) cudaEventDestroy(b);
 	if(out) cudaFree(out);
-	if(e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return NBPM_ERR_CUDA; }
+	if(e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return 4; }
 	double flops = 2.0 * (double)blocks * threads * iters * CH;
 	*tflops = flops / (ms * 1e-3) / 1e12;
 	return 0;
 }
 
-}  // namespace nbpm
+}  // namespace nbpm_bench
 
-extern "C" int nbpm_fma_peak(int precision, double* tflops) {
-	if(!tflops) { nbpm::set_last_error("null argument"); return NBPM_ERR_ARG; }
-	if(precision == NBPM_FP64) return nbpm::run_peak<double>(tflops);
-	if(precision == NBPM_FP32) return nbpm::run_peak<float>(tflops);
-	nbpm::set_last_error("unknown precision");
-	return NBPM_ERR_ARG;
+// precision: 0 = FP64, 1 = FP32. Returns 0, or 4 (CUDA error) / 6 (bad argument).
+extern "C" int nbpm_bench_fma_peak(int precision, double* tflops) {
+	if(!tflops) { nbpm_bench::set_last_error("null argument"); return 6; }
+	if(precision == 0) return nbpm_bench::run_peak<double>(tflops);
+	if(precision == 1) return nbpm_bench::run_peak<float>(tflops);
+	nbpm_bench::set_last_error("unknown precision");
+	return 6;
 }
+
+extern "C" const char* nbpm_bench_last_error(void) { return nbpm_bench::g_err; }

@@ -144,15 +144,16 @@ int nbpm_periodic_tridiag_solve(int L, int nlines, const double* inf, const doub
 		const double* rhs, double* x, void* stream);
 
 /* Same solve as nbpm_periodic_tridiag_solve for callers that cannot allocate device memory:
- * code recording inside a CUDA stream capture (a cudaMalloc there breaks the capture),
- * real-time loops that must avoid the allocator and its implicit synchronisation, and hosts
- * that give the whole device memory to their own pool. It allocates nothing: its scratch is a
- * fixed 32 MiB device array (2 Mi complex FP64 values) that every device loading the library
- * holds until the process exits, so sizes with 5*nlines*(L-1) + 2*nlines above 2*1024*1024
- * are rejected with NBPM_ERR_SIZE. The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress); make that first call before any stream capture. All calls
- * share the array: calls that overlap on the GPU (other streams, other host threads) race on
- * it and must be serialised by the caller. No counterpart in the reference. */
+ * real-time loops that must avoid the allocator's latency and the implicit synchronisation of
+ * cudaMalloc/cudaFree, and hosts that give the whole device memory to their own pool. It
+ * allocates nothing: its scratch is a fixed 32 MiB device array (2 Mi complex FP64 values)
+ * that every device loading the library holds until the process exits, so sizes with
+ * 5*nlines*(L-1) + 2*nlines above 2*1024*1024 are rejected with NBPM_ERR_SIZE. The first call
+ * on a device looks up the array's device address (cudaGetSymbolAddress) and keeps it. The
+ * call returns after the solve completed on the given stream. All calls share the array and
+ * it keeps the last call's contents (every value a call reads is written earlier by the same
+ * call): calls that overlap on the GPU (other streams, other host threads) race on it and must
+ * be serialised by the caller. No counterpart in the reference. */
 int nbpm_periodic_tridiag_solve_noalloc(int L, int nlines, const double* inf, const double* mid,
 		const double* sup, const double* rhs, double* x, void* stream);
 
@@ -288,11 +289,6 @@ int nbpm_microscope_spectrum(nbpm_microscope* m, const nbpm_viewer_settings* set
 /* Device time of the last focus and spectrum calls (ms) and device memory held (bytes). */
 int nbpm_microscope_timing(const nbpm_microscope* m, double* focus_ms, double* spectrum_ms,
 		long long* device_bytes);
-
-/* Measured FMA throughput of the current device in TFLOP/s (2 flop per FMA), FP32 or FP64:
- * the compute ceiling the FP64 plain path and the compute-heavy kernels are reported against.
- * No counterpart in the reference. */
-int nbpm_fma_peak(int precision, double* tflops);
 
 /* Message of the last failure on this thread ("" if none). */
 const char* nbpm_last_error(void);

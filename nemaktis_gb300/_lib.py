@@ -114,7 +114,6 @@ EXPORTS = {
     "nbpm_microscope_spectrum": (c_int, [c_void_p, ctypes.POINTER(ViewerSettings), c_void_p, c_ll]),
     "nbpm_microscope_timing": (c_int, [c_void_p, ctypes.POINTER(c_double), ctypes.POINTER(c_double),
                                        ctypes.POINTER(c_ll)]),
-    "nbpm_fma_peak": (c_int, [c_int, ctypes.POINTER(c_double)]),
     "nbpm_last_error": (c_char_p, []),
     "nbpm_version": (c_char_p, []),
 }

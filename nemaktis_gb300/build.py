@@ -1,7 +1,9 @@
 """Compile libnbpm.so (the sm_103a CUDA backend) in-tree with nvcc.
 
-Output: nemaktis_gb300/_build/libnbpm.so (git-ignored). One translation unit, one
--gencode (compute_103a / sm_103a), so a rebuild on a fresh machine takes well under a minute.
+Output: nemaktis_gb300/_build/libnbpm.so (git-ignored), compiled from a few translation units
+in parallel with one -gencode (compute_103a / sm_103a), so a rebuild on a fresh machine takes
+well under a minute. build_bench() compiles the benchmark's FMA probe (bench_peaks.cu beside
+bench.py) into its own library, libnbpm_bench.so, which the product library does not contain.
 """
 import os
 import shutil
@@ -12,10 +14,12 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libnbpm.so")
 SOURCES = ["nbpm.cu", "solve_x_f32.cu", "solve_x_f64.cu", "solve_y_f32.cu", "solve_y_f64.cu", "linesolve.cu",
-           "linesolve_noalloc.cu", "micrograph.cu", "serve.cu", "peaks.cu"]
+           "linesolve_noalloc.cu", "micrograph.cu", "serve.cu"]
 HEADERS = ["bpm_kernels.cuh", "fft_kernels.cuh", "cplx.cuh", "host_settings.h", "host_expr.h", "host_json.h",
            "solve_dispatch.cuh", "plan_iface.h", "vti_writer.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+BENCH_SRC = os.path.join(HERE, "..", "bench_peaks.cu")
+BENCH_LIB = os.path.join(BUILD, "libnbpm_bench.so")
 
 
 def nvcc():
@@ -57,6 +61,18 @@ def build(force=False, verbose=False, extra=()):
     subprocess.run([nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lgomp"], check=True)
     os.replace(tmp, LIB)
     return LIB
+
+
+def build_bench(force=False):
+    """Build libnbpm_bench.so (the benchmark's FMA throughput probe) if missing or stale."""
+    if not force and os.path.exists(BENCH_LIB) and os.path.getmtime(BENCH_LIB) >= os.path.getmtime(BENCH_SRC):
+        return BENCH_LIB
+    os.makedirs(BUILD, exist_ok=True)
+    tmp = BENCH_LIB + ".tmp%d" % os.getpid()
+    subprocess.run([nvcc(), "-O3", "-std=c++17", *ARCH, "-Xcompiler", "-fPIC", "-shared", "-o", tmp, BENCH_SRC],
+                   check=True)
+    os.replace(tmp, BENCH_LIB)
+    return BENCH_LIB
 
 
 if __name__ == "__main__":

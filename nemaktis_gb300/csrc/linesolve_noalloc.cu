@@ -1,12 +1,12 @@
 // Allocation-free variant of the periodic tridiagonal line solve.
 //
 // nbpm_periodic_tridiag_solve allocates its factorisation scratch on each call. Some callers
-// cannot do that: code that records the solve inside a CUDA stream capture (a cudaMalloc
-// there invalidates the capture), real-time loops that must not hit the implicit device
-// synchronisation or the allocator latency of cudaMalloc, and hosts that hand the whole device
-// memory to their own pool and forbid any other allocation. This entry point takes its scratch
-// from a fixed array in device memory that the library reserves when it is loaded, so a call
-// allocates nothing; the caller still provides the inputs and the output.
+// cannot do that: real-time loops that must not pay the allocator's latency or the implicit
+// device synchronisation of cudaMalloc/cudaFree, and hosts that hand the whole device memory
+// to their own pool and forbid any other allocation. This entry point takes its scratch from a
+// fixed array in device memory that the library reserves when it is loaded, so a call
+// allocates nothing; the caller still provides the inputs and the output. The call is
+// synchronous: it returns after the solve has completed on the given stream.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -30,10 +30,18 @@ int pt_run(int L, int nlines, const double* inf, const double* mid, const double
 constexpr size_t NOALLOC_SCRATCH_ELEMS = (size_t)2 << 20;
 static __device__ __align__(256) cx<double> g_noalloc_scratch[NOALLOC_SCRATCH_ELEMS];
 
-// Device address of the scratch array, looked up once per device. In host code the symbol
-// g_noalloc_scratch is only a host-side stand-in, never a device address.
+// Device address of the scratch array, looked up once per device (with that device current)
+// and kept. In host code the symbol g_noalloc_scratch is only a host-side stand-in, never a
+// device address. A kept address is checked against the runtime before use: after a
+// cudaDeviceReset the module is loaded again and the address is looked up anew.
 static std::mutex g_noalloc_mu;
 static cx<double>* g_noalloc_addr[256] = {};
+
+static bool noalloc_addr_valid(cx<double>* p, int dev) {
+	cudaPointerAttributes a;
+	if(cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
+	return a.type == cudaMemoryTypeDevice && a.device == dev && a.devicePointer == static_cast<void*>(p);
+}
 
 static cx<double>* noalloc_scratch(std::string& err) {
 	int dev = 0;
@@ -41,7 +49,7 @@ static cx<double>* noalloc_scratch(std::string& err) {
 	if(e != cudaSuccess) { err = cudaGetErrorString(e); return nullptr; }
 	if(dev < 0 || dev >= 256) { err = "device ordinal out of range"; return nullptr; }
 	std::lock_guard<std::mutex> lk(g_noalloc_mu);
-	if(!g_noalloc_addr[dev]) {
+	if(!g_noalloc_addr[dev] || !noalloc_addr_valid(g_noalloc_addr[dev], dev)) {
 		void* p = nullptr;
 		e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
 		if(e != cudaSuccess || !p) {

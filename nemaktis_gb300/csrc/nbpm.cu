@@ -577,20 +577,26 @@ struct Plan : PlanBase {
 		CK(cudaStreamSynchronize(stream));
 	}
 
-	// Device address of a page-locked, mapped host buffer (the caller's result array), or null.
-	static void* mapped_host(void* p) {
-		const char* e = std::getenv("NBPM_ZEROCOPY");
-		if(e && std::atoi(e) == 0) return nullptr;
-		cudaPointerAttributes a;
+	// Device address of a page-locked, mapped host buffer of the given size (the caller's result
+	// array), or null. Both ends of the range must be mapped with one contiguous device mapping,
+	// so that a kernel writing the whole array through it stays inside the mapped range.
+	static void* mapped_host(void* p, size_t bytes) {
+		if(!bytes) return nullptr;
+		cudaPointerAttributes a, b;
 		if(cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return nullptr; }
-		return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+		if(a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+		char* last = static_cast<char*>(p) + bytes - 1;
+		if(cudaPointerGetAttributes(&b, last) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+		if(b.type != cudaMemoryTypeHost || !b.devicePointer) return nullptr;
+		if(static_cast<char*>(b.devicePointer) - static_cast<char*>(a.devicePointer) != (ptrdiff_t)(bytes - 1)) return nullptr;
+		return a.devicePointer;
 	}
 
 	void download() override {
 		for(auto& hp : S) {
 			SampleHost& h = *hp;
 			size_t n = (size_t)h.slots * 2 * h.geom.N;
-			void* dE = mapped_host(h.E);
+			void* dE = mapped_host(h.E, n * sizeof(cx<double>));
 			if(sizeof(R) == sizeof(double) && dE) {
 				// page-locked result array: copied by a kernel through the mapping
 				k_copy<R><<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, h.F.as<cx<R>>(), static_cast<cx<R>*>(dE));
@@ -1041,7 +1047,12 @@ struct Plan : PlanBase {
 		const SolveCfg& sc = scfg[h.index];
 		const double sz = sizeof(cx<R>);
 		double fp = (double)Gm.N * nsl * 2 * sz;
-		double bytes = fp * (1 + (dst ? 1 : 0) + (acc_out ? 2 : 0) + (acc_in2 ? 1 : 0)) + (double)Gm.N * ng * (2 * NFAC + (wood ? 14 : 20)) * sz;
+		// algorithmic bytes: every distinct field read once (an accumulator input that is the
+		// source itself is not read twice), every field written once, coefficients and factors
+		// once per wavelength
+		const int reads = 1 + (acc_in && acc_in != src ? 1 : 0) + (acc_in2 && acc_in2 != src && acc_in2 != acc_in ? 1 : 0);
+		const int writes = (dst ? 1 : 0) + (acc_out ? 1 : 0);
+		double bytes = fp * (reads + writes) + (double)Gm.N * ng * (2 * NFAC + (wood ? 14 : 20)) * sz;
 		SolveLaunch L;
 		L.stream = cs;
 		if(dirn == 0) {

@@ -3,8 +3,8 @@ reference's own Python code.
 
 Imports HighLevelPythonInterface/nemaktis/light_propagator.py (OpticalFields: objective filter
 :618-646, focus_fields :708-719) and field_viewer.py (FieldViewer._update_specter :348-388,
-_update_averaged_specter :391-455) from a reference checkout (NEMAKTIS_REF, default the
-read-only reference mount of the build machine). Their GUI, VTK, dtmm and bpm_backend imports
+_update_averaged_specter :391-455) from a reference checkout whose root is the required first
+argument (``python make_golden.py <nemaktis checkout>``). Their GUI, VTK, dtmm and bpm_backend imports
 are replaced by empty stand-ins that the exercised code never calls, and pyfftw by numpy.fft
 with pyfftw's documented FFTW.__call__ semantics (forward unnormalised, backward normalised by
 the transform size). Writes micrograph_golden.npz next to this script. Not run by the tests;
@@ -16,7 +16,7 @@ import types
 
 import numpy as np
 
-REF = os.environ.get("NEMAKTIS_REF", "/root/reference")
+REF = None  # root of the reference checkout, set from the command line
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -126,4 +126,7 @@ def main():
 
 
 if __name__ == "__main__":
+    if len(sys.argv) != 2 or not os.path.isdir(os.path.join(sys.argv[1], "HighLevelPythonInterface")):
+        raise SystemExit("usage: python make_golden.py <root of a Nemaktis checkout>")
+    REF = os.path.abspath(sys.argv[1])
     main()

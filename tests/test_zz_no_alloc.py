@@ -1,12 +1,12 @@
 """GPU test of the allocation-free periodic line solve (nbpm_periodic_tridiag_solve_noalloc).
 
-Callers that record work inside a CUDA stream capture, run real-time loops that must not go
-through the device allocator, or hand the whole device memory to their own pool cannot let
-the library call cudaMalloc. For them the library offers a variant of the periodic line solve
-whose scratch is a fixed device array reserved when the library loads. This test calls it
-through the C ABI twice in a row, with different systems, and checks each result against the
-allocating entry point on the same inputs; it also checks that sizes above the fixed scratch
-are refused with a clear error. It lives in a file of its own that pytest collects last."""
+Callers that run real-time loops that must not go through the device allocator, or that hand
+the whole device memory to their own pool, cannot let the library call cudaMalloc. For them
+the library offers a variant of the periodic line solve whose scratch is a fixed device array
+reserved when the library loads. This test calls it through the C ABI twice in a row, with
+different systems, and checks each result against the allocating entry point on the same
+inputs; it also checks that sizes above the fixed scratch are refused with a clear error. It
+lives in a file of its own that pytest collects last."""
 import ctypes
 
 import numpy as np
