@@ -175,7 +175,8 @@ def run_ours(args):
     for c in samples:
         E = np.zeros(c["shape"], np.complex128)
         bufs.append({"json": c["json"], "lc": c["lc"], "E": E, "mask": c.get("mask"), "formula": c.get("formula")})
-    plan = api.Plan(bufs, precision=prec, groups_per_pass=0)
+    plan = api.Plan(bufs, precision=prec, groups_per_pass=0, tune=not args.no_tune, solve_config=args.solve_config)
+    solve_cfg = [plan.solve_config(i) for i in range(len(samples))]
     plan.upload()
     for _ in range(args.warmup):
         plan.execute()
@@ -220,11 +221,25 @@ def run_ours(args):
         if rank == 0:
             print(json.dumps({"metric": "voxel-steps/s", "value": value, "unit": "voxel-steps/s", "steps": args.steps,
                               "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
-                              "config": {"workload": samples[0]["desc"], "precision": prec},
+                              "config": {"workload": samples[0]["desc"], "precision": prec,
+                                         "line_solves": [c for c, _ in solve_cfg]},
                               "gpu_launches": launches, "clocks": clocks}))
         return
     prof = profile_kernels(plan, lib)
     plan.close()
+
+    # The rule-based line-solve configuration on the same workload, for the tuner's gain.
+    tuning = {"configs": [c for c, _ in solve_cfg], "how": [r for _, r in solve_cfg]}
+    if not args.no_tune and args.solve_config is None:
+        hb = [{"json": c["json"], "lc": c["lc"], "E": np.zeros(c["shape"], np.complex128), "mask": c.get("mask"),
+               "formula": c.get("formula")} for c in samples]
+        with api.Plan(hb, precision=prec, groups_per_pass=0, tune=False) as hp:
+            hp.upload()
+            hp.execute()
+            hms = [hp.execute()["compute_ms"] for _ in range(2)]
+            tuning["rule_based_configs"] = [hp.solve_config(i)[0] for i in range(len(samples))]
+        tuning["rule_based_ms_per_step"] = float(np.mean(hms))
+        tuning["tuned_ms_per_step"] = dev_ms / args.steps
 
     # FP64 plain path on the same workload (one wavelength per launch), one step.
     fp64 = None
@@ -290,7 +305,7 @@ def run_ours(args):
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "clocks": clocks, "gpu_launches": launches, "wall_s": wall,
         "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "fp64_plain": fp64, "fma_peaks_measured": peaks_meas,
-        "config4": c4,
+        "config4": c4, "line_solves": tuning,
         "kernel_profile": {k: {"ms_per_step": v["ms"], "launches_per_step": v["launches"]} for k, v in (prof or {}).items()},
     }
     if rank == 0:
@@ -559,6 +574,8 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-config4", action="store_true", help="no config-4 sub-record in the default line")
+    ap.add_argument("--no-tune", action="store_true", help="rule-based line-solve configuration (no timing runs)")
+    ap.add_argument("--solve-config", default=None, help='force a line-solve configuration "<x>;<y>"')
     ap.add_argument("--only-value", action="store_true", help="time the device-resident run only")
     ap.add_argument("--serve-requests", type=int, default=12, help="requests in the serving trace")
     args = ap.parse_args()

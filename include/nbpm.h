@@ -36,6 +36,11 @@ typedef struct nbpm_options {
 	int use_graph;        /* capture the slab loop in a CUDA graph (default 1) */
 	int device;           /* CUDA device ordinal (default 0) */
 	int verbose;          /* print the reference's progress lines to stdout */
+	int tune;             /* 1 (default): the first plan of a shape times the candidate line-solve
+	                         configurations and keeps the fastest (cached per shape for the
+	                         process); 0: rule-based configuration, no timing runs */
+	const char* solve_config; /* NULL, or "<x>;<y>" forcing one candidate per direction (as listed
+	                         by nbpm_solve_candidates; either part may be "auto") */
 } nbpm_options;
 
 typedef struct nbpm_timing {
@@ -120,6 +125,23 @@ int nbpm_plan_profile(nbpm_plan* plan, char (*names)[48], double* ms, int* launc
 
 /* Device memory the plan holds, bytes. */
 long long nbpm_plan_device_bytes(const nbpm_plan* plan);
+
+/* Line-solve configuration of sample `sample` of the plan as "<x>;<y>" (e.g.
+ * "xc:M=8:KS=4;yq:KS=2"), and in `report` (may be NULL) how it was chosen: forced, rule-based,
+ * or the tuner's device time per candidate. The reference runs one sequential Thomas sweep per
+ * line on every mesh (BlockSparseMatrix.cpp:195-259, 386-451); no counterpart there. */
+int nbpm_plan_solve_config(const nbpm_plan* plan, int sample, char* config, int n_config, char* report,
+		int n_report);
+
+/* The candidate line-solve configurations for the mesh and slots of the JSON settings at a
+ * precision and wavelengths per pass: "x=<c>|<c>...\ny=<c>|...\ndefault=<x>;<y>". Host-side
+ * (uses the current device's SM count and shared memory when a device is present). No
+ * counterpart in the reference. */
+int nbpm_solve_candidates(const char* json_str, int precision, int groups_per_pass, char* out, int n);
+
+/* Forgets every tuned configuration of the process (the next plan of each shape times its
+ * candidates again). Returns 0. No counterpart in the reference. */
+int nbpm_tune_cache_clear(void);
 
 /* Evaluates a refractive-index expression in the variable "lambda" (µm) with the backend's
  * expression evaluator (the reference uses muParser, PhysicsCoefficients.cpp:27-103). */

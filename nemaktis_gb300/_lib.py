@@ -24,7 +24,7 @@ class NbpmError(RuntimeError):
 
 class Options(ctypes.Structure):
     _fields_ = [("precision", c_int), ("groups_per_pass", c_int), ("use_graph", c_int),
-                ("device", c_int), ("verbose", c_int)]
+                ("device", c_int), ("verbose", c_int), ("tune", c_int), ("solve_config", c_char_p)]
 
 
 class Timing(ctypes.Structure):
@@ -87,6 +87,9 @@ EXPORTS = {
     "nbpm_plan_destroy": (c_int, [c_void_p]),
     "nbpm_plan_device_bytes": (c_ll, [c_void_p]),
     "nbpm_plan_profile": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, ctypes.POINTER(c_int)]),
+    "nbpm_plan_solve_config": (c_int, [c_void_p, c_int, c_void_p, c_int, c_void_p, c_int]),
+    "nbpm_solve_candidates": (c_int, [c_char_p, c_int, c_int, c_void_p, c_int]),
+    "nbpm_tune_cache_clear": (c_int, []),
     "nbpm_eval_index": (c_int, [c_char_p, c_double, ctypes.POINTER(c_double)]),
     "nbpm_mask_weights": (c_int, [c_char_p, c_char_p, c_void_p, c_int, c_void_p, c_void_p]),
     "nbpm_periodic_tridiag_solve": (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
@@ -151,8 +154,25 @@ def check(rc):
     return rc
 
 
-def options(precision=FP64, groups_per_pass=0, use_graph=1, device=0, verbose=0):
+def options(precision=FP64, groups_per_pass=0, use_graph=1, device=0, verbose=0, tune=1, solve_config=None):
+    """nbpm_options; solve_config ("<x>;<y>", see solve_candidates) must stay referenced by the
+    caller while the options are in use (ctypes keeps the bytes object alive on the struct)."""
     o = Options()
     load().nbpm_default_options(ctypes.byref(o))
     o.precision, o.groups_per_pass, o.use_graph, o.device, o.verbose = precision, groups_per_pass, use_graph, device, verbose
+    o.tune = int(tune)
+    o.solve_config = None if solve_config is None else solve_config.encode()
     return o
+
+
+def solve_candidates(json_str, precision=FP64, groups_per_pass=0):
+    """Candidate line-solve configurations for the settings' mesh and slots:
+    {"x": [...], "y": [...], "default": "<x>;<y>"}."""
+    buf = ctypes.create_string_buffer(8192)
+    js = json_str.encode() if isinstance(json_str, str) else json_str
+    check(load().nbpm_solve_candidates(js, precision, groups_per_pass, buf, len(buf)))
+    out = {}
+    for line in buf.value.decode().splitlines():
+        k, v = line.split("=", 1)
+        out[k] = v.split("|") if k in ("x", "y") else v
+    return out

@@ -47,14 +47,18 @@ class _Samples:
                                  E.ctypes.data, E.size)
 
 
-def run(json_str, lc, E, mask=None, formula=None, precision="fp64", groups_per_pass=0, use_graph=True):
+def run(json_str, lc, E, mask=None, formula=None, precision="fp64", groups_per_pass=0, use_graph=True, tune=True,
+        solve_config=None):
     return run_batch([{"json": json_str, "lc": lc, "E": E, "mask": mask, "formula": formula}],
-                     precision, groups_per_pass, use_graph)
+                     precision, groups_per_pass, use_graph, tune, solve_config)
 
 
-def run_batch(samples, precision="fp64", groups_per_pass=0, use_graph=True):
+def run_batch(samples, precision="fp64", groups_per_pass=0, use_graph=True, tune=True, solve_config=None):
+    """solve_config: None (tuned or rule-based line solves, see tune) or "<x>;<y>" forcing one of
+    the candidates listed by _lib.solve_candidates for every sample."""
     S = _Samples(samples)
-    o = options(precision=_precision(precision), groups_per_pass=groups_per_pass, use_graph=int(use_graph))
+    o = options(precision=_precision(precision), groups_per_pass=groups_per_pass, use_graph=int(use_graph),
+                tune=int(tune), solve_config=solve_config)
     t = Timing()
     check(load().nbpm_run_batch(len(samples), S.arr, ctypes.byref(o), ctypes.byref(t)))
     return _timing_dict(t)
@@ -63,10 +67,11 @@ def run_batch(samples, precision="fp64", groups_per_pass=0, use_graph=True):
 class Plan:
     """Device-resident plan (nbpm_plan_*)."""
 
-    def __init__(self, samples, precision="fp64", groups_per_pass=0, use_graph=True):
+    def __init__(self, samples, precision="fp64", groups_per_pass=0, use_graph=True, tune=True, solve_config=None):
         self._S = _Samples(samples)
         self._lib = load()
-        o = options(precision=_precision(precision), groups_per_pass=groups_per_pass, use_graph=int(use_graph))
+        o = options(precision=_precision(precision), groups_per_pass=groups_per_pass, use_graph=int(use_graph),
+                    tune=int(tune), solve_config=solve_config)
         h = ctypes.c_void_p()
         check(self._lib.nbpm_plan_create(len(samples), self._S.arr, ctypes.byref(o), ctypes.byref(h)))
         self._h = h
@@ -81,6 +86,13 @@ class Plan:
 
     def download(self):
         check(self._lib.nbpm_plan_download(self._h))
+
+    def solve_config(self, sample=0):
+        """(configuration "<x>;<y>", how it was chosen) of one sample's line solves."""
+        cfg = ctypes.create_string_buffer(256)
+        rep = ctypes.create_string_buffer(4096)
+        check(self._lib.nbpm_plan_solve_config(self._h, sample, cfg, len(cfg), rep, len(rep)))
+        return cfg.value.decode(), rep.value.decode()
 
     def device_bytes(self):
         return int(self._lib.nbpm_plan_device_bytes(self._h))

@@ -438,123 +438,6 @@ __global__ void k_coef(const S* __restrict__ QA, const S* __restrict__ QB,
 }
 
 // ---------------------------------------------------------------------------------------
-// Pre-factorisation of the periodic line solves (I - mu*R_cc) x = b, one thread per
-// (group, comp, line), in the plan's precision. Restates shifted_block_vmult_inv (BlockSparseMatrix.cpp:
-// 195-258 and 386-449): Thomas sweep with beta0 = 2*mid0 and the Sherman-Morrison corner
-// vector corr (corr0 = -1/2). Everything that does not depend on the right-hand side is
-// computed here once per (wavelength, slab) and shared by all (q, pol) slots:
-//   F_A    alpha_i = -inf_i/beta_i   F_RB  1/beta_i        F_C   -gamma_i
-//   F_COR  corr_i after back-substitution
-//   F_W    w_i = prod_{j<i}(-gamma_j), so that the back-substituted x_0 = sum_i w_i d_i
-//          is formed during the forward sweep
-// The forward sweep is then d_i = alpha_i d_{i-1} + b_i/beta_i and the backward sweep
-// x_{i-1} = d_{i-1} - gamma_{i-1} x_i: both first-order affine recurrences whose
-// coefficients do not depend on b, which is what the chunked solves below exploit.
-// plus per line r0 = inf0/mid0 and rden = 1/(1 + corr0 - r0*corr_{L-2}) in FP64.
-// scr holds gamma and the forward corr: [group][comp][2][N].
-// ---------------------------------------------------------------------------------------
-// One launch covers the x factorisations (threads [0, ngroups*2*Ny)) and the y ones (the
-// following ngroups*2*Nx threads); scratch halves are separate.
-template <typename S>
-__global__ void k_factor(Geom G, int ngroups, int chunkMx, int chunksX, const cx<S>* __restrict__ diag,
-		cx<S>* __restrict__ facx, size_t planex, cx<double>* __restrict__ lscx,
-		cx<S>* __restrict__ facy, size_t planey, cx<double>* __restrict__ lscy, cx<S>* __restrict__ scr_all) {
-	typedef S T;
-	int Nx = G.Nx, Ny = G.Ny, N = G.N;
-	int t = blockIdx.x * blockDim.x + threadIdx.x;
-	const int nx_threads = ngroups * 2 * Ny;
-	const int dirn = t < nx_threads ? 0 : 1;
-	if(dirn == 1) t -= nx_threads;
-	const int chunkM = dirn == 0 ? chunkMx : 0;
-	cx<S>* fac = dirn == 0 ? facx : facy;
-	const size_t plane = dirn == 0 ? planex : planey;
-	cx<double>* lsc = dirn == 0 ? lscx : lscy;
-	cx<S>* scr = scr_all + (size_t)dirn * ngroups * 2 * 2 * N;
-	int L = dirn == 0 ? Nx : Ny;
-	int nlines = dirn == 0 ? Ny : Nx;
-	if(t >= ngroups * 2 * nlines || L <= 3) return;
-	int line = t % nlines;
-	int c = (t / nlines) % 2;
-	int g = t / (2 * nlines);
-	const cx<T>* Dg = diag + (size_t)g * NDIAG * N + (size_t)(dirn * 6 + c * 3) * N;
-	cx<S>* Fc = fac + ((size_t)g * 2 + c) * NFAC * plane;
-	cx<T>* sG = scr + ((size_t)g * 2 + c) * 2 * N;
-	cx<T>* sC = sG + N;
-	cx<double>* ls = lsc + (((size_t)g * 2 + c) * nlines + line) * 2;
-	const int stride = dirn == 0 ? 1 : Nx;
-	const int base = dirn == 0 ? Nx * line : line;
-	// point index of element i (stencil coefficient / scratch layout)
-	auto P = [&](int i) { return base + i * stride; };
-	// factor storage index: natural layout, or chunk-interleaved x-line layout where element
-	// i = ci*M + k of chunk ci (of chunksX chunks per line) sits at k*chunksX + ci (coalesced
-	// for the chunked solves, one lane per chunk)
-	auto Q = [&](int i) -> size_t {
-		if(chunkM <= 0) return (size_t)P(i);
-		return (size_t)line * chunksX * chunkM + (size_t)(i % chunkM) * chunksX + (i / chunkM);
-	};
-	const cx<T> one = mk<T>(1, 0);
-	auto sup = [&](int i) { return -Dg[2 * (size_t)N + P(i)]; };
-	auto mid = [&](int i) { return one - Dg[1 * (size_t)N + P(i)]; };
-	auto inf = [&](int i) { return -Dg[P(i)]; };
-
-	cx<T> beta = (T)2 * mid(0);
-	cx<T> rb = crecip(beta);
-	Fc[F_RB * plane + Q(0)] = cvt<S>(rb);
-	Fc[F_A * plane + Q(0)] = mk<S>(0, 0);
-	cx<T> corr = mk<T>(-0.5, 0);
-	sC[P(0)] = corr;
-	for(int i = 1; i < L - 2; i++) {
-		cx<T> gam = sup(i - 1) * rb;
-		sG[P(i - 1)] = gam;
-		Fc[F_C * plane + Q(i - 1)] = cvt<S>(-gam);
-		cx<T> in = inf(i);
-		beta = mid(i) - in * gam;
-		rb = crecip(beta);
-		Fc[F_RB * plane + Q(i)] = cvt<S>(rb);
-		Fc[F_A * plane + Q(i)] = cvt<S>(-(in * rb));
-		corr = -(in * corr) * rb;
-		sC[P(i)] = corr;
-	}
-	cx<T> gl = sup(L - 3) * rb;
-	sG[P(L - 3)] = gl;
-	Fc[F_C * plane + Q(L - 3)] = cvt<S>(-gl);
-	cx<T> inL = inf(L - 2);
-	beta = mid(L - 2) + cdiv(sup(L - 2) * inf(0), mid(0)) - inL * gl;
-	rb = crecip(beta);
-	Fc[F_RB * plane + Q(L - 2)] = cvt<S>(rb);
-	Fc[F_A * plane + Q(L - 2)] = cvt<S>(-(inL * rb));
-	cx<T> corr_last = (sup(L - 2) - inL * corr) * rb;
-	Fc[F_COR * plane + Q(L - 2)] = cvt<S>(corr_last);
-	Fc[F_C * plane + Q(L - 2)] = mk<S>(0, 0);
-	cx<T> cn = corr_last;
-	for(int i = L - 2; i > 0; i--) {
-		cx<T> cv = sC[P(i - 1)] - sG[P(i - 1)] * cn;
-		Fc[F_COR * plane + Q(i - 1)] = cvt<S>(cv);
-		cn = cv;
-	}
-	cx<T> w = one;
-	Fc[F_W * plane + Q(0)] = cvt<S>(w);
-	for(int i = 1; i < L - 1; i++) {
-		w = -(w * sG[P(i - 1)]);
-		Fc[F_W * plane + Q(i)] = cvt<S>(w);
-	}
-	if(chunkM > 0) {
-		// padding elements of the interleaved layout act as identity maps
-		for(int i = L - 1; i < chunksX * chunkM; i++) {
-			Fc[F_A * plane + Q(i)] = mk<S>(0, 0);
-			Fc[F_RB * plane + Q(i)] = mk<S>(0, 0);
-			Fc[F_W * plane + Q(i)] = mk<S>(0, 0);
-			Fc[F_C * plane + Q(i)] = mk<S>(0, 0);
-			Fc[F_COR * plane + Q(i)] = mk<S>(0, 0);
-		}
-	}
-	// Sherman-Morrison scalars in FP64
-	cx<double> r0 = cdiv(cvt<double>(inf(0)), cvt<double>(mid(0)));
-	ls[0] = r0;
-	ls[1] = crecip(mk(1.0, 0.0) + cvt<double>(cn) - r0 * cvt<double>(corr_last));
-}
-
-// ---------------------------------------------------------------------------------------
 // Right-hand-side kernels over all (point, slot) pairs of a pass.
 // ---------------------------------------------------------------------------------------
 template <typename R>
@@ -626,7 +509,7 @@ struct Stencil {
 
 // Step kinds of the composite stencil kernel (ParaxialPrimaryEvolutionOperator.cpp:153-207
 // with the duplicate-row/column fix-ups of BlockSparseMatrix.cpp folded in analytically).
-enum { ST_EXPL_Y = 0, ST_EXPL_X = 1, ST_WOOD_X = 2, ST_WOOD_Y = 3, ST_GIVEN = 4 };
+enum { ST_EXPL_Y = 0, ST_EXPL_X = 1, ST_WOOD_X = 2, ST_WOOD_Y = 3 };
 
 // One component of a composite stencil step at point (ix, iy). EXPL kinds return
 // f + mu*R f (explicit half-step), WOOD kinds return mu*R_offdiag t (Woodbury right-hand side).
@@ -695,12 +578,6 @@ __device__ __forceinline__ void composite_m(const Stencil<R>& st, int comp, int 
 	const int xx = ix == Nx - 1 ? 0 : ix, yy = iy == Ny - 1 ? 0 : iy;
 	const bool ax = Nx > 3, ay = Ny > 3;
 	const int p = ix + Nx * iy;
-	if(KIND == ST_GIVEN) {
-		const cx<R>* fc = comp == 0 ? f0 : f1;
-#pragma unroll
-		for(int j = 0; j < KS; j++) out[j] = fc[j * ss + p];
-		return;
-	}
 #pragma unroll
 	for(int j = 0; j < KS; j++) out[j] = mk<R>(0, 0);
 	if(KIND == ST_EXPL_Y) {
@@ -763,222 +640,6 @@ __device__ __forceinline__ void composite_m(const Stencil<R>& st, int comp, int 
 			st.template dxdy_m<KS>(3, xx, yy, f1, ss, out);
 		}
 		else st.template dy_m<KS>(2, ix, yy, f0, ss, out);
-	}
-}
-
-// Stencil terms of one composite step at one point, gathered once so that they can be applied
-// to every slot of a wavelength group: value = [f_comp(p)] + sum_t coef_t * f_{src_t}(tap_t).
-template <typename R>
-struct Terms {
-	int n;
-	cx<R> c[14];
-	int tap[14];
-	unsigned char src[14];
-	__device__ __forceinline__ void add(cx<R> cv, int t, int s) { c[n] = cv; tap[n] = t; src[n] = (unsigned char)s; n++; }
-	__device__ __forceinline__ void dx(const Stencil<R>& st, int b, int x, int y, int s) {
-		int p = x + st.Nx * y, Nx = st.Nx;
-		int mx = x == 0 ? Nx - 2 : x - 1, px = x == Nx - 2 ? 0 : x + 1;
-		int base = C_DX + 3 * b;
-		add(st.c(base, p), mx + Nx * y, s); add(st.c(base + 1, p), p, s); add(st.c(base + 2, p), px + Nx * y, s);
-	}
-	__device__ __forceinline__ void dy(const Stencil<R>& st, int b, int x, int y, int s) {
-		int p = x + st.Nx * y, Nx = st.Nx, Ny = st.Ny;
-		int my = y == 0 ? Ny - 2 : y - 1, py = y == Ny - 2 ? 0 : y + 1;
-		int base = C_DY + 3 * b;
-		add(st.c(base, p), x + Nx * my, s); add(st.c(base + 1, p), p, s); add(st.c(base + 2, p), x + Nx * py, s);
-	}
-	__device__ __forceinline__ void dxdy(const Stencil<R>& st, int b, int x, int y, int s) {
-		int p = x + st.Nx * y, Nx = st.Nx, Ny = st.Ny;
-		int mx = x == 0 ? Nx - 2 : x - 1, px = x == Nx - 2 ? 0 : x + 1;
-		int my = y == 0 ? Ny - 2 : y - 1, py = y == Ny - 2 ? 0 : y + 1;
-		int base = C_DXDY + 4 * b;
-		add(st.c(base, p), px + Nx * py, s); add(st.c(base + 1, p), mx + Nx * py, s);
-		add(st.c(base + 2, p), px + Nx * my, s); add(st.c(base + 3, p), mx + Nx * my, s);
-	}
-};
-
-// The terms of composite<KIND>(comp) at (ix, iy), same folding of the duplicate row/column.
-// Returns whether the f_comp(p) identity term is present (explicit half-steps).
-template <typename R, int KIND>
-__device__ __forceinline__ bool gather_terms(const Stencil<R>& st, int comp, int ix, int iy, Terms<R>& T) {
-	const int Nx = st.Nx, Ny = st.Ny;
-	const int xx = ix == Nx - 1 ? 0 : ix, yy = iy == Ny - 1 ? 0 : iy;
-	const bool ax = Nx > 3, ay = Ny > 3;
-	T.n = 0;
-	if(KIND == ST_EXPL_Y) {
-		if(comp == 0) { if(ay) { T.dy(st, 0, ix, yy, 0); T.dy(st, 1, ix, yy, 1); } }
-		else if(ay) {
-			if(ax) { T.dy(st, 3, xx, yy, 1); T.dxdy(st, 3, xx, yy, 1); T.dy(st, 2, xx, yy, 0); T.dxdy(st, 2, xx, yy, 0); }
-			else { T.dy(st, 3, ix, yy, 1); T.dy(st, 2, ix, yy, 0); }
-		}
-		return true;
-	}
-	if(KIND == ST_EXPL_X) {
-		if(comp == 0) {
-			if(ax) {
-				if(ay) { T.dx(st, 0, xx, yy, 0); T.dxdy(st, 0, xx, yy, 0); T.dx(st, 1, xx, yy, 1); T.dxdy(st, 1, xx, yy, 1); }
-				else { T.dx(st, 0, xx, iy, 0); T.dx(st, 1, xx, iy, 1); }
-			}
-		}
-		else if(ax) { T.dx(st, 3, xx, iy, 1); T.dx(st, 2, xx, iy, 0); }
-		return true;
-	}
-	if(KIND == ST_WOOD_X) {
-		if(comp == 0) {
-			if(ax) {
-				if(ay) { T.dx(st, 1, xx, yy, 1); T.dxdy(st, 1, xx, yy, 1); T.dxdy(st, 0, xx, yy, 0); }
-				else T.dx(st, 1, xx, iy, 1);
-			}
-		}
-		else if(ax) T.dx(st, 2, xx, iy, 0);
-		return false;
-	}
-	if(comp == 0) { if(ay) T.dy(st, 1, ix, yy, 1); }
-	else if(ay) {
-		if(ax) { T.dy(st, 2, xx, yy, 0); T.dxdy(st, 2, xx, yy, 0); T.dxdy(st, 3, xx, yy, 1); }
-		else T.dy(st, 2, ix, yy, 0);
-	}
-	return false;
-}
-
-// Right-hand sides of one composite step for every slot of a wavelength group: one thread per
-// (point, comp, group); the stencil terms are gathered once and applied to all 2*Nq slots.
-template <typename R, int KIND>
-__global__ void __launch_bounds__(256) k_rhs(Geom G, int slot0, const cx<R>* __restrict__ coef,
-		const cx<R>* __restrict__ src, cx<R>* __restrict__ dst) {
-	int p = blockIdx.x * blockDim.x + threadIdx.x;
-	const int N = G.N, Nx = G.Nx, Ny = G.Ny;
-	if(p >= N) return;
-	const int c = blockIdx.y % 2, g = blockIdx.y / 2;
-	const Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
-	Terms<R> T;
-	bool ident = gather_terms<R, KIND>(st, c, p % Nx, p / Nx, T);
-	const size_t ss = 2 * (size_t)N;
-	const cx<R>* f = src + (size_t)g * G.spg * ss;
-	cx<R>* o = dst + (size_t)g * G.spg * ss + (size_t)c * N + p;
-	for(int sl = 0; sl < G.spg; sl++) {
-		const cx<R>* fs = f + sl * ss;
-		cx<R> v = ident ? fs[(size_t)c * N + p] : mk<R>(0, 0);
-		for(int t = 0; t < T.n; t++) v += T.c[t] * fs[(size_t)T.src[t] * N + T.tap[t]];
-		o[sl * ss] = v;
-	}
-}
-
-// x-line solve, group-cooperative form: one block per (line, comp, wavelength group) owns the
-// line for every (q, pol) slot of the group. The right-hand sides are formed with the stencil
-// terms gathered once per point and applied to all slots, the factor planes of the line are
-// loaded once into shared memory, and the block's warps solve the slots (one slot per warp at a
-// time) with the chunked scan of k_solve_xc.
-template <typename R, int M, int KIND>
-__global__ void __launch_bounds__(256) k_solve_xg(Geom G, int slot0, const cx<R>* __restrict__ coef,
-		const cx<R>* __restrict__ fac, size_t plane, const cx<double>* __restrict__ lsc,
-		const cx<R>* __restrict__ src, cx<R>* __restrict__ dst, const cx<R>* acc_in, cx<R>* acc_out) {
-	extern __shared__ unsigned char smem_raw[];
-	const int NWp = blockDim.x / 32;
-	const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-	const int Nx = G.Nx, Ny = G.Ny, N = G.N, spg = G.spg;
-	const int iy = blockIdx.x;
-	const int c = blockIdx.y % 2, g = blockIdx.y / 2;
-	const int n_unk = Nx - 1;
-	const int PITCH = 32 * (M + 1);
-	cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw);        // [spg][PITCH]
-	cx<R>* sf = buf + (size_t)spg * PITCH;                    // [NFAC][32*M]
-	const cx<R>* Fc = fac + ((size_t)g * 2 + c) * NFAC * plane + (size_t)iy * 32 * M;
-	for(int e = threadIdx.x; e < NFAC * 32 * M; e += blockDim.x) {
-		int f = e / (32 * M), i = e % (32 * M);
-		sf[e] = Fc[f * plane + i];
-	}
-	const Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
-	const size_t ss = 2 * (size_t)N;
-	const cx<R>* f0 = src + (size_t)g * spg * ss;
-	for(int e = threadIdx.x; e < n_unk; e += blockDim.x) {
-		Terms<R> T;
-		bool ident = gather_terms<R, KIND>(st, c, e, iy, T);
-		const int p = e + Nx * iy;
-		const int bi = (e / M) * (M + 1) + e % M;
-		for(int sl = 0; sl < spg; sl++) {
-			const cx<R>* fs = f0 + sl * ss;
-			cx<R> v = ident ? fs[(size_t)c * N + p] : mk<R>(0, 0);
-			for(int t = 0; t < T.n; t++) v += T.c[t] * fs[(size_t)T.src[t] * N + T.tap[t]];
-			buf[sl * PITCH + bi] = v;
-		}
-	}
-	__syncthreads();
-	const cx<double>* ls = lsc + (((size_t)g * 2 + c) * Ny + iy) * 2;
-	const cx<double> r0 = ls[0], rden = ls[1];
-	const int i0 = lane * M;
-	const int last = n_unk - 1, lane_last = last / M, k_last = last % M;
-	const cx<R> one = mk<R>(1, 0), zero = mk<R>(0, 0);
-	for(int sl = warp; sl < spg; sl += NWp) {
-		cx<R>* b = buf + sl * PITCH + lane * (M + 1);
-		cx<R> v[M];
-		cx<R> A = one, B = zero;
-#pragma unroll
-		for(int k = 0; k < M; k++) {
-			v[k] = zero;
-			if(i0 + k < n_unk) {
-				cx<R> a = sf[F_A * 32 * M + k * 32 + lane];
-				cx<R> bb = b[k] * sf[F_RB * 32 * M + k * 32 + lane];
-				v[k] = bb;
-				B = a * B + bb;
-				A = a * A;
-			}
-		}
-#pragma unroll
-		for(int o = 1; o < 32; o <<= 1) {
-			cx<R> Ap = shfl_up_c(A, o), Bp = shfl_up_c(B, o);
-			if(lane >= o) { B = A * Bp + B; A = A * Ap; }
-		}
-		cx<R> d = shfl_up_c(B, 1);
-		if(lane == 0) d = zero;
-		cx<R> acc = zero, dl = zero;
-#pragma unroll
-		for(int k = 0; k < M; k++) {
-			if(i0 + k < n_unk) {
-				d = sf[F_A * 32 * M + k * 32 + lane] * d + v[k];
-				v[k] = d;
-				acc += sf[F_W * 32 * M + k * 32 + lane] * d;
-			}
-			if(k == k_last) dl = d;
-		}
-#pragma unroll
-		for(int o = 16; o > 0; o >>= 1) acc += shfl_xor_c(acc, o);
-		dl = shfl_idx_c(dl, lane_last);
-		const cx<R> fr = cvt<R>((cvt<double>(acc) - r0 * cvt<double>(dl)) * rden);
-		A = one;
-		B = zero;
-#pragma unroll
-		for(int k = M - 1; k >= 0; k--) {
-			if(i0 + k < n_unk) {
-				cx<R> cc = sf[F_C * 32 * M + k * 32 + lane];
-				B = cc * B + v[k];
-				A = cc * A;
-			}
-		}
-#pragma unroll
-		for(int o = 1; o < 32; o <<= 1) {
-			cx<R> An = shfl_down_c(A, o), Bn = shfl_down_c(B, o);
-			if(lane + o < 32) { B = A * Bn + B; A = A * An; }
-		}
-		d = shfl_down_c(B, 1);
-		if(lane == 31) d = zero;
-#pragma unroll
-		for(int k = M - 1; k >= 0; k--) {
-			if(i0 + k < n_unk) {
-				d = sf[F_C * 32 * M + k * 32 + lane] * d + v[k];
-				b[k] = d - fr * sf[F_COR * 32 * M + k * 32 + lane];
-			}
-		}
-	}
-	__syncthreads();
-	for(int sl = 0; sl < spg; sl++) {
-		const size_t off = (size_t)(g * spg + sl) * ss + (size_t)c * N + (size_t)iy * Nx;
-		for(int e = threadIdx.x; e < Nx; e += blockDim.x) {
-			int ee = e == Nx - 1 ? 0 : e;
-			cx<R> x = buf[sl * PITCH + (ee / M) * (M + 1) + ee % M];
-			if(dst) dst[off + e] = x;
-			if(acc_out) acc_out[off + e] = acc_in[off + e] + x;
-		}
 	}
 }
 
@@ -1085,8 +746,21 @@ __device__ __forceinline__ cx<R> shfl_xor_c(cx<R> v, int m) {
 // accesses stay coalesced; the factor planes are stored chunk-interleaved (element l*M+k at
 // k*32+l) and are also loaded once for the KS slots. Block = LT warps = LT lines.
 // ---------------------------------------------------------------------------------------
-// Chunk-parallel factorisation: the same outputs as k_factor, with every line split into
-// chunks processed by different threads. The pivots follow the continued fraction
+// Pre-factorisation of the periodic line solves (I - mu*R_cc) x = b per (group, comp, line), in
+// the plan's precision. Restates shifted_block_vmult_inv (BlockSparseMatrix.cpp:195-258 and
+// 386-449): Thomas sweep with beta0 = 2*mid0 and the Sherman-Morrison corner vector corr
+// (corr0 = -1/2). Everything that does not depend on the right-hand side is computed here once
+// per (wavelength, slab) and shared by all (q, pol) slots:
+//   F_A    alpha_i = -inf_i/beta_i   F_RB  1/beta_i        F_C   -gamma_i
+//   F_COR  corr_i after back-substitution
+//   F_W    w_i = prod_{j<i}(-gamma_j), so that the back-substituted x_0 = sum_i w_i d_i
+//          is formed during the forward sweep
+// plus per line r0 = inf0/mid0 and rden = 1/(1 + corr0 - r0*corr_{L-2}) in FP64. The forward
+// sweep of a solve is then d_i = alpha_i d_{i-1} + b_i/beta_i and the backward sweep
+// x_{i-1} = d_{i-1} - gamma_{i-1} x_i: both first-order affine recurrences whose coefficients
+// do not depend on b, which is what the chunked solves exploit.
+// Chunk-parallel form: every line is split into chunks processed by different threads. The
+// pivots follow the continued fraction
 // beta_i = mid'_i - inf_i sup_{i-1} / beta_{i-1}, a Moebius map: (p, q) -> M_i (p, q) with
 // M_i = [[mid'_i, -inf_i sup_{i-1}], [1, 0]] and beta = p / q. Each chunk forms the product of
 // its maps (rescaled to keep it bounded; the map is projective), the chunk products are
@@ -1714,6 +1388,100 @@ __global__ void __launch_bounds__(MAXT, NBPM_YC_MINB) k_solve_yc(Geom G, int slo
 					if(dst) dst[off + qe] = y;
 					if(KIND != ST_EXPL_X && acc_out)
 						acc_out[off + qe] = (acc_in2 ? acc_in[off + qe] + acc_in2[off + qe] : acc_in[off + qe]) + y;
+				}
+			}
+		}
+	}
+}
+
+// y-line solve fused with its right-hand side, sequential form: one thread per (column, KS
+// slots of one wavelength), both field components. Consecutive threads take consecutive columns,
+// so every load and store of a row is coalesced. The forward sweep
+//   d_i = alpha_i d_{i-1} + b_i / beta_i,   S = sum_i w_i d_i
+// stores d_i in scr (a field-sized buffer that none of the inputs alias: the output buffer
+// itself when there is one), the Sherman-Morrison factor f = (S - r0 d_{n-1}) rden is formed in
+// FP64, and the backward sweep x_i = d_i - gamma_i x_{i+1} turns d into the solution
+// x_i - f corr_i in place. Every thread is independent: no barriers, no cross-chunk combine,
+// and a tenth of the instructions per point of the chunked form (the stencil taps of the
+// neighbouring columns come from L1). Restates BlockSparseMatrixDY::shifted_block_vmult_inv
+// (BlockSparseMatrix.cpp:386-451) with the right-hand side of ParaxialPrimaryEvolutionOperator::
+// apply (ParaxialPrimaryEvolutionOperator.cpp:153-209) for KIND = ST_EXPL_X (explicit x
+// half-step) or ST_WOOD_Y (Woodbury term). Outputs: dst = x (may be null), acc_out =
+// (acc_in [+ acc_in2]) + x (may be null); row Ny-1 receives row 0 (period Ny-1).
+template <typename R, int KIND, int KS>
+__global__ void __launch_bounds__(128) k_solve_yq(Geom G, int nch, const cx<R>* __restrict__ coef,
+		const cx<R>* __restrict__ fac, size_t plane, const cx<double>* __restrict__ lsc,
+		const cx<R>* __restrict__ src, cx<R>* scr, cx<R>* dst, const cx<R>* acc_in, cx<R>* acc_out,
+		const cx<R>* acc_in2) {
+	const int Nx = G.Nx, Ny = G.Ny, N = G.N;
+	const int ix = blockIdx.x * blockDim.x + threadIdx.x;
+	if(ix >= Nx) return;
+	const int g = blockIdx.y / nch, ch = blockIdx.y % nch;
+	const int s0 = g * G.spg + ch * KS;
+	const int n = Ny - 1;
+	const size_t ss = 2 * (size_t)N;
+	const Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
+	const cx<R>* f0 = src + (size_t)s0 * ss;
+	const cx<R>* F0 = fac + ((size_t)g * 2 + 0) * NFAC * plane;
+	const cx<R>* F1 = fac + ((size_t)g * 2 + 1) * NFAC * plane;
+	cx<R>* sc = scr + (size_t)s0 * ss;
+	const cx<R> zero = mk<R>(0, 0);
+	cx<R> d0[KS], d1[KS], a0[KS], a1[KS];
+#pragma unroll
+	for(int j = 0; j < KS; j++) { d0[j] = zero; d1[j] = zero; a0[j] = zero; a1[j] = zero; }
+#pragma unroll 2
+	for(int i = 0; i < n; i++) {
+		const size_t q = (size_t)ix + (size_t)Nx * i;
+		cx<R> r0[KS], r1[KS];
+		composite_m<R, KIND, KS>(st, 0, ix, i, f0, r0);
+		composite_m<R, KIND, KS>(st, 1, ix, i, f0, r1);
+		const cx<R> A0 = F0[F_A * plane + q], B0 = F0[F_RB * plane + q], W0 = F0[F_W * plane + q];
+		const cx<R> A1 = F1[F_A * plane + q], B1 = F1[F_RB * plane + q], W1 = F1[F_W * plane + q];
+#pragma unroll
+		for(int j = 0; j < KS; j++) {
+			const cx<R> b0 = r0[j] * B0, b1 = r1[j] * B1;
+			d0[j] = A0 * d0[j] + b0;
+			d1[j] = A1 * d1[j] + b1;
+			a0[j] += W0 * d0[j];
+			a1[j] += W1 * d1[j];
+			sc[j * ss + q] = d0[j];
+			sc[j * ss + N + q] = d1[j];
+		}
+	}
+	const cx<double>* l0 = lsc + (((size_t)g * 2 + 0) * Nx + ix) * 2;
+	const cx<double>* l1 = lsc + (((size_t)g * 2 + 1) * Nx + ix) * 2;
+	const cx<double> r00 = l0[0], rd0 = l0[1], r01 = l1[0], rd1 = l1[1];
+	cx<R> fr0[KS], fr1[KS], x0[KS], x1[KS];
+#pragma unroll
+	for(int j = 0; j < KS; j++) {
+		fr0[j] = cvt<R>((cvt<double>(a0[j]) - r00 * cvt<double>(d0[j])) * rd0);
+		fr1[j] = cvt<R>((cvt<double>(a1[j]) - r01 * cvt<double>(d1[j])) * rd1);
+		x0[j] = zero;
+		x1[j] = zero;
+	}
+	const size_t qe = (size_t)ix + (size_t)Nx * n;
+#pragma unroll 2
+	for(int i = n - 1; i >= 0; i--) {
+		const size_t q = (size_t)ix + (size_t)Nx * i;
+		const cx<R> C0 = F0[F_C * plane + q], K0 = F0[F_COR * plane + q];
+		const cx<R> C1 = F1[F_C * plane + q], K1 = F1[F_COR * plane + q];
+#pragma unroll
+		for(int j = 0; j < KS; j++) {
+			const size_t o0 = (size_t)(s0 + j) * ss + q, o1 = o0 + N;
+			x0[j] = C0 * x0[j] + sc[j * ss + q];
+			x1[j] = C1 * x1[j] + sc[j * ss + N + q];
+			const cx<R> y0 = x0[j] - fr0[j] * K0, y1 = x1[j] - fr1[j] * K1;
+			if(dst) { dst[o0] = y0; dst[o1] = y1; }
+			if(KIND != ST_EXPL_X && acc_out) {
+				acc_out[o0] = (acc_in2 ? acc_in[o0] + acc_in2[o0] : acc_in[o0]) + y0;
+				acc_out[o1] = (acc_in2 ? acc_in[o1] + acc_in2[o1] : acc_in[o1]) + y1;
+			}
+			if(i == 0) {
+				const size_t e0 = (size_t)(s0 + j) * ss + qe, e1 = e0 + N;
+				if(dst) { dst[e0] = y0; dst[e1] = y1; }
+				if(KIND != ST_EXPL_X && acc_out) {
+					acc_out[e0] = (acc_in2 ? acc_in[e0] + acc_in2[e0] : acc_in[e0]) + y0;
+					acc_out[e1] = (acc_in2 ? acc_in[e1] + acc_in2[e1] : acc_in[e1]) + y1;
 				}
 			}
 		}

@@ -16,6 +16,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <deque>
+#include <map>
 #include <memory>
 #include <stdexcept>
 #include <mutex>
@@ -29,6 +30,7 @@
 #include "vti_writer.h"
 #include "host_settings.h"
 #include "solve_dispatch.cuh"
+#include "solve_config.h"
 
 namespace nbpm {
 
@@ -36,6 +38,68 @@ static thread_local std::string g_last_error;
 
 // Shared with the other translation units of the library.
 void set_last_error(const std::string& m) { g_last_error = m; }
+
+// Tuned line-solve configurations, per shape key (direction | precision | mesh | slots per
+// wavelength | wavelengths per pass | Woodbury steps | SMs), shared by every plan of the process.
+// With NBPM_TUNE_CACHE set to a file name, entries are read from that file when the cache is
+// first used and each new entry is appended to it, so later processes skip the timing runs.
+namespace {
+struct TuneCache {
+	std::mutex m;
+	std::map<std::string, std::string> entries;
+	bool loaded = false;
+	std::string file;
+};
+TuneCache& tune_cache() {
+	static TuneCache* c = new TuneCache();  // never destroyed (see plan_cache)
+	return *c;
+}
+void tune_cache_load(TuneCache& c) {
+	if(c.loaded) return;
+	c.loaded = true;
+	const char* f = std::getenv("NBPM_TUNE_CACHE");
+	if(!f || !*f) return;
+	c.file = f;
+	if(FILE* fp = std::fopen(f, "r")) {
+		char line[512];
+		while(std::fgets(line, sizeof line, fp)) {
+			std::string l(line);
+			while(!l.empty() && (l.back() == '\n' || l.back() == '\r')) l.pop_back();
+			size_t t = l.find('\t');
+			if(t != std::string::npos) c.entries[l.substr(0, t)] = l.substr(t + 1);
+		}
+		std::fclose(fp);
+	}
+}
+}  // namespace
+
+bool tune_cache_get(const std::string& key, std::string& val) {
+	TuneCache& c = tune_cache();
+	std::lock_guard<std::mutex> lk(c.m);
+	tune_cache_load(c);
+	auto it = c.entries.find(key);
+	if(it == c.entries.end()) return false;
+	val = it->second;
+	return true;
+}
+
+void tune_cache_put(const std::string& key, const std::string& val) {
+	TuneCache& c = tune_cache();
+	std::lock_guard<std::mutex> lk(c.m);
+	tune_cache_load(c);
+	c.entries[key] = val;
+	if(!c.file.empty())
+		if(FILE* fp = std::fopen(c.file.c_str(), "a")) {
+			std::fprintf(fp, "%s\t%s\n", key.c_str(), val.c_str());
+			std::fclose(fp);
+		}
+}
+
+void tune_cache_clear() {
+	TuneCache& c = tune_cache();
+	std::lock_guard<std::mutex> lk(c.m);
+	c.entries.clear();
+}
 
 #define CK(call)                                                                                   \
 	do {                                                                                           \
@@ -224,23 +288,9 @@ struct Plan : PlanBase {
 	double last_slab_ms = 0;
 	size_t smem_limit = 0;
 	int nsm = 152;  // streaming multiprocessors of the device (queried at setup)
-	bool shift_fused = true;  // one-pass transition kernel (NBPM_SHIFT_FUSED=0: four passes)
-	bool factor_seq = false;  // one thread per line factorisation (NBPM_FACTOR_SEQ=1)
-	// line-solve configuration per sample (chunk sizes of the parallel kernels; 0 = sequential)
-	// x: k_solve_xc with KSx slots per warp, or (NBPM_XMODE=1) the group-cooperative k_solve_xg
-	// (all slots of a wavelength per block) when its shared memory fits. y: ymode 0 = fused
-	// right-hand side (k_solve_yc with KSy slots per thread), 1 (NBPM_YMODE=1) = group-
-	// cooperative k_rhs + k_solve_yc(GIVEN). Defaults measured fastest on GB300.
-	struct SolveCfg {
-		int Mx = 0, My = 0, WY = 0, KSx = 1, KSy = 1;
-		bool xg = false;
-		bool ys = false;  // y-lines too long for k_solve_yc: k_solve_ys with scratch-held chunks
-		bool xs = false;  // x-lines with long chunks: k_solve_xs with the chunks in shared memory
-		int WPLx = 1;     // warps per x-line (k_solve_xw when > 1: 32*WPLx chunks of Mx points)
-		bool y1024w = false;  // Woodbury y-solves with 32 warps of 8-row chunks, 2 slots per thread
-		int ymode = 0;
-		size_t plane_x = 0, plane_y = 0, smem_xg = 0;
-	};
+	// Line-solve configuration per sample (solve_config.h): forced by opts.solve_config, timed
+	// per shape by tune() (opts.tune), or the rule-based default.
+	std::vector<std::string> tune_notes;  // per sample: how its configuration was chosen
 	DevBuf T3;
 	std::vector<SolveCfg> scfg;
 
@@ -386,18 +436,17 @@ struct Plan : PlanBase {
 			(int)((size_t)16 * 32 * 8 * sizeof(cx<R>) + 64 * sizeof(cx<R>))));
 		CK(cudaFuncSetAttribute(k_shift_fused<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 			(int)((size_t)4 * (SHT + 6) * (SHT + 6) * sizeof(cx<R>))));
-		if(const char* e = std::getenv("NBPM_SHIFT_FUSED")) shift_fused = std::atoi(e) != 0;
-		if(const char* e = std::getenv("NBPM_FACTOR_SEQ")) factor_seq = std::atoi(e) != 0;
 		if(sizeof(R) == sizeof(float)) {
-			set_solve_smem_x_f32((int)smem_limit); set_solve_smem_y_f32((int)smem_limit); set_solve_smem_xg_f32((int)smem_limit);
+			set_solve_smem_x_f32((int)smem_limit); set_solve_smem_y_f32((int)smem_limit);
 			set_solve_smem_xs_f32((int)smem_limit); set_solve_smem_xw_f32((int)smem_limit);
 		}
 		else {
-			set_solve_smem_x_f64((int)smem_limit); set_solve_smem_y_f64((int)smem_limit); set_solve_smem_xg_f64((int)smem_limit);
+			set_solve_smem_x_f64((int)smem_limit); set_solve_smem_y_f64((int)smem_limit);
 			set_solve_smem_xs_f64((int)smem_limit); set_solve_smem_xw_f64((int)smem_limit);
 		}
 		CK(cudaGetLastError());
 		allocate();
+		choose_configs();
 	}
 
 	int gpp(const SampleHost& h) const {
@@ -412,92 +461,31 @@ struct Plan : PlanBase {
 		else b.alloc(bytes);
 	}
 
+	SolveShape shape_of(const SampleHost& h) const {
+		SolveShape sh;
+		sh.Nx = h.s.Nx; sh.Ny = h.s.Ny; sh.spg = h.spg; sh.ng = gpp(h);
+		sh.fp32 = sizeof(R) == sizeof(float); sh.nsm = nsm;
+		if(smem_limit) sh.smem = smem_limit;
+		return sh;
+	}
+
 	void allocate() {
 		scfg.clear();
 		dev_bytes = 0;
+		bool need_t3 = false;
 		size_t maxT = 0, maxQ = 0, maxC = 0, maxD = 0, maxFx = 0, maxL = 0, maxScr = 0, maxStage = 0;
 		for(auto& hp : S) {
 			SampleHost& h = *hp;
 			size_t N = h.geom.N;
 			int ng = gpp(h);
-			SolveCfg sc;
-			int ux = h.s.Nx - 1, uy = h.s.Ny - 1;
-			if(h.s.Nx > 3) {
-				for(int M = 2; M <= 32; M *= 2) if(32 * M >= ux) { sc.Mx = M; break; }
-				// long lines: several warps per line with 8-point chunks (k_solve_xw), unless
-				// NBPM_XW=0
-				const char* exw = std::getenv("NBPM_XW");
-				if(ux > 256 && ux <= 8 * 256 && !(exw && std::atoi(exw) == 0)) { sc.Mx = 8; sc.WPLx = (ux + 255) / 256; }
-			}
-			if(h.s.Ny > 3) {
-				// block of 32 columns x WY <= 16 warps (<= 512 threads, <= 128 registers)
-				int wmax = 16;
-				if(const char* e = std::getenv("NBPM_YWMAX")) wmax = std::min(16, std::max(1, std::atoi(e)));
-				for(int M = 2; M <= 32; M *= 2) if((uy + M - 1) / M <= wmax) { sc.My = M; break; }
-				if(sc.My) sc.WY = (uy + sc.My - 1) / sc.My;
-				// Woodbury y-solves of 129-256-row lines: 32 warps of 8-row chunks, two slots per
-				// thread (1024-thread blocks), measured faster on GB300 than 16 warps of 16 rows;
-				// the explicit-step solve keeps the 16-warp form. NBPM_Y1024=0 disables.
-				const char* ey = std::getenv("NBPM_Y1024");
-				if(sizeof(R) == sizeof(float) && uy > 128 && uy <= 256 && !(ey && std::atoi(ey) == 0) && h.spg % 2 == 0)
-					sc.y1024w = true;
-			}
-			// slots per thread: largest KS dividing 2*Nq with a compiled (M, KS) instance
-			// per-thread chunk values (M*KS complex) kept within 32 FP32 / 16 FP64 complex registers
-			const int cap = sizeof(R) == sizeof(float) ? 32 : 16;
-			int kmx = 4, kmy = 4;
-			if(const char* e = std::getenv("NBPM_KSX")) kmx = std::max(1, std::atoi(e));
-			if(const char* e = std::getenv("NBPM_KSY")) kmy = std::max(1, std::atoi(e));
-			auto pick_ks = [&](int M, int kmax) {
-				for(int ks : {4, 2, 1})
-					if(ks <= kmax && h.spg % ks == 0 && solve_pair_ok(M, ks) && (M * ks <= cap || ks == 1)) return ks;
-				return 0;
-			};
-			if(sc.Mx) { sc.KSx = pick_ks(sc.Mx, kmx); if(!sc.KSx) sc.Mx = 0; }
-			if(sc.My) { sc.KSy = pick_ks(sc.My, kmy); if(!sc.KSy) { sc.My = 0; sc.WY = 0; sc.y1024w = false; } }
-			// small grids leave SMs idle: fewer slots per thread, more blocks (unless the slots
-			// per thread are set through NBPM_KSX / NBPM_KSY)
-			{
-				const size_t want = 2 * (size_t)nsm;
-				auto xblocks = [&](int ks) { return (size_t)((h.s.Ny + 3) / 4) * 2 * ng * (h.spg / ks); };
-				auto yblocks = [&](int ks) { return (size_t)((h.s.Nx + 31) / 32) * 2 * ng * (h.spg / ks); };
-				if(sc.Mx && sc.WPLx == 1 && !std::getenv("NBPM_KSX"))
-					while(sc.KSx > 1 && xblocks(sc.KSx) < want && solve_pair_ok(sc.Mx, sc.KSx / 2)) sc.KSx /= 2;
-				if(sc.My && !std::getenv("NBPM_KSY"))
-					while(sc.KSy > 1 && yblocks(sc.KSy) < want && solve_pair_ok(sc.My, sc.KSy / 2)) sc.KSy /= 2;
-				if(sc.KSy < 2) sc.y1024w = false;
-				// FP64 (bound by the FP64 pipe) with short y-lines on few blocks: k_solve_ys with one
-				// slot per thread, measured 2x faster on GB300 for 64x64 meshes
-				if(sizeof(R) == sizeof(double) && sc.My && sc.My <= 4 && yblocks(1) < (size_t)nsm &&
-						!std::getenv("NBPM_YS")) {
-					sc.My = 0; sc.WY = 0; sc.ys = true; sc.KSy = 1;
-				}
-			}
-			if(kmy < 2) sc.y1024w = false;
-			if(const char* e = std::getenv("NBPM_YS")) if(std::atoi(e) == 1 && h.s.Ny > 3) { sc.My = 0; sc.WY = 0; }
-			if(sc.WPLx == 1 && (sc.Mx >= 32 || (sc.Mx && std::getenv("NBPM_XS") && std::atoi(std::getenv("NBPM_XS")) == 1))) {
-				sc.xs = true;
-				sc.KSx = 1;
-				for(int ks : {4, 2}) if(ks <= kmx && h.spg % ks == 0 && (size_t)4 * ks * 32 * (sc.Mx + 1) * sizeof(cx<R>) <= 100 * 1024) { sc.KSx = ks; break; }
-			}
-			// y-lines beyond the chunked kernel's reach (Ny > 513) use the one-thread-per-column
-			// solve, measured faster on GB300 than k_solve_ys for 1024-row meshes; NBPM_YS=1
-			// selects k_solve_ys for every mesh.
-			if(h.s.Ny > 3 && sc.My == 0 && std::getenv("NBPM_YS") && std::atoi(std::getenv("NBPM_YS")) == 1) {
-				sc.ys = true;
-				sc.KSy = 1;
-				for(int ks : {4, 2}) if(ks <= kmy && h.spg % ks == 0) { sc.KSy = ks; break; }
-			}
-			if(opt.verbose)
-				std::printf("line solves: x M=%d KS=%d, y M=%d WY=%d KS=%d\n", sc.Mx, sc.KSx, sc.My, sc.WY, sc.KSy);
-			sc.plane_x = sc.Mx ? std::max(N, (size_t)h.s.Ny * 32 * sc.WPLx * sc.Mx) : N;
-			if(sc.Mx) {
-				sc.smem_xg = ((size_t)h.spg * 32 * (sc.Mx + 1) + (size_t)NFAC * 32 * sc.Mx) * sizeof(cx<R>);
-				sc.xg = false;  // measured slower than k_solve_xc on the 256x256 batched workload
-			}
-			if(const char* e = std::getenv("NBPM_XMODE")) sc.xg = sc.Mx && sc.smem_xg <= smem_limit && std::atoi(e) == 1;
-			if(const char* e = std::getenv("NBPM_YMODE")) sc.ymode = std::atoi(e);
-			sc.plane_y = N;
+			const SolveShape sh = shape_of(h);
+			SolveCfg sc = heuristic(sh);
+			// buffers sized for every candidate the tuner may pick
+			size_t px = sc.plane_x;
+			for(auto& c : x_candidates(sh)) px = std::max(px, c.plane_x);
+			sc.plane_x = px;
+			for(auto& c : y_candidates(sh)) need_t3 |= c.ys;
+			need_t3 |= sc.ys;
 			scfg.push_back(sc);
 			maxT = std::max(maxT, (size_t)ng * h.spg * 2 * N);
 			maxQ = std::max(maxQ, (size_t)2 * ng * NQ * N);
@@ -531,8 +519,6 @@ struct Plan : PlanBase {
 		}
 		dalloc(T, sizeof(cx<R>) * maxT);
 		dalloc(T2, sizeof(cx<R>) * maxT);
-		bool need_t3 = false;
-		for(auto& c : scfg) need_t3 |= (c.My > 0 && c.ymode == 1) || c.ys;
 		if(need_t3) dalloc(T3, sizeof(cx<R>) * maxT);
 		dalloc(Qring, sizeof(R) * maxQ);
 		dalloc(coef, sizeof(cx<R>) * maxC);
@@ -547,6 +533,119 @@ struct Plan : PlanBase {
 		dalloc(stage, sizeof(cx<double>) * maxStage);
 		dev_bytes += T.bytes + T2.bytes + Qring.bytes + coef.bytes + diag.bytes + facx.bytes + facy.bytes +
 			lscx.bytes + lscy.bytes + scr.bytes + stage.bytes + T3.bytes;
+	}
+
+	// ---- line-solve configuration: forced, tuned or rule-based ----
+	void choose_configs() {
+		tune_notes.assign(S.size(), std::string());
+		const std::string forced = opt.solve_config ? std::string(opt.solve_config) : std::string();
+		bool zeroed = false;
+		for(auto& hp : S) {
+			SampleHost& h = *hp;
+			const SolveShape sh = shape_of(h);
+			SolveCfg& sc = scfg[h.index];
+			const size_t pmax = sc.plane_x;
+			const auto xc = x_candidates(sh), yc = y_candidates(sh);
+			if(!forced.empty()) {
+				size_t k = forced.find(';');
+				std::string fx = forced.substr(0, k), fy = k == std::string::npos ? "auto" : forced.substr(k + 1);
+				auto pick = [&](const std::vector<SolveCfg>& cands, const std::string& want, bool x) {
+					for(auto& c : cands) if((x ? c.xstr() : c.ystr()) == want) { if(x) sc.set_x(c); else sc.set_y(c); return; }
+					std::string all;
+					for(auto& c : cands) all += (all.empty() ? "" : ", ") + (x ? c.xstr() : c.ystr());
+					throw BackendError(E_ARG, "solve configuration '" + want + "' is not a candidate for the " +
+						std::to_string(h.s.Nx) + "x" + std::to_string(h.s.Ny) + " mesh with " + std::to_string(h.spg) +
+						" slots per wavelength (candidates: " + all + ")");
+				};
+				if(fx != "auto") pick(xc, fx, true);
+				if(fy != "auto") pick(yc, fy, false);
+				tune_notes[h.index] = "forced";
+				if(fx != "auto" && fy != "auto") { sc.plane_x = pmax; continue; }
+			}
+			if(opt.tune == 0 || (xc.size() <= 1 && yc.size() <= 1)) {
+				if(tune_notes[h.index].empty()) tune_notes[h.index] = "rule-based";
+				sc.plane_x = pmax;
+				continue;
+			}
+			if(!zeroed) { zero_workspace(); zeroed = true; }
+			const std::string key = tune_key(h);
+			std::string note;
+			for(int dirn = 0; dirn < 2; dirn++) {
+				if(!forced.empty() && (dirn == 0 ? forced.substr(0, forced.find(';')) != "auto"
+						: (forced.find(';') != std::string::npos && forced.substr(forced.find(';') + 1) != "auto")))
+					continue;
+				const auto& cands = dirn == 0 ? xc : yc;
+				std::string hit;
+				if(tune_cache_get((dirn == 0 ? "x|" : "y|") + key, hit)) {
+					for(auto& c : cands)
+						if((dirn == 0 ? c.xstr() : c.ystr()) == hit) { if(dirn == 0) sc.set_x(c); else sc.set_y(c); }
+					note += std::string(dirn == 0 ? "x" : "y") + " cached " + hit + "; ";
+					continue;
+				}
+				const SolveCfg keep = sc;
+				double best = 1e300;
+				SolveCfg win = sc;
+				std::string times;
+				for(auto& c : cands) {
+					SolveCfg t = keep;
+					if(dirn == 0) t.set_x(c); else t.set_y(c);
+					t.plane_x = pmax;
+					sc = t;
+					double ms = time_direction(h, dirn);
+					char b[96];
+					std::snprintf(b, sizeof b, "%s %.3f ms", (dirn == 0 ? c.xstr() : c.ystr()).c_str(), ms);
+					times += (times.empty() ? "" : ", ") + std::string(b);
+					if(ms < best) { best = ms; win = t; }
+				}
+				sc = win;
+				const std::string ws = dirn == 0 ? win.xstr() : win.ystr();
+				tune_cache_put((dirn == 0 ? "x|" : "y|") + key, ws);
+				note += std::string(dirn == 0 ? "x" : "y") + " tuned " + ws + " [" + times + "]; ";
+			}
+			sc.plane_x = pmax;
+			tune_notes[h.index] = (tune_notes[h.index].empty() ? "" : tune_notes[h.index] + ", ") + note;
+			if(opt.verbose) std::printf("line solves %s: %s\n", sc.str().c_str(), note.c_str());
+		}
+		launches = 0;
+	}
+
+	std::string tune_key(const SampleHost& h) const {
+		char b[160];
+		std::snprintf(b, sizeof b, "%s|%dx%d|spg%d|ng%d|nw%d|sm%d", sizeof(R) == sizeof(float) ? "fp32" : "fp64", h.s.Nx,
+			h.s.Ny, h.spg, gpp(h), h.s.n_woodbury, nsm);
+		return b;
+	}
+
+	// Zeroes the workspace the timing runs read (their values do not change the kernels' speed,
+	// but uninitialised memory could hold NaN or denormal patterns).
+	void zero_workspace() {
+		for(DevBuf* b : {&T, &T2, &T3, &coef, &facx, &facy, &lscx, &lscy})
+			if(b->p) CK(cudaMemsetAsync(b->p, 0, b->bytes, stream));
+		for(auto& hp : S) CK(cudaMemsetAsync(hp->F.p, 0, hp->F.bytes, stream));
+		CK(cudaStreamSynchronize(stream));
+	}
+
+	// Device time of one slab's solves of one direction with the current configuration of
+	// sample h (explicit step + Woodbury iterates, eager launches on the main stream): the best of
+	// three runs after one warm-up.
+	double time_direction(SampleHost& h, int dirn) {
+		const Geom Gm = h.geom;
+		const int ng = gpp(h), nsl = ng * h.spg;
+		cx<R>* Fp = h.F.as<cx<R>>();
+		fx_cur = facx.as<cx<R>>(); fy_cur = facy.as<cx<R>>();
+		lx_cur = lscx.as<cx<double>>(); ly_cur = lscy.as<cx<double>>();
+		cs = stream;
+		float best = 1e30f;
+		for(int r = 0; r < 4; r++) {
+			CK(cudaEventRecord(ev[2], stream));
+			rec_adi(h, Gm, 0, nsl, ng, h.s.n_woodbury, coef.as<cx<R>>(), Fp, T.as<cx<R>>(), T2.as<cx<R>>(), Fp, dirn);
+			CK(cudaEventRecord(ev[3], stream));
+			CK(cudaEventSynchronize(ev[3]));
+			float ms = 0;
+			CK(cudaEventElapsedTime(&ms, ev[2], ev[3]));
+			if(r > 0) best = std::min(best, ms);
+		}
+		return best;
 	}
 
 	void upload() override {
@@ -831,25 +930,17 @@ struct Plan : PlanBase {
 			if(iz >= 2) CK(cudaStreamWaitEvent(streamB, eAdi[iz & 1], 0));
 			int lx_n = ng * 2 * Ny, ly_n = ng * 2 * Nx;
 			const double fb = (double)N * ng * 2 * (3 * sc + NFAC * sc + 4 * sc);
-			if(factor_seq) {
-				launch("factor", 2 * fb, [&] {
-					k_factor<R><<<(lx_n + ly_n + 63) / 64, 64, 0, cs>>>(Gm, ng, scf.Mx, 32 * scf.WPLx, ps.Dg, fx, scf.plane_x, lx, fy,
-						scf.plane_y, ly, scr.as<cx<R>>());
-				});
-			}
-			else {
-				// y factorisation: 8 chunk warps per 32 columns, 16 when the grid leaves SMs idle
-				const int LT = 4, WF = ((Nx + 31) / 32) * 2 * ng < nsm && Ny - 1 >= 256 ? 16 : 8;
-				launch("factor_x", fb, [&] {
-					k_factor_chunked<R, 0><<<dim3((unsigned)((Ny + LT - 1) / LT), (unsigned)(ng * 2)), dim3(32, LT), 0, cs>>>(
-						Gm, ng, scf.Mx, 32 * scf.WPLx, 1, ps.Dg, fx, scf.plane_x, lx);
-				});
-				size_t smem = (size_t)WF * 32 * 8 * sizeof(cx<R>) + 64 * sizeof(cx<R>);
-				launch("factor_y", fb, [&] {
-					k_factor_chunked<R, 1><<<dim3((unsigned)((Nx + 31) / 32), (unsigned)(ng * 2)), dim3(32, WF), smem, cs>>>(
-						Gm, ng, 0, 32, WF, ps.Dg, fy, scf.plane_y, ly);
-				});
-			}
+			// y factorisation: 8 chunk warps per 32 columns, 16 when the grid leaves SMs idle
+			const int LT = 4, WF = ((Nx + 31) / 32) * 2 * ng < nsm && Ny - 1 >= 256 ? 16 : 8;
+			launch("factor_x", fb, [&] {
+				k_factor_chunked<R, 0><<<dim3((unsigned)((Ny + LT - 1) / LT), (unsigned)(ng * 2)), dim3(32, LT), 0, cs>>>(
+					Gm, ng, scf.Mx, 32 * scf.WPLx, 1, ps.Dg, fx, scf.plane_x, lx);
+			});
+			size_t smem = (size_t)WF * 32 * 8 * sizeof(cx<R>) + 64 * sizeof(cx<R>);
+			launch("factor_y", fb, [&] {
+				k_factor_chunked<R, 1><<<dim3((unsigned)((Nx + 31) / 32), (unsigned)(ng * 2)), dim3(32, WF), smem, cs>>>(
+					Gm, ng, 0, 32, WF, ps.Dg, fy, scf.plane_y, ly);
+			});
 			CK(cudaEventRecord(eFac, streamB));
 			// ---- main stream ----
 			cs = stream;
@@ -987,7 +1078,7 @@ struct Plan : PlanBase {
 			});
 			return Fp;
 		}
-		if(CB && scfg[h.index].Mx > 0 && shift_fused) {
+		if(CB && scfg[h.index].Mx > 0) {
 			const int nsh = two_shifts ? 2 : 1;
 			dim3 grid((unsigned)((Gm.Nx + SHT - 1) / SHT), (unsigned)((Gm.Ny + SHT - 1) / SHT), (unsigned)nsl);
 			size_t smem = (size_t)4 * (SHT + 6) * (SHT + 6) * sizeof(cx<R>);
@@ -1038,12 +1129,14 @@ struct Plan : PlanBase {
 	// Whether the fused solve of direction dirn runs k_solve_xc / k_solve_yc, the kernels that take
 	// a second accumulator input.
 	bool solve_takes_acc2(const SolveCfg& sc, int dirn) const {
-		return dirn == 0 ? (sc.Mx > 0 && !sc.xg && sc.WPLx == 1 && !sc.xs) : (sc.My > 0 && !sc.ys);
+		return dirn == 0 ? (sc.Mx > 0 && sc.WPLx == 1 && !sc.xs) : (sc.yq > 0 || (sc.My > 0 && !sc.ys));
 	}
 
+	// scr: a field-sized buffer the solve may overwrite (none of src, acc_in, acc_in2), used by the
+	// sequential y solve for its forward values.
 	void rec_solve_fused(int dirn, bool wood, SampleHost& h, const Geom& Gm, int slot0, int nsl, int ng,
 			const cx<R>* C, const cx<R>* src, cx<R>* dst, const cx<R>* acc_in, cx<R>* acc_out,
-			const cx<R>* acc_in2 = nullptr) {
+			const cx<R>* acc_in2, cx<R>* scr) {
 		const SolveCfg& sc = scfg[h.index];
 		const double sz = sizeof(cx<R>);
 		double fp = (double)Gm.N * nsl * 2 * sz;
@@ -1057,17 +1150,6 @@ struct Plan : PlanBase {
 		L.stream = cs;
 		if(dirn == 0) {
 			L.M = sc.Mx; L.kind = wood ? ST_WOOD_X : ST_EXPL_Y;
-			if(sc.xg) {
-				L.KS = 0;
-				L.grid = dim3((unsigned)Gm.Ny, (unsigned)(ng * 2));
-				L.block = dim3(256);
-				L.smem = sc.smem_xg;
-				launch(wood ? "wood_solve_x" : "expl_solve_x", bytes, [&] {
-					if(!launch_solve_xg<R>(L, Gm, slot0, C, fx_cur, sc.plane_x, lx_cur, src, dst, acc_in, acc_out))
-						throw BackendError(E_INTERNAL, "no x-solve instance");
-				});
-				return;
-			}
 			const int LT = 4;
 			L.KS = sc.KSx;
 			int nch = h.spg / L.KS;
@@ -1100,18 +1182,19 @@ struct Plan : PlanBase {
 					throw BackendError(E_INTERNAL, "no x-solve instance");
 			});
 		}
+		else if(sc.yq) {
+			L.KS = sc.yq; L.kind = wood ? ST_WOOD_Y : ST_EXPL_X;
+			const int nch = h.spg / L.KS;
+			L.block = dim3(128);
+			L.grid = dim3((unsigned)((Gm.Nx + 127) / 128), (unsigned)(ng * nch));
+			L.smem = 0;
+			if(!scr || scr == src || scr == acc_in || scr == acc_in2) throw BackendError(E_INTERNAL, "y-solve scratch aliases an input");
+			launch(wood ? "wood_solve_y" : "expl_solve_y", bytes, [&] {
+				if(!launch_solve_yq<R>(L, Gm, nch, C, fy_cur, sc.plane_y, ly_cur, src, scr, dst, acc_in, acc_out, acc_in2))
+					throw BackendError(E_INTERNAL, "no y-solve instance");
+			});
+		}
 		else {
-			const cx<R>* rsrc = src;
-			if(sc.ymode == 1) {
-				// right-hand sides for all slots of each group, then a plain chunked solve
-				cx<R>* R3 = T3.as<cx<R>>();
-				launch(wood ? "wood_rhs_y" : "expl_rhs_y", fp * 2 + (double)Gm.N * ng * (wood ? 14 : 20) * sz, [&] {
-					dim3 gr((unsigned)((Gm.N + 255) / 256), (unsigned)(ng * 2));
-					if(wood) k_rhs<R, ST_WOOD_Y><<<gr, 256, 0, cs>>>(Gm, slot0, C, src, R3);
-					else k_rhs<R, ST_EXPL_X><<<gr, 256, 0, cs>>>(Gm, slot0, C, src, R3);
-				});
-				rsrc = R3;
-			}
 			if(sc.ys) {
 				const int WS = 8;
 				L.M = 0; L.KS = sc.KSy; L.kind = wood ? ST_WOOD_Y : ST_EXPL_X;
@@ -1126,9 +1209,9 @@ struct Plan : PlanBase {
 				});
 				return;
 			}
-			L.M = sc.My; L.KS = sc.KSy; L.kind = sc.ymode == 1 ? ST_GIVEN : (wood ? ST_WOOD_Y : ST_EXPL_X);
+			L.M = sc.My; L.KS = sc.KSy; L.kind = wood ? ST_WOOD_Y : ST_EXPL_X;
 			int WY = sc.WY;
-			if(wood && sc.y1024w && sc.ymode != 1) {
+			if(wood && sc.y1024w) {
 				L.M = 8; L.KS = 2;
 				WY = (Gm.Ny - 1 + 7) / 8;
 			}
@@ -1139,7 +1222,7 @@ struct Plan : PlanBase {
 			if(yc_values_in_smem(L.M, L.KS, WY > 16 ? 1024 : 512, (int)sizeof(cx<R>)))
 				L.smem += (size_t)L.KS * L.M * WY * 32 * sizeof(cx<R>);  // chunk values
 			launch(wood ? "wood_solve_y" : "expl_solve_y", bytes, [&] {
-				if(!launch_solve_yc<R>(L, Gm, slot0, nch, C, fy_cur, sc.plane_y, ly_cur, rsrc,
+				if(!launch_solve_yc<R>(L, Gm, slot0, nch, C, fy_cur, sc.plane_y, ly_cur, src,
 						dst, acc_in, acc_out, acc_in2))
 					throw BackendError(E_INTERNAL, "no y-solve instance");
 			});
@@ -1147,19 +1230,21 @@ struct Plan : PlanBase {
 	}
 
 	// ParaxialPrimaryEvolutionOperator::apply (ParaxialPrimaryEvolutionOperator.cpp:153-209).
+	// only_dirn >= 0: that direction's solves alone (the tuner's timing runs).
 	void rec_adi(SampleHost& h, const Geom& Gm, int slot0, int nsl, int ng, int Nw, const cx<R>* C, cx<R>* Fp,
-			cx<R>* Tb, cx<R>* T2b, const cx<R>* xsrc) {
+			cx<R>* Tb, cx<R>* T2b, const cx<R>* xsrc, int only_dirn = -1) {
 		const int N = Gm.N;
 		const double sc = sizeof(cx<R>);
 		dim3 gr = pgrid(N, nsl);
 		const double fp = (double)N * nsl;
 		const SolveCfg& cfg = scfg[h.index];
 		for(int dirn = 0; dirn < 2; dirn++) {
-			bool fused = dirn == 0 ? cfg.Mx > 0 : (cfg.My > 0 || cfg.ys);
+			if(only_dirn >= 0 && dirn != only_dirn) continue;
+			bool fused = dirn == 0 ? cfg.Mx > 0 : (cfg.My > 0 || cfg.ys || cfg.yq > 0);
 			if(fused) {
 				// t0 = solve(f + mu R f) written to T; Woodbury: t_k = solve(mu R' t_{k-1}),
 				// F = t0 + t1 + ... accumulated by the solves (the last t_k is not stored).
-				rec_solve_fused(dirn, false, h, Gm, slot0, nsl, ng, C, dirn == 0 ? xsrc : Fp, Tb, nullptr, nullptr);
+				rec_solve_fused(dirn, false, h, Gm, slot0, nsl, ng, C, dirn == 0 ? xsrc : Fp, Tb, nullptr, nullptr, nullptr, Tb);
 			}
 			else {
 				if(dirn == 0)
@@ -1187,11 +1272,12 @@ struct Plan : PlanBase {
 			for(int it = 1; it <= Nw; it++) {
 				const cx<R>* ai = it == 1 ? Tb : Fp;
 				if(acc2) {
-					if(it == 1) rec_solve_fused(dirn, true, h, Gm, slot0, nsl, ng, C, cur, oth, nullptr, nullptr);
-					else rec_solve_fused(dirn, true, h, Gm, slot0, nsl, ng, C, cur, nullptr, Tb, Fp, cur);
+					if(it == 1) rec_solve_fused(dirn, true, h, Gm, slot0, nsl, ng, C, cur, oth, nullptr, nullptr, nullptr, oth);
+					else rec_solve_fused(dirn, true, h, Gm, slot0, nsl, ng, C, cur, nullptr, Tb, Fp, cur, Fp);
 				}
 				else if(fused) {
-					rec_solve_fused(dirn, true, h, Gm, slot0, nsl, ng, C, cur, it == Nw ? nullptr : oth, ai, Fp);
+					// oth holds t_{it-2} (or nothing), no longer needed: free for the forward values
+					rec_solve_fused(dirn, true, h, Gm, slot0, nsl, ng, C, cur, it == Nw ? nullptr : oth, ai, Fp, nullptr, oth);
 				}
 				else {
 					if(dirn == 0)
@@ -1326,6 +1412,13 @@ struct Plan : PlanBase {
 		return true;
 	}
 
+	bool solve_config(int sample, std::string& cfg, std::string& note) const override {
+		if(sample < 0 || sample >= (int)S.size() || sample >= (int)scfg.size()) return false;
+		cfg = scfg[sample].str();
+		note = sample < (int)tune_notes.size() ? tune_notes[sample] : std::string();
+		return true;
+	}
+
 	bool fields_view(int sample, PlanFieldsView& v) const override {
 		if(sample < 0 || sample >= (int)S.size()) return false;
 		const SampleHost& h = *S[sample];
@@ -1390,6 +1483,8 @@ void nbpm_default_options(nbpm_options* o) {
 	o->use_graph = 1;
 	o->device = 0;
 	o->verbose = 0;
+	o->tune = 1;
+	o->solve_config = nullptr;
 }
 
 const char* nbpm_last_error(void) { return g_last_error.c_str(); }
@@ -1497,6 +1592,56 @@ int nbpm_plan_profile(nbpm_plan* p, char (*names)[48], double* ms, int* launches
 
 long long nbpm_plan_device_bytes(const nbpm_plan* p) { return p ? p->impl->device_bytes() : 0; }
 
+static void copy_out(const std::string& src, char* dst, int n) {
+	if(!dst || n <= 0) return;
+	std::snprintf(dst, (size_t)n, "%s", src.c_str());
+}
+
+int nbpm_plan_solve_config(const nbpm_plan* p, int sample, char* config, int n_config, char* report, int n_report) {
+	API_GUARD({
+		if(!p || !config || n_config <= 0) return fail(E_ARG, "null argument");
+		std::string c, note;
+		if(!p->impl->solve_config(sample, c, note)) return fail(E_ARG, "sample index out of range");
+		copy_out(c, config, n_config);
+		copy_out(note, report, n_report);
+		return 0;
+	})
+}
+
+int nbpm_solve_candidates(const char* json_str, int precision, int groups_per_pass, char* out, int n) {
+	g_last_error.clear();
+	API_GUARD({
+		if(!json_str || !out || n <= 0) return fail(E_ARG, "null argument");
+		if(precision != NBPM_FP64 && precision != NBPM_FP32) return fail(E_ARG, "unknown precision");
+		BackendSettings s = parse_settings(json_str);
+		SolveShape sh;
+		sh.Nx = s.Nx; sh.Ny = s.Ny; sh.spg = 2 * (int)s.q.size();
+		int G = (int)s.wavelengths.size();
+		sh.ng = groups_per_pass <= 0 ? G : std::max(1, std::min(groups_per_pass, G));
+		sh.fp32 = precision == NBPM_FP32;
+		int dev = 0, v = 0;
+		if(cudaGetDevice(&dev) == cudaSuccess) {
+			if(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0) sh.nsm = v;
+			if(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) == cudaSuccess && v > 0) sh.smem = (size_t)v;
+		}
+		cudaGetLastError();
+		std::string r = "x=";
+		auto xs = x_candidates(sh), ys = y_candidates(sh);
+		for(size_t i = 0; i < xs.size(); i++) r += (i ? "|" : "") + xs[i].xstr();
+		r += "\ny=";
+		for(size_t i = 0; i < ys.size(); i++) r += (i ? "|" : "") + ys[i].ystr();
+		r += "\ndefault=" + heuristic(sh).str();
+		if((int)r.size() >= n) return fail(E_SIZE, "output buffer too small");
+		copy_out(r, out, n);
+		return 0;
+	})
+}
+
+int nbpm_tune_cache_clear(void) {
+	tune_cache_clear();
+	return 0;
+}
+
 int nbpm_plan_destroy(nbpm_plan* p) {
 	delete p;
 	return 0;
@@ -1525,7 +1670,8 @@ std::string plan_key(int n, const nbpm_sample* s, const nbpm_options* opts) {
 	nbpm_default_options(&o);
 	if(opts) o = *opts;
 	std::string k = std::to_string(o.precision) + "/" + std::to_string(o.groups_per_pass) + "/" +
-		std::to_string(o.use_graph) + "/" + std::to_string(o.device) + "/" + std::to_string(o.verbose);
+		std::to_string(o.use_graph) + "/" + std::to_string(o.device) + "/" + std::to_string(o.verbose) + "/" +
+		std::to_string(o.tune) + "/" + (o.solve_config ? o.solve_config : "");
 	for(int i = 0; i < n; i++) {
 		if(!s[i].json_str) return std::string();
 		k += "|" + std::to_string(s[i].n_lc_vals) + "/" + std::to_string(s[i].n_E_vals) + "/" +

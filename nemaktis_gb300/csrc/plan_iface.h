@@ -56,6 +56,9 @@ struct PlanBase {
 	virtual double slab_ms() const = 0;
 	virtual void profile(std::vector<std::string>& names, std::vector<double>& ms, std::vector<int>& cnt,
 		std::vector<double>& bytes) = 0;
+	// Line-solve configuration of a sample ("<x>;<y>", solve_config.h) and how it was chosen
+	// (forced, rule-based, or the tuner's timings); false for an index out of range.
+	virtual bool solve_config(int sample, std::string& cfg, std::string& note) const = 0;
 };
 
 // Parses and validates the samples (host only; throws BackendError); the device is not

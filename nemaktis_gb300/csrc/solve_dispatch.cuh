@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include "bpm_kernels.cuh"
+#include "solve_config.h"
 
 namespace nbpm {
 
@@ -26,9 +27,6 @@ bool launch_solve_yc(const SolveLaunch& L, Geom G, int slot0, int nch, const cx<
 	size_t plane, const cx<double>* lsc, const cx<R>* src, cx<R>* dst, const cx<R>* ai, cx<R>* ao,
 	const cx<R>* ai2 = nullptr);
 template <typename R>
-bool launch_solve_xg(const SolveLaunch& L, Geom G, int slot0, const cx<R>* coef, const cx<R>* fac, size_t plane,
-	const cx<double>* lsc, const cx<R>* src, cx<R>* dst, const cx<R>* ai, cx<R>* ao);
-template <typename R>
 bool launch_solve_xw(const SolveLaunch& L, Geom G, int slot0, int nch, const cx<R>* coef, const cx<R>* fac,
 	size_t plane, const cx<double>* lsc, const cx<R>* src, cx<R>* dst, const cx<R>* ai, cx<R>* ao);
 void set_solve_smem_xw_f32(int bytes);
@@ -41,22 +39,14 @@ void set_solve_smem_xs_f64(int bytes);
 template <typename R>
 bool launch_solve_ys(const SolveLaunch& L, Geom G, int slot0, int nch, const cx<R>* coef, const cx<R>* fac,
 	size_t plane, const cx<double>* lsc, const cx<R>* src, cx<R>* dst, const cx<R>* ai, cx<R>* ao, cx<R>* vbuf);
-void set_solve_smem_xg_f32(int bytes);
-void set_solve_smem_xg_f64(int bytes);
+// Sequential y-line solve (k_solve_yq): grid (columns / block.x, groups * nch), KS in {1, 2, 4}.
+// scr receives the forward values; it must alias none of src, ai, ai2 (it may be dst or ao).
+template <typename R>
+bool launch_solve_yq(const SolveLaunch& L, Geom G, int nch, const cx<R>* coef, const cx<R>* fac, size_t plane,
+	const cx<double>* lsc, const cx<R>* src, cx<R>* scr, cx<R>* dst, const cx<R>* ai, cx<R>* ao, const cx<R>* ai2);
 void set_solve_smem_x_f32(int bytes);
 void set_solve_smem_x_f64(int bytes);
 void set_solve_smem_y_f32(int bytes);
 void set_solve_smem_y_f64(int bytes);
-
-// (M, KS) pairs with compiled instances.
-inline bool solve_pair_ok(int M, int KS) {
-	switch(M) {
-		case 2: case 4: return KS == 1 || KS == 2 || KS == 4;
-		case 8: return KS == 1 || KS == 2 || KS == 4;
-		case 16: return KS == 1 || KS == 2;
-		case 32: return KS == 1;
-	}
-	return false;
-}
 
 }  // namespace nbpm

@@ -33,27 +33,6 @@ void set_solve_smem_x_f32(int bytes) {
 	NBPM_XA_PAIRS(ST_WOOD_X)
 }
 
-#define NBPM_XG(MM, KD) \
-	if(L.M == MM && L.kind == KD) { \
-		k_solve_xg<float, MM, KD><<<L.grid, L.block, L.smem, L.stream>>>(G, slot0, coef, fac, plane, lsc, src, dst, ai, ao); \
-		return true; \
-	}
-#define NBPM_XG_ALL(KD) NBPM_XG(2, KD) NBPM_XG(4, KD) NBPM_XG(8, KD) NBPM_XG(16, KD) NBPM_XG(32, KD)
-
-template <>
-bool launch_solve_xg<float>(const SolveLaunch& L, Geom G, int slot0, const cx<float>* coef, const cx<float>* fac,
-		size_t plane, const cx<double>* lsc, const cx<float>* src, cx<float>* dst, const cx<float>* ai, cx<float>* ao) {
-	NBPM_XG_ALL(ST_EXPL_Y)
-	NBPM_XG_ALL(ST_WOOD_X)
-	return false;
-}
-
-void set_solve_smem_xg_f32(int bytes) {
-#define NBPM_XGA(MM, KD) cudaFuncSetAttribute(k_solve_xg<float, MM, KD>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-	NBPM_XGA(2, ST_EXPL_Y) NBPM_XGA(4, ST_EXPL_Y) NBPM_XGA(8, ST_EXPL_Y) NBPM_XGA(16, ST_EXPL_Y) NBPM_XGA(32, ST_EXPL_Y)
-	NBPM_XGA(2, ST_WOOD_X) NBPM_XGA(4, ST_WOOD_X) NBPM_XGA(8, ST_WOOD_X) NBPM_XGA(16, ST_WOOD_X) NBPM_XGA(32, ST_WOOD_X)
-}
-
 #define NBPM_XS(KK, KD) \
 	if(L.KS == KK && L.kind == KD) { \
 		k_solve_xs<float, KD, KK><<<L.grid, L.block, L.smem, L.stream>>>(G, slot0, nch, L.M, coef, fac, plane, lsc, \

@@ -42,7 +42,6 @@ bool launch_solve_yc<float>(const SolveLaunch& L, Geom G, int slot0, int nch, co
 	}
 	NBPM_YC_PAIRS(ST_EXPL_X)
 	NBPM_YC_PAIRS(ST_WOOD_Y)
-	NBPM_YC_PAIRS(ST_GIVEN)
 	return false;
 }
 
@@ -59,7 +58,6 @@ void set_solve_smem_y_f32(int bytes) {
 	cudaFuncSetAttribute(k_solve_yc<float, 8, ST_WOOD_Y, 2, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 	NBPM_YA_PAIRS(ST_EXPL_X)
 	NBPM_YA_PAIRS(ST_WOOD_Y)
-	NBPM_YA_PAIRS(ST_GIVEN)
 }
 
 #define NBPM_YS(KK, KD) \
@@ -75,6 +73,22 @@ bool launch_solve_ys<float>(const SolveLaunch& L, Geom G, int slot0, int nch, co
 		const cx<float>* ai, cx<float>* ao, cx<float>* vbuf) {
 	NBPM_YS(1, ST_EXPL_X) NBPM_YS(2, ST_EXPL_X) NBPM_YS(4, ST_EXPL_X)
 	NBPM_YS(1, ST_WOOD_Y) NBPM_YS(2, ST_WOOD_Y) NBPM_YS(4, ST_WOOD_Y)
+	return false;
+}
+
+#define NBPM_YQ(KK, KD) \
+	if(L.KS == KK && L.kind == KD) { \
+		k_solve_yq<float, KD, KK><<<L.grid, L.block, 0, L.stream>>>(G, nch, coef, fac, plane, lsc, src, scr, dst, ai, ao, \
+			ai2); \
+		return true; \
+	}
+
+template <>
+bool launch_solve_yq<float>(const SolveLaunch& L, Geom G, int nch, const cx<float>* coef, const cx<float>* fac,
+		size_t plane, const cx<double>* lsc, const cx<float>* src, cx<float>* scr, cx<float>* dst, const cx<float>* ai,
+		cx<float>* ao, const cx<float>* ai2) {
+	NBPM_YQ(1, ST_EXPL_X) NBPM_YQ(2, ST_EXPL_X) NBPM_YQ(4, ST_EXPL_X)
+	NBPM_YQ(1, ST_WOOD_Y) NBPM_YQ(2, ST_WOOD_Y) NBPM_YQ(4, ST_WOOD_Y)
 	return false;
 }
 

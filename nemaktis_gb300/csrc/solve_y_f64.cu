@@ -42,7 +42,6 @@ bool launch_solve_yc<double>(const SolveLaunch& L, Geom G, int slot0, int nch, c
 	}
 	NBPM_YC_PAIRS(ST_EXPL_X)
 	NBPM_YC_PAIRS(ST_WOOD_Y)
-	NBPM_YC_PAIRS(ST_GIVEN)
 	return false;
 }
 
@@ -59,7 +58,6 @@ void set_solve_smem_y_f64(int bytes) {
 	cudaFuncSetAttribute(k_solve_yc<double, 8, ST_WOOD_Y, 2, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 	NBPM_YA_PAIRS(ST_EXPL_X)
 	NBPM_YA_PAIRS(ST_WOOD_Y)
-	NBPM_YA_PAIRS(ST_GIVEN)
 }
 
 #define NBPM_YS(KK, KD) \
@@ -75,6 +73,22 @@ bool launch_solve_ys<double>(const SolveLaunch& L, Geom G, int slot0, int nch, c
 		const cx<double>* ai, cx<double>* ao, cx<double>* vbuf) {
 	NBPM_YS(1, ST_EXPL_X) NBPM_YS(2, ST_EXPL_X) NBPM_YS(4, ST_EXPL_X)
 	NBPM_YS(1, ST_WOOD_Y) NBPM_YS(2, ST_WOOD_Y) NBPM_YS(4, ST_WOOD_Y)
+	return false;
+}
+
+#define NBPM_YQ(KK, KD) \
+	if(L.KS == KK && L.kind == KD) { \
+		k_solve_yq<double, KD, KK><<<L.grid, L.block, 0, L.stream>>>(G, nch, coef, fac, plane, lsc, src, scr, dst, ai, ao, \
+			ai2); \
+		return true; \
+	}
+
+template <>
+bool launch_solve_yq<double>(const SolveLaunch& L, Geom G, int nch, const cx<double>* coef, const cx<double>* fac,
+		size_t plane, const cx<double>* lsc, const cx<double>* src, cx<double>* scr, cx<double>* dst, const cx<double>* ai,
+		cx<double>* ao, const cx<double>* ai2) {
+	NBPM_YQ(1, ST_EXPL_X) NBPM_YQ(2, ST_EXPL_X) NBPM_YQ(4, ST_EXPL_X)
+	NBPM_YQ(1, ST_WOOD_Y) NBPM_YQ(2, ST_WOOD_Y) NBPM_YQ(4, ST_WOOD_Y)
 	return false;
 }
 

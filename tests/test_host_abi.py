@@ -142,3 +142,29 @@ def test_install_as_module():
     import bpm_backend as bb
     assert bb is m and hasattr(bb, "run_backend_with_mask")
     del sys.modules["bpm_backend"]
+
+
+def test_solve_candidates_cover_the_kernel_families(lib):
+    """Host-side candidate lists (no device needed): the rule-based default is a candidate, and
+    each mesh offers the kernel families its line lengths allow."""
+    from nemaktis_gb300 import _lib, workloads
+
+    def cands(dims, q=((0.0, 0.0),), prec=_lib.FP64):
+        js = workloads.settings_json(dims, (0.25, 0.25, 0.25), [0.6], np.asarray(q, float))
+        return _lib.solve_candidates(js, prec)
+
+    for dims in [(40, 24, 4), (300, 12, 4), (600, 6, 3), (2100, 5, 3), (12, 200, 5), (10, 530, 4), (3, 16, 4), (16, 2, 4)]:
+        c = cands(dims)
+        dx, dy = c["default"].split(";")
+        assert dx in c["x"] and dy in c["y"], (dims, c)
+    assert cands((3, 16, 4))["x"] == ["xseq"]
+    assert cands((16, 2, 4))["y"] == ["yseq"]
+    assert any(x.startswith("xw:") for x in cands((300, 12, 4))["x"])
+    assert any(x.startswith("xs:") for x in cands((600, 6, 3))["x"])
+    assert cands((2100, 5, 3))["x"] == ["xseq"]
+    y200 = cands((12, 200, 5), q=((0.0, 0.0), (0.1, 0.0)), prec=_lib.FP32)["y"]
+    assert any(y.endswith(":W1024") for y in y200) and any(y.startswith("yq:") for y in y200)
+    y530 = cands((10, 530, 4))["y"]
+    assert "yseq" in y530 and not any(y.startswith("yc:") for y in y530)
+    with pytest.raises(_lib.NbpmError):
+        _lib.solve_candidates("{}", _lib.FP64)

@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 import oracle
-from nemaktis_gb300 import api, bpm_backend, workloads
+from nemaktis_gb300 import _lib, api, bpm_backend, workloads
 from tests.helpers import case, rand_director, rand_qtensor, rel_l2, uniform_jones
 
 pytestmark = pytest.mark.gpu
@@ -145,8 +145,10 @@ def test_plain_equals_batched(gpu, precision):
     js, lc, shape = case((12, 10, 6), wavelengths=(0.45, 0.55, 0.7), q=((0.0, 0.0), (0.1, -0.05)))
     a = np.zeros(shape, np.complex128)
     b = np.zeros(shape, np.complex128)
-    api.run(js, lc, a, precision=precision, groups_per_pass=0)
-    api.run(js, lc, b, precision=precision, groups_per_pass=1)
+    # the same line-solve configuration in both (the tuner may pick per pass width)
+    cfg = _lib.solve_candidates(js, _lib.FP32 if precision == "fp32" else _lib.FP64)["default"]
+    api.run(js, lc, a, precision=precision, groups_per_pass=0, solve_config=cfg)
+    api.run(js, lc, b, precision=precision, groups_per_pass=1, solve_config=cfg)
     assert np.array_equal(a, b)
 
 
