@@ -331,6 +331,14 @@ def config4_record(steps=2):
     launches = plan.execute()["kernel_launches"]
     plan.download()
     plan.close()
+    # each sample alone (its own plan), for the gain of running the samples side by side
+    alone_ms = []
+    for c in samples:
+        b1 = [{"json": c["json"], "lc": c["lc"], "E": np.zeros(c["shape"], np.complex128)}]
+        with api.Plan(b1, precision="fp32", groups_per_pass=0) as p1:
+            p1.upload()
+            p1.execute()
+            alone_ms.append(float(np.mean([p1.execute()["compute_ms"] for _ in range(steps)])))
     k = 2  # the 512^2x96 sample
     E64 = np.zeros(samples[k]["shape"], np.complex128)
     api.run(samples[k]["json"], samples[k]["lc"], E64, precision="fp64", groups_per_pass=1)
@@ -339,6 +347,7 @@ def config4_record(steps=2):
     return {"workload": samples[0]["desc"], "voxel_steps_per_step": vs, "precision": "fp32",
             "value": vs * steps / (float(np.sum(ms)) / 1e3), "unit": "voxel-steps/s",
             "ms_per_step": float(np.mean(ms)), "steps": steps, "warmup": 1, "gpu_launches_per_step": launches,
+            "samples_alone_ms": alone_ms, "samples_alone_sum_ms": float(np.sum(alone_ms)),
             "e2e": e2e, "fp32_rel_l2_vs_fp64": {"sample": "512x512x96", "value": err}}
 
 
@@ -497,65 +506,143 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def _replay(srv, trace, keep_outputs, sample_every=0.25):
+    """Submits each request of the trace at its arrival time (real time) and waits for all.
+    Returns (infos, wall seconds, outputs of the requests in keep_outputs, queue samples)."""
+    from nemaktis_gb300 import workloads
+    samples = []
+    stop = threading.Event()
+    t0 = time.perf_counter()
+
+    def sampler():
+        while not stop.is_set():
+            st = srv.stats()
+            samples.append((time.perf_counter() - t0, st["queued"], st["running"], st["done"]))
+            stop.wait(sample_every)
+
+    th = threading.Thread(target=sampler, daemon=True)
+    th.start()
+    hs, outs = [], {}
+    for k, t in enumerate(trace):
+        dt = t0 + t["arrival"] - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        E = workloads.new_fields(t["shape"])
+        if k in keep_outputs:
+            outs[k] = E
+        hs.append(srv.submit(t["json"], t["lc"], E, t["mask"], t["formula"]))
+        del E
+    infos = []
+    for h in hs:
+        infos.append(h.wait())  # a finished request drops its buffers
+    wall = time.perf_counter() - t0
+    stop.set()
+    th.join(timeout=2)
+    return infos, wall, outs, samples
+
+
+def _fifo(trace, service_s):
+    """Latencies (ms) of a one-at-a-time FIFO server with the given service times."""
+    clock, lat = 0.0, []
+    for t, svc in zip(trace, service_s):
+        clock = max(clock, t["arrival"]) + svc
+        lat.append(1e3 * (clock - t["arrival"]))
+    return np.array(lat), clock
+
+
 def run_serve(args):
-    """Serving mix: a seeded Poisson trace replayed in real time against the FP32 server, then the
-    same trace through a plain FP64 one-request-at-a-time loop (requests served in arrival order,
-    one wavelength per launch; each request's queueing is simulated from the measured service
-    times). Reports throughput and p50/p99 latency of both, and the server's per-request relative
-    L2 error against the FP64 results."""
+    """Serving (the Poisson request-stream configuration: 50 req/s, meshes 64^2x32 .. 512^2x128,
+    1-32 wavelengths, 1-19 wave vectors, 2 polarisations, FP32, 150 GB device budget).
+
+    1. Offered load: a window of `--serve-requests` arrivals of the seeded 50 req/s trace,
+       replayed in real time against the FP32 server. The mix needs far more device time than 50
+       req/s leaves, so the queue grows: reported are the completion rate while the server is
+       backlogged (its saturation throughput on this mix), the ratio of offered to served rate,
+       the queue length over time and p50/p99 latency of the window.
+    2. Below saturation: `--serve-below` requests of the same mix arriving at half the measured
+       saturation rate; p50/p99 latency of a stable queue.
+    3. FP64 one request at a time: the plain FP64 path's service time measured on a sample of the
+       requests (one per mesh size where present), modelled per voxel-step for the others, and a
+       FIFO queue simulated on both traces; the FP32 results of the sampled requests are compared
+       with the FP64 ones (relative L2).
+    Directors are drawn from a pool of seeds per generator and mesh (run time does not depend on
+    their values)."""
     from nemaktis_gb300 import api, workloads
     from nemaktis_gb300.serving import Server
-    trace = workloads.serving_trace(args.serve_requests, rate=50.0, seed=0)
-    total_vs = sum(t["voxel_steps"] for t in trace)
-    # warm-up: context, modules, allocator
+    n_over = args.serve_requests
+    trace = workloads.serving_trace(n_over, rate=50.0, seed=0, director_pool=3)
+    # FP64 sample: the first request of each mesh size
+    sample_idx, seen = [], set()
+    for k, t in enumerate(trace):
+        if t["dims"] not in seen:
+            seen.add(t["dims"])
+            sample_idx.append(k)
     wu = workloads.serving_trace(1, seed=99)[0]
+    clk = Clocks()
     with Server(precision="fp32") as srv:
-        E = np.zeros(wu["shape"], np.complex128)
+        E = workloads.new_fields(wu["shape"])
         srv.submit(wu["json"], wu["lc"], E, wu["mask"], wu["formula"]).wait()
-        out32 = [np.zeros(t["shape"], np.complex128) for t in trace]
-        clk = Clocks()
+        del E
         clk.start()
-        t0 = time.perf_counter()
-        hs = []
-        for t, E in zip(trace, out32):
-            dt = t0 + t["arrival"] - time.perf_counter()
-            if dt > 0:
-                time.sleep(dt)
-            hs.append(srv.submit(t["json"], t["lc"], E, t["mask"], t["formula"]))
-        infos = [h.wait() for h in hs]
-        t_end = time.perf_counter()
-        clocks = clk.stop()
+        infos, wall, outs32, qs = _replay(srv, trace, set(sample_idx))
         st = srv.stats()
-    lat32 = np.array([i["latency_ms"] for i in infos])
-    wall32 = t_end - t0
-    # FP64 plain, one request at a time, same trace
-    clock = 0.0
-    lat64, errs = [], []
-    t64_busy = 0.0
-    for t, E32 in zip(trace, out32):
-        E = np.zeros(t["shape"], np.complex128)
-        s = time.perf_counter()
+    lat = np.array([i["latency_ms"] for i in infos])
+    vs = np.array([t["voxel_steps"] for t in trace], float)
+    # saturation: completions while the queue was non-empty after the last arrival
+    t_last = trace[-1]["arrival"]
+    busy = [q for q in qs if q[0] >= t_last and q[1] + q[2] > 0]
+    if len(busy) >= 2:
+        sat_rps = (busy[-1][3] - busy[0][3]) / max(1e-9, busy[-1][0] - busy[0][0])
+    else:
+        sat_rps = len(trace) / wall
+    sat_vs = float(vs.sum() / wall)
+    # below saturation
+    rate_below = max(0.05, 0.5 * sat_rps)
+    trace_b = workloads.serving_trace(args.serve_below, rate=rate_below, seed=1, director_pool=3)
+    with Server(precision="fp32") as srv:
+        infos_b, wall_b, _, qs_b = _replay(srv, trace_b, set())
+    clocks = clk.stop()
+    lat_b = np.array([i["latency_ms"] for i in infos_b])
+    # FP64 one at a time: measured on the sample, per voxel-step for the rest
+    svc64, errs = {}, []
+    for k in sample_idx:
+        t = trace[k]
+        E = workloads.new_fields(t["shape"])
+        s0 = time.perf_counter()
         api.run(t["json"], t["lc"], E, mask=t["mask"], formula=t["formula"], precision="fp64", groups_per_pass=1)
-        svc = time.perf_counter() - s
-        t64_busy += svc
-        clock = max(clock, t["arrival"]) + svc
-        lat64.append(1e3 * (clock - t["arrival"]))
-        errs.append(float(np.linalg.norm(E32 - E) / np.linalg.norm(E)))
-    lat64 = np.array(lat64)
+        svc64[k] = time.perf_counter() - s0
+        errs.append(float(np.linalg.norm(outs32[k] - E) / np.linalg.norm(E)))
+    by_dims = {trace[k]["dims"]: svc64[k] / trace[k]["voxel_steps"] for k in sample_idx}
+
+    def model(tr):
+        return [svc64.get(k, by_dims.get(t["dims"], np.mean(list(by_dims.values()))) * t["voxel_steps"])
+                if tr is trace else by_dims.get(t["dims"], np.mean(list(by_dims.values()))) * t["voxel_steps"]
+                for k, t in enumerate(tr)]
+
+    lat64, mk64 = _fifo(trace, model(trace))
+    lat64_b, mk64_b = _fifo(trace_b, model(trace_b))
+    qgrowth = [{"t_s": round(q[0], 2), "queued": q[1], "running": q[2], "done": q[3]} for q in qs[::max(1, len(qs) // 40)]]
     line = {
         "metric": "serving: voxel-steps/s and p50/p99 end-to-end latency, FP32 continuous batching vs FP64 one at a time",
-        "value": total_vs / wall32, "unit": "voxel-steps/s", "n_gpus": 1, "steps": 1, "warmup": 1,
-        "higher_is_better": True, "dtype": "complex-f32", "data": "synthetic (seeded trace and director fields)",
-        "config": {"workload": "serving mix: %d requests, Poisson 50 req/s, meshes 64^2x32..512^2x128, 1-32 "
-                               "wavelengths, 1-19 q, d=0.25um, budget 150 GB" % len(trace),
-                   "requests": [{k: t[k] for k in ("arrival", "kind", "dims", "n_wavelengths", "n_q", "voxel_steps")}
-                                for t in trace]},
-        "server": {"wall_s": wall32, "p50_ms": float(np.percentile(lat32, 50)), "p99_ms": float(np.percentile(lat32, 99)),
-                   "mean_queue_ms": float(np.mean([i["queue_ms"] for i in infos])), "peak_device_gb": st["peak_bytes"] / 1e9,
-                   "rounds": st["rounds"], "done": st["done"], "failed": st["failed"]},
-        "fp64_one_at_a_time": {"value": total_vs / clock, "busy_s": t64_busy, "makespan_s": clock,
-                               "p50_ms": float(np.percentile(lat64, 50)), "p99_ms": float(np.percentile(lat64, 99))},
-        "max_rel_l2_fp32_vs_fp64": max(errs),
+        "value": sat_vs, "unit": "voxel-steps/s", "n_gpus": 1, "steps": 1, "warmup": 1,
+        "higher_is_better": True, "dtype": "complex-f32", "data": "synthetic (seeded trace, director pool of 3 seeds per generator and mesh)",
+        "config": {"workload": "serving mix: Poisson 50 req/s, meshes 64^2x32..512^2x128 (p .4/.3/.2/.1), 1-32 "
+                               "wavelengths, 1-19 q, 2 pol, d=0.25um, device budget 150 GB",
+                   "window_requests": len(trace), "window_arrival_s": t_last,
+                   "mean_request_voxel_steps": float(vs.mean())},
+        "offered_load": {"rate_rps": 50.0, "served_rps_saturated": sat_rps, "overload_factor": 50.0 / max(1e-9, sat_rps),
+                         "wall_s": wall, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                         "mean_queue_ms": float(np.mean([i["queue_ms"] for i in infos])),
+                         "peak_device_gb": st["peak_bytes"] / 1e9, "queue_over_time": qgrowth,
+                         "done": st["done"], "failed": st["failed"]},
+        "below_saturation": {"rate_rps": rate_below, "requests": len(trace_b), "wall_s": wall_b,
+                             "p50_ms": float(np.percentile(lat_b, 50)), "p99_ms": float(np.percentile(lat_b, 99))},
+        "fp64_one_at_a_time": {"measured_requests": len(sample_idx), "service_s_per_voxel_step": {"x".join(map(str, d)): v for d, v in by_dims.items()},
+                               "offered_load": {"value": float(vs.sum() / mk64), "makespan_s": mk64,
+                                                "p50_ms": float(np.percentile(lat64, 50)), "p99_ms": float(np.percentile(lat64, 99))},
+                               "below_saturation": {"p50_ms": float(np.percentile(lat64_b, 50)),
+                                                    "p99_ms": float(np.percentile(lat64_b, 99))}},
+        "max_rel_l2_fp32_vs_fp64": max(errs) if errs else None,
         "clocks": clocks,
     }
     print(json.dumps(line), flush=True)
@@ -577,7 +664,8 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="rule-based line-solve configuration (no timing runs)")
     ap.add_argument("--solve-config", default=None, help='force a line-solve configuration "<x>;<y>"')
     ap.add_argument("--only-value", action="store_true", help="time the device-resident run only")
-    ap.add_argument("--serve-requests", type=int, default=12, help="requests in the serving trace")
+    ap.add_argument("--serve-requests", type=int, default=100, help="arrivals of the 50 req/s window")
+    ap.add_argument("--serve-below", type=int, default=30, help="requests of the below-saturation trace")
     args = ap.parse_args()
     world, rank, local = dist_env()
     if world > 1:

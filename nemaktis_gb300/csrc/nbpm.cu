@@ -151,6 +151,32 @@ struct SampleHost {
 	cx<double>* hstage = nullptr;  // pinned host staging of one pass's plane
 	// device
 	DevBuf dir, dmask, dwts, F, E0, gpsd, shiftd, partial, wl, nout, qv, bstage;
+	// The sample's lane: its own streams (sample 0 uses the plan's), events and workspace, so that
+	// the samples of a batch run side by side on the device, each in its own branch of the graph.
+	struct Lane {
+		cudaStream_t main = nullptr, setup = nullptr;
+		bool owns_streams = false;
+		cudaEvent_t eFork = nullptr, eJoin = nullptr, eCoef = nullptr, eFac = nullptr, eTrans = nullptr;
+		cudaEvent_t eAdi[2] = {nullptr, nullptr};
+		cudaEvent_t eNref = nullptr, eNrefFork = nullptr, eEnd = nullptr;
+		// workspace: field-sized iterates T, T2 (T3 for the scratch-chunk y solve), eps and
+		// coefficient rings, diagonal stencils, double-buffered factor planes / line scalars
+		// (slab iz uses half iz & 1), screen and widening buffers
+		DevBuf T, T2, T3, Qring, coef, diag, facx, facy, lscx, lscy, scr, stage;
+		size_t facx_half = 0, facy_half = 0, lsc_half = 0;
+		std::vector<cudaEvent_t*> events() {
+			return {&eFork, &eJoin, &eCoef, &eFac, &eTrans, &eAdi[0], &eAdi[1], &eNref, &eNrefFork, &eEnd};
+		}
+		~Lane() {
+			if(main) cudaStreamSynchronize(main);
+			if(setup) cudaStreamSynchronize(setup);
+			for(cudaEvent_t* e : events()) if(*e) cudaEventDestroy(*e);
+			if(owns_streams) {
+				if(setup) cudaStreamDestroy(setup);
+				if(main) cudaStreamDestroy(main);
+			}
+		}
+	} lane;
 	~SampleHost() { if(hstage) cudaFreeHost(hstage); }
 };
 
@@ -235,21 +261,23 @@ template <typename R>
 struct Plan : PlanBase {
 	nbpm_options opt;
 	std::vector<std::unique_ptr<SampleHost>> S;
-	cudaStream_t stream = nullptr;   // main stream (right-hand-side work, copies)
-	cudaStream_t streamB = nullptr;  // per-slab setup (eps planes, coefficients, factorisations)
+	// The plan's own streams (sample 0's lane) and, while a sample is recorded, that sample's
+	// lane (select()): stream = right-hand-side work and copies, streamB = per-slab setup (eps
+	// planes, coefficients, factorisations).
+	cudaStream_t stream0 = nullptr, streamB0 = nullptr;
+	cudaStream_t stream = nullptr;
+	cudaStream_t streamB = nullptr;
 	cudaStream_t cs = nullptr;       // stream the next launch goes to
 	cudaEvent_t eFork = nullptr, eJoin = nullptr, eCoef = nullptr, eFac = nullptr, eTrans = nullptr, eAdi[2] = {nullptr, nullptr};
 	cudaEvent_t eNref = nullptr, eNrefFork = nullptr;
-	// double-buffered factor planes / line scalars: slab iz uses half iz & 1
-	size_t facx_half = 0, facy_half = 0, lsc_half = 0;
+	cudaEvent_t eBatch = nullptr;    // start of a batch recording on the plan's stream
+	SampleHost::Lane* W = nullptr;   // workspace of the sample being recorded
 	cx<R>* fx_cur = nullptr;
 	cx<R>* fy_cur = nullptr;
 	cx<double>* lx_cur = nullptr;
 	cx<double>* ly_cur = nullptr;
 	cudaGraphExec_t gexec = nullptr;
 	cudaEvent_t ev[6];
-	// workspace (shared by passes, sized for the largest)
-	DevBuf T, T2, Qring, coef, diag, facx, facy, lscx, lscy, scr, stage, twx, twy;
 	std::vector<DevBuf*> tw_bufs;
 	std::vector<std::unique_ptr<DevBuf>> tw_store;
 	std::vector<std::pair<int, cx<R>*>> tw_tables;
@@ -291,22 +319,31 @@ struct Plan : PlanBase {
 	// Line-solve configuration per sample (solve_config.h): forced by opts.solve_config, timed
 	// per shape by tune() (opts.tune), or the rule-based default.
 	std::vector<std::string> tune_notes;  // per sample: how its configuration was chosen
-	DevBuf T3;
 	std::vector<SolveCfg> scfg;
+
+	// Makes h's lane current: its streams, events and workspace.
+	void select(SampleHost& h) {
+		auto& L = h.lane;
+		stream = L.main; streamB = L.setup; cs = stream;
+		eFork = L.eFork; eJoin = L.eJoin; eCoef = L.eCoef; eFac = L.eFac; eTrans = L.eTrans;
+		eAdi[0] = L.eAdi[0]; eAdi[1] = L.eAdi[1]; eNref = L.eNref; eNrefFork = L.eNrefFork;
+		W = &L;
+	}
 
 	Plan(const nbpm_options& o) : opt(o) {
 		for(auto& e : ev) e = nullptr;
 	}
 	~Plan() override {
-		if(stream) cudaStreamSynchronize(stream);
-		if(streamB) cudaStreamSynchronize(streamB);
+		if(stream0) cudaStreamSynchronize(stream0);
+		if(streamB0) cudaStreamSynchronize(streamB0);
+		S.clear();  // lanes: their streams and events
 		if(eDone) cudaEventDestroy(eDone);
+		if(eBatch) cudaEventDestroy(eBatch);
 		for(auto e : evpool) cudaEventDestroy(e);
 		if(gexec) cudaGraphExecDestroy(gexec);
 		for(auto& e : ev) if(e) cudaEventDestroy(e);
-		for(cudaEvent_t e : {eFork, eJoin, eCoef, eFac, eTrans, eAdi[0], eAdi[1], eNref, eNrefFork}) if(e) cudaEventDestroy(e);
-		if(streamB) cudaStreamDestroy(streamB);
-		if(stream) cudaStreamDestroy(stream);
+		if(streamB0) cudaStreamDestroy(streamB0);
+		if(stream0) cudaStreamDestroy(stream0);
 	}
 
 	cx<R>* twiddles(int n) {
@@ -420,11 +457,20 @@ struct Plan : PlanBase {
 	void setup_device() override {
 		// Host-side validation is complete; only now touch the device.
 		CK(cudaSetDevice(opt.device));
-		CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-		CK(cudaStreamCreateWithFlags(&streamB, cudaStreamNonBlocking));
-		for(cudaEvent_t* e : {&eFork, &eJoin, &eCoef, &eFac, &eTrans, &eAdi[0], &eAdi[1], &eNref, &eNrefFork})
-			CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
-		cs = stream;
+		CK(cudaStreamCreateWithFlags(&stream0, cudaStreamNonBlocking));
+		CK(cudaStreamCreateWithFlags(&streamB0, cudaStreamNonBlocking));
+		CK(cudaEventCreateWithFlags(&eBatch, cudaEventDisableTiming));
+		for(auto& hp : S) {
+			auto& L = hp->lane;
+			if(hp->index == 0) { L.main = stream0; L.setup = streamB0; }
+			else {
+				L.owns_streams = true;
+				CK(cudaStreamCreateWithFlags(&L.main, cudaStreamNonBlocking));
+				CK(cudaStreamCreateWithFlags(&L.setup, cudaStreamNonBlocking));
+			}
+			for(cudaEvent_t* e : L.events()) CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+		}
+		select(*S[0]);
 		for(auto& e : ev) CK(cudaEventCreate(&e));
 		int dev = opt.device;
 		int optin = 0;
@@ -472,8 +518,6 @@ struct Plan : PlanBase {
 	void allocate() {
 		scfg.clear();
 		dev_bytes = 0;
-		bool need_t3 = false;
-		size_t maxT = 0, maxQ = 0, maxC = 0, maxD = 0, maxFx = 0, maxL = 0, maxScr = 0, maxStage = 0;
 		for(auto& hp : S) {
 			SampleHost& h = *hp;
 			size_t N = h.geom.N;
@@ -482,19 +526,34 @@ struct Plan : PlanBase {
 			SolveCfg sc = heuristic(sh);
 			// buffers sized for every candidate the tuner may pick
 			size_t px = sc.plane_x;
-			for(auto& c : x_candidates(sh)) px = std::max(px, c.plane_x);
+			for(auto& c : x_candidates(sh, true)) px = std::max(px, c.plane_x);
 			sc.plane_x = px;
-			for(auto& c : y_candidates(sh)) need_t3 |= c.ys;
-			need_t3 |= sc.ys;
+			bool need_t3 = sc.ys;
+			for(auto& c : y_candidates(sh, true)) need_t3 |= c.ys;
 			scfg.push_back(sc);
-			maxT = std::max(maxT, (size_t)ng * h.spg * 2 * N);
-			maxQ = std::max(maxQ, (size_t)2 * ng * NQ * N);
-			maxC = std::max(maxC, (size_t)2 * ng * NCOEF * N);  // two slabs (transition kernels)
-			maxD = std::max(maxD, (size_t)ng * NDIAG * N);
-			maxFx = std::max(maxFx, (size_t)ng * 2 * NFAC * std::max(sc.plane_x, sc.plane_y));
-			maxL = std::max(maxL, (size_t)ng * 2 * std::max(h.s.Nx, h.s.Ny) * 2);
-			maxScr = std::max(maxScr, (size_t)2 * ng * 2 * 2 * N);  // x and y halves
-			if(sizeof(R) != sizeof(double)) maxStage = std::max(maxStage, (size_t)h.slots * 2 * N);
+			// the sample's workspace (its lane)
+			{
+				auto& L = h.lane;
+				const size_t nT = (size_t)ng * h.spg * 2 * N, nFx = (size_t)ng * 2 * NFAC * std::max(sc.plane_x, sc.plane_y);
+				const size_t nL = (size_t)ng * 2 * std::max(h.s.Nx, h.s.Ny) * 2;
+				dalloc(L.T, sizeof(cx<R>) * nT);
+				dalloc(L.T2, sizeof(cx<R>) * nT);
+				if(need_t3) dalloc(L.T3, sizeof(cx<R>) * nT);
+				dalloc(L.Qring, sizeof(R) * (size_t)2 * ng * NQ * N);
+				dalloc(L.coef, sizeof(cx<R>) * (size_t)2 * ng * NCOEF * N);  // two slabs (transition kernels)
+				dalloc(L.diag, sizeof(cx<R>) * (size_t)ng * NDIAG * N);
+				L.facx_half = L.facy_half = nFx;
+				L.lsc_half = nL;
+				dalloc(L.facx, sizeof(cx<R>) * nFx * 2);
+				dalloc(L.facy, sizeof(cx<R>) * nFx * 2);
+				dalloc(L.lscx, sizeof(cx<double>) * nL * 2);
+				dalloc(L.lscy, sizeof(cx<double>) * nL * 2);
+				dalloc(L.scr, sizeof(cx<R>) * (size_t)2 * ng * 2 * 2 * N);  // x and y halves
+				if(sizeof(R) != sizeof(double)) dalloc(L.stage, sizeof(cx<double>) * (size_t)h.slots * 2 * N);
+				for(DevBuf* b : {&L.T, &L.T2, &L.T3, &L.Qring, &L.coef, &L.diag, &L.facx, &L.facy, &L.lscx, &L.lscy,
+						&L.scr, &L.stage})
+					dev_bytes += b->bytes;
+			}
 			// per-sample buffers
 			dalloc(h.dir, sizeof(double) * h.nvox * h.fd);
 			if(h.has_mask) dalloc(h.dmask, h.nvox);
@@ -517,22 +576,6 @@ struct Plan : PlanBase {
 			if(dry) dev_bytes += sizeof(cx<R>) * (size_t)(h.s.Nx + h.s.Ny);
 			else { twiddles(h.s.Nx); twiddles(h.s.Ny); }
 		}
-		dalloc(T, sizeof(cx<R>) * maxT);
-		dalloc(T2, sizeof(cx<R>) * maxT);
-		if(need_t3) dalloc(T3, sizeof(cx<R>) * maxT);
-		dalloc(Qring, sizeof(R) * maxQ);
-		dalloc(coef, sizeof(cx<R>) * maxC);
-		dalloc(diag, sizeof(cx<R>) * maxD);
-		facx_half = facy_half = maxFx;
-		lsc_half = maxL;
-		dalloc(facx, sizeof(cx<R>) * maxFx * 2);
-		dalloc(facy, sizeof(cx<R>) * maxFx * 2);
-		dalloc(lscx, sizeof(cx<double>) * maxL * 2);
-		dalloc(lscy, sizeof(cx<double>) * maxL * 2);
-		dalloc(scr, sizeof(cx<R>) * maxScr);
-		dalloc(stage, sizeof(cx<double>) * maxStage);
-		dev_bytes += T.bytes + T2.bytes + Qring.bytes + coef.bytes + diag.bytes + facx.bytes + facy.bytes +
-			lscx.bytes + lscy.bytes + scr.bytes + stage.bytes + T3.bytes;
 	}
 
 	// ---- line-solve configuration: forced, tuned or rule-based ----
@@ -547,6 +590,7 @@ struct Plan : PlanBase {
 			const size_t pmax = sc.plane_x;
 			const auto xc = x_candidates(sh), yc = y_candidates(sh);
 			if(!forced.empty()) {
+				const auto xr = x_candidates(sh, true), yr = y_candidates(sh, true);
 				size_t k = forced.find(';');
 				std::string fx = forced.substr(0, k), fy = k == std::string::npos ? "auto" : forced.substr(k + 1);
 				auto pick = [&](const std::vector<SolveCfg>& cands, const std::string& want, bool x) {
@@ -557,8 +601,8 @@ struct Plan : PlanBase {
 						std::to_string(h.s.Nx) + "x" + std::to_string(h.s.Ny) + " mesh with " + std::to_string(h.spg) +
 						" slots per wavelength (candidates: " + all + ")");
 				};
-				if(fx != "auto") pick(xc, fx, true);
-				if(fy != "auto") pick(yc, fy, false);
+				if(fx != "auto") pick(xr, fx, true);
+				if(fy != "auto") pick(yr, fy, false);
 				tune_notes[h.index] = "forced";
 				if(fx != "auto" && fy != "auto") { sc.plane_x = pmax; continue; }
 			}
@@ -607,6 +651,13 @@ struct Plan : PlanBase {
 			if(opt.verbose) std::printf("line solves %s: %s\n", sc.str().c_str(), note.c_str());
 		}
 		launches = 0;
+		// the scratch field of the scratch-chunk y solve is kept only where that solve was chosen
+		for(auto& hp : S)
+			if(!scfg[hp->index].ys && hp->lane.T3.p) {
+				dev_bytes -= (long long)hp->lane.T3.bytes;
+				hp->lane.T3.alloc(0);
+			}
+		select(*S[0]);
 	}
 
 	std::string tune_key(const SampleHost& h) const {
@@ -619,10 +670,12 @@ struct Plan : PlanBase {
 	// Zeroes the workspace the timing runs read (their values do not change the kernels' speed,
 	// but uninitialised memory could hold NaN or denormal patterns).
 	void zero_workspace() {
-		for(DevBuf* b : {&T, &T2, &T3, &coef, &facx, &facy, &lscx, &lscy})
-			if(b->p) CK(cudaMemsetAsync(b->p, 0, b->bytes, stream));
-		for(auto& hp : S) CK(cudaMemsetAsync(hp->F.p, 0, hp->F.bytes, stream));
-		CK(cudaStreamSynchronize(stream));
+		for(auto& hp : S) {
+			auto& L = hp->lane;
+			for(DevBuf* b : {&L.T, &L.T2, &L.T3, &L.coef, &L.facx, &L.facy, &L.lscx, &L.lscy, &hp->F})
+				if(b->p) CK(cudaMemsetAsync(b->p, 0, b->bytes, stream0));
+		}
+		CK(cudaStreamSynchronize(stream0));
 	}
 
 	// Device time of one slab's solves of one direction with the current configuration of
@@ -632,13 +685,13 @@ struct Plan : PlanBase {
 		const Geom Gm = h.geom;
 		const int ng = gpp(h), nsl = ng * h.spg;
 		cx<R>* Fp = h.F.as<cx<R>>();
-		fx_cur = facx.as<cx<R>>(); fy_cur = facy.as<cx<R>>();
-		lx_cur = lscx.as<cx<double>>(); ly_cur = lscy.as<cx<double>>();
-		cs = stream;
+		select(h);
+		fx_cur = W->facx.as<cx<R>>(); fy_cur = W->facy.as<cx<R>>();
+		lx_cur = W->lscx.as<cx<double>>(); ly_cur = W->lscy.as<cx<double>>();
 		float best = 1e30f;
 		for(int r = 0; r < 4; r++) {
 			CK(cudaEventRecord(ev[2], stream));
-			rec_adi(h, Gm, 0, nsl, ng, h.s.n_woodbury, coef.as<cx<R>>(), Fp, T.as<cx<R>>(), T2.as<cx<R>>(), Fp, dirn);
+			rec_adi(h, Gm, 0, nsl, ng, h.s.n_woodbury, W->coef.as<cx<R>>(), Fp, W->T.as<cx<R>>(), W->T2.as<cx<R>>(), Fp, dirn);
 			CK(cudaEventRecord(ev[3], stream));
 			CK(cudaEventSynchronize(ev[3]));
 			float ms = 0;
@@ -651,6 +704,7 @@ struct Plan : PlanBase {
 	void upload() override {
 		for(auto& hp : S) {
 			SampleHost& h = *hp;
+			select(h);
 			CK(cudaMemcpyAsync(h.dir.p, h.lc, h.dir.bytes, cudaMemcpyHostToDevice, stream));
 			if(h.has_mask) CK(cudaMemcpyAsync(h.dmask.p, h.mask.data(), h.nvox, cudaMemcpyHostToDevice, stream));
 			if(h.has_wts) CK(cudaMemcpyAsync(h.dwts.p, h.wts.data(), h.dwts.bytes, cudaMemcpyHostToDevice, stream));
@@ -667,13 +721,14 @@ struct Plan : PlanBase {
 					CK(cudaMemcpyAsync(h.E0.p, h.E, n * sizeof(cx<double>), cudaMemcpyHostToDevice, stream));
 				}
 				else {
-					CK(cudaMemcpyAsync(stage.p, h.E, n * sizeof(cx<double>), cudaMemcpyHostToDevice, stream));
-					k_narrow<R><<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, stage.as<cx<double>>(), h.E0.as<cx<R>>());
+					CK(cudaMemcpyAsync(W->stage.p, h.E, n * sizeof(cx<double>), cudaMemcpyHostToDevice, stream));
+					k_narrow<R><<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, W->stage.as<cx<double>>(), h.E0.as<cx<R>>());
 					CK(cudaGetLastError());
 				}
 			}
+			CK(cudaStreamSynchronize(stream));
 		}
-		CK(cudaStreamSynchronize(stream));
+		select(*S[0]);
 	}
 
 	// Device address of a page-locked, mapped host buffer of the given size (the caller's result
@@ -694,6 +749,7 @@ struct Plan : PlanBase {
 	void download() override {
 		for(auto& hp : S) {
 			SampleHost& h = *hp;
+			select(h);
 			size_t n = (size_t)h.slots * 2 * h.geom.N;
 			void* dE = mapped_host(h.E, n * sizeof(cx<double>));
 			if(sizeof(R) == sizeof(double) && dE) {
@@ -710,12 +766,13 @@ struct Plan : PlanBase {
 				CK(cudaGetLastError());
 			}
 			else {
-				k_widen<R><<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, h.F.as<cx<R>>(), stage.as<cx<double>>());
+				k_widen<R><<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, h.F.as<cx<R>>(), W->stage.as<cx<double>>());
 				CK(cudaGetLastError());
-				CK(cudaMemcpyAsync(h.E, stage.p, n * sizeof(cx<double>), cudaMemcpyDeviceToHost, stream));
+				CK(cudaMemcpyAsync(h.E, W->stage.p, n * sizeof(cx<double>), cudaMemcpyDeviceToHost, stream));
 			}
 		}
-		CK(cudaStreamSynchronize(stream));
+		for(auto& hp : S) CK(cudaStreamSynchronize(hp->lane.main));
+		select(*S[0]);
 		host_finish();
 	}
 
@@ -799,10 +856,21 @@ struct Plan : PlanBase {
 		}
 	}
 
+	// Every sample on its own lane: the lanes of samples 1.. fork from the plan's stream and join
+	// it again at the end, so that in the captured graph the samples are parallel branches.
 	void record() {
 		launches = 0;
-		cs = stream;
-		for(auto& hp : S) record_sample(*hp);
+		select(*S[0]);
+		if(S.size() > 1) CK(cudaEventRecord(eBatch, stream0));
+		for(auto& hp : S) {
+			select(*hp);
+			if(hp->index > 0) CK(cudaStreamWaitEvent(stream, eBatch, 0));
+			record_sample(*hp);
+			if(hp->index > 0) CK(cudaEventRecord(hp->lane.eEnd, stream));
+		}
+		select(*S[0]);
+		for(auto& hp : S)
+			if(hp->index > 0) CK(cudaStreamWaitEvent(stream0, hp->lane.eEnd, 0));
 	}
 
 	// State of one pass of wavelength groups through the slab loop. Kept between calls when a
@@ -860,13 +928,13 @@ struct Plan : PlanBase {
 		ps.nsl = ps.ng * h.spg;
 		ps.gps = h.gpsd.as<GroupParams>() + ga;
 		ps.Fp = h.F.as<cx<R>>() + (size_t)ps.slot0 * 2 * N;
-		ps.Tb = T.as<cx<R>>();
-		ps.T2b = T2.as<cx<R>>();
-		ps.Qr[0] = Qring.as<R>();
+		ps.Tb = W->T.as<cx<R>>();
+		ps.T2b = W->T2.as<cx<R>>();
+		ps.Qr[0] = W->Qring.as<R>();
 		ps.Qr[1] = ps.Qr[0] + (size_t)ps.ng * NQ * N;
-		ps.Cring[0] = coef.as<cx<R>>();
-		ps.Cring[1] = coef.as<cx<R>>() + (size_t)ps.ng * NCOEF * N;
-		ps.Dg = diag.as<cx<R>>();
+		ps.Cring[0] = W->coef.as<cx<R>>();
+		ps.Cring[1] = W->coef.as<cx<R>>() + (size_t)ps.ng * NCOEF * N;
+		ps.Dg = W->diag.as<cx<R>>();
 		ps.eps_bytes = (double)N * ps.ng * (h.fd * 8 + (mk_ ? 1 : 0) + NQ * sizeof(R));
 		ps.field_pts = (double)N * ps.nsl;
 		const int ng = ps.ng, nsl = ps.nsl, slot0 = ps.slot0;
@@ -911,10 +979,10 @@ struct Plan : PlanBase {
 			R* QB = ps.Qr[(iz + 1) & 1];
 			cx<R>* C = ps.Cring[iz & 1];
 			const SolveCfg& scf = scfg[h.index];
-			cx<R>* fx = facx.as<cx<R>>() + (size_t)(iz & 1) * facx_half;
-			cx<R>* fy = facy.as<cx<R>>() + (size_t)(iz & 1) * facy_half;
-			cx<double>* lx = lscx.as<cx<double>>() + (size_t)(iz & 1) * lsc_half;
-			cx<double>* ly = lscy.as<cx<double>>() + (size_t)(iz & 1) * lsc_half;
+			cx<R>* fx = W->facx.as<cx<R>>() + (size_t)(iz & 1) * W->facx_half;
+			cx<R>* fy = W->facy.as<cx<R>>() + (size_t)(iz & 1) * W->facy_half;
+			cx<double>* lx = W->lscx.as<cx<double>>() + (size_t)(iz & 1) * W->lsc_half;
+			cx<double>* ly = W->lscy.as<cx<double>>() + (size_t)(iz & 1) * W->lsc_half;
 			// ---- setup stream ----
 			cs = streamB;
 			launch("eps_plane", ps.eps_bytes, [&] {
@@ -928,7 +996,6 @@ struct Plan : PlanBase {
 			CK(cudaEventRecord(eCoef, streamB));
 			// factor(iz) overwrites the half the line solves of slab iz-2 used
 			if(iz >= 2) CK(cudaStreamWaitEvent(streamB, eAdi[iz & 1], 0));
-			int lx_n = ng * 2 * Ny, ly_n = ng * 2 * Nx;
 			const double fb = (double)N * ng * 2 * (3 * sc + NFAC * sc + 4 * sc);
 			// y factorisation: 8 chunk warps per 32 columns, 16 when the grid leaves SMs idle
 			const int LT = 4, WF = ((Nx + 31) / 32) * 2 * ng < nsm && Ny - 1 >= 256 ? 16 : 8;
@@ -1204,7 +1271,7 @@ struct Plan : PlanBase {
 				L.smem = (size_t)(4 * L.KS * WS * 32 + 2 * L.KS * 32) * sizeof(cx<R>);
 				launch(wood ? "wood_solve_y" : "expl_solve_y", bytes + fp * 2, [&] {
 					if(!launch_solve_ys<R>(L, Gm, slot0, nch, C, fy_cur, sc.plane_y, ly_cur, src, dst, acc_in, acc_out,
-							T3.as<cx<R>>()))
+							W->T3.as<cx<R>>()))
 						throw BackendError(E_INTERNAL, "no y-solve instance");
 				});
 				return;
@@ -1305,8 +1372,7 @@ struct Plan : PlanBase {
 		try { record(); }
 		catch(...) { profiling = false; throw; }
 		profiling = false;
-		CK(cudaStreamSynchronize(stream));
-		CK(cudaStreamSynchronize(streamB));
+		CK(cudaDeviceSynchronize());
 		for(auto& r : prof) {
 			float t = 0;
 			CK(cudaEventElapsedTime(&t, r.a, r.b));
@@ -1373,13 +1439,14 @@ struct Plan : PlanBase {
 		if(S.size() != 1 || gpp(*S[0]) != S[0]->G) throw BackendError(E_ARG, "stepped plans hold one sample in one pass");
 		CK(cudaSetDevice(opt.device));
 		if(!eDone) CK(cudaEventCreateWithFlags(&eDone, cudaEventDisableTiming));
-		cs = stream;
+		select(*S[0]);
 		rec_prologue(*S[0]);
 		sps = rec_pass_begin(*S[0], 0);
 		rec_bulk(*S[0], sps, 0, nullptr);
 	}
 	int step_advance(int nslabs) override {
 		CK(cudaSetDevice(opt.device));
+		select(*S[0]);
 		SampleHost& h = *S[0];
 		int end = std::min(h.geom.Nz - 1, sps.iz + std::max(0, nslabs));
 		rec_pass_slabs(h, sps, end);
@@ -1387,6 +1454,7 @@ struct Plan : PlanBase {
 	}
 	void step_finish() override {
 		CK(cudaSetDevice(opt.device));
+		select(*S[0]);
 		SampleHost& h = *S[0];
 		rec_pass_end(h, sps);
 		rec_screen(h);
@@ -1395,15 +1463,17 @@ struct Plan : PlanBase {
 			CK(cudaMemcpyAsync(h.E, h.F.p, n * sizeof(cx<double>), cudaMemcpyDeviceToHost, stream));
 		}
 		else {
-			k_widen<R><<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, h.F.as<cx<R>>(), stage.as<cx<double>>());
+			k_widen<R><<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, h.F.as<cx<R>>(), W->stage.as<cx<double>>());
 			CK(cudaGetLastError());
-			CK(cudaMemcpyAsync(h.E, stage.p, n * sizeof(cx<double>), cudaMemcpyDeviceToHost, stream));
+			CK(cudaMemcpyAsync(h.E, W->stage.p, n * sizeof(cx<double>), cudaMemcpyDeviceToHost, stream));
 		}
 		CK(cudaEventRecord(eDone, stream));
 	}
 	void sync() override {
-		CK(cudaStreamSynchronize(stream));
-		CK(cudaStreamSynchronize(streamB));
+		for(auto& hp : S) {
+			CK(cudaStreamSynchronize(hp->lane.main));
+			CK(cudaStreamSynchronize(hp->lane.setup));
+		}
 	}
 	bool step_done() override {
 		cudaError_t e = cudaEventQuery(eDone);
@@ -1723,7 +1793,7 @@ int nbpm_run_batch(int n_samples, const nbpm_sample* samples, const nbpm_options
 	// the kept plan, if this call matches it and no other call holds it
 	std::unique_lock<std::mutex> lk(plan_cache().m, std::defer_lock);
 	const std::string key = plan_cache_on() ? plan_key(n_samples, samples, opts) : std::string();
-	if(!key.empty()) lk.try_lock();
+	if(!key.empty()) (void)lk.try_lock();
 	nbpm_plan* p = nullptr;
 	std::unique_ptr<nbpm_plan> guard;
 	bool reused = false;

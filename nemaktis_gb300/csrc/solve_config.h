@@ -70,8 +70,10 @@ struct SolveShape {
 	bool fp32 = false;
 	int nsm = 152;      // streaming multiprocessors
 	size_t smem = 227 * 1024;  // opt-in shared memory per block
+	bool relax = false;  // every compiled instance (forced configurations), not only the timed set
 	size_t csize() const { return fp32 ? 8 : 16; }
-	int cap() const { return fp32 ? 32 : 16; }  // chunk values (M * KS complex) kept per thread
+	// chunk values (M * KS complex) kept per thread
+	int cap() const { return fp32 || relax ? 32 : 16; }
 };
 
 inline size_t plane_x_of(const SolveCfg& c, const SolveShape& s) {
@@ -92,8 +94,12 @@ inline bool yc_fits(int M, int ks, int WY, const SolveShape& s) {
 	return ((size_t)(4 + 3 * ks) * WY * 32 + (size_t)ks * 32) * s.csize() <= s.smem;
 }
 
-// Candidates for the x-lines (y fields left at their defaults).
-inline std::vector<SolveCfg> x_candidates(const SolveShape& s) {
+// Candidates for the x-lines (y fields left at their defaults). relaxed: every configuration
+// with a compiled instance (chunk values up to 32 complex per thread in either precision), the
+// set a forced configuration is checked against; the tuner times the default set.
+inline std::vector<SolveCfg> x_candidates(const SolveShape& s0, bool relaxed = false) {
+	SolveShape s = s0;
+	if(relaxed) s.relax = true;
 	std::vector<SolveCfg> out;
 	const int ux = s.Nx - 1;
 	if(s.Nx > 3) {
@@ -121,8 +127,10 @@ inline std::vector<SolveCfg> x_candidates(const SolveShape& s) {
 	return out;
 }
 
-// Candidates for the y-lines (x fields left at their defaults).
-inline std::vector<SolveCfg> y_candidates(const SolveShape& s) {
+// Candidates for the y-lines (x fields left at their defaults); relaxed as for x_candidates.
+inline std::vector<SolveCfg> y_candidates(const SolveShape& s0, bool relaxed = false) {
+	SolveShape s = s0;
+	if(relaxed) s.relax = true;
 	std::vector<SolveCfg> out;
 	const int uy = s.Ny - 1;
 	if(s.Ny > 3) {

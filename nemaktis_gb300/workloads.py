@@ -191,14 +191,18 @@ SERVE_MESHES = [(64, 64, 32), (128, 128, 48), (256, 256, 64), (512, 512, 128)]
 SERVE_MESH_P = [0.4, 0.3, 0.2, 0.1]
 
 
-def serving_trace(n_requests, rate=50.0, seed=0, d=0.25):
+def serving_trace(n_requests, rate=50.0, seed=0, d=0.25, director_pool=0):
     """Serving mix: Poisson arrivals at `rate` per second; mesh drawn from 64^2x32, 128^2x48,
     256^2x64, 512^2x128 with p = .4/.3/.2/.1; director from {twisted nematic, cholesteric
     droplet (masked), random smooth}, seeded per request; N_lambda ~ U{1..32} on [0.40, 0.80];
-    N_q ~ U{1..19}: the first N_q points of the 3-ring hexagonal Koehler grid at NA 0.25."""
+    N_q ~ U{1..19}: the first N_q points of the 3-ring hexagonal Koehler grid at NA 0.25.
+    director_pool > 0 draws each request's director seed from that many seeds per (generator,
+    mesh) and shares the arrays between requests with the same seed (bounded generation time and
+    host memory for long traces; the run time does not depend on the director's values)."""
     rng = np.random.default_rng(seed)
     t = 0.0
     out = []
+    pool = {}
     q19 = hex_wavevectors(3, 0.25)
     for i in range(n_requests):
         t += rng.exponential(1.0 / rate)
@@ -210,14 +214,21 @@ def serving_trace(n_requests, rate=50.0, seed=0, d=0.25):
         q = q19[:nq]
         req = {"arrival": t, "kind": kind, "dims": dims, "n_wavelengths": nl, "n_q": nq}
         Nx, Ny, Nz = dims
-        if kind == "tn":
-            lc = twisted_nematic(dims=dims, d=d, seed=seed * 1000 + i)
-            mask = formula = None
-        elif kind == "droplet":
-            lc, mask, formula = cholesteric_droplet(dims=dims, d=d, radius=0.4 * d * (Nx - 1), pitch=5.0)
+        dseed = seed * 1000 + (i if director_pool <= 0 else int(rng.integers(director_pool)))
+        pkey = (kind, dims, dseed if kind != "droplet" else 0)
+        if pkey in pool:
+            lc, mask, formula = pool[pkey]
         else:
-            lc = random_smooth(dims, d=d, corr_len=2.0, seed=seed * 1000 + i)
-            mask = formula = None
+            if kind == "tn":
+                lc = twisted_nematic(dims=dims, d=d, seed=dseed)
+                mask = formula = None
+            elif kind == "droplet":
+                lc, mask, formula = cholesteric_droplet(dims=dims, d=d, radius=0.4 * d * (Nx - 1), pitch=5.0)
+            else:
+                lc = random_smooth(dims, d=d, corr_len=2.0, seed=dseed)
+                mask = formula = None
+            if director_pool > 0:
+                pool[pkey] = (lc, mask, formula)
         req.update({"json": settings_json(dims, (d, d, d), wl, q, no="1.5", ne="1.7", nhost="1.55", NA=0.4),
                     "lc": lc, "mask": mask, "formula": formula, "shape": (len(wl), nq, 4, Ny, Nx),
                     "voxel_steps": Nx * Ny * (Nz - 1) * len(wl) * nq * 2})
