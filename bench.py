@@ -608,6 +608,8 @@ def run_serve(args):
     for k in sample_idx:
         t = trace[k]
         E = workloads.new_fields(t["shape"])
+        # the first call of a shape also tunes its line solves and builds its graph: time the second
+        api.run(t["json"], t["lc"], E, mask=t["mask"], formula=t["formula"], precision="fp64", groups_per_pass=1)
         s0 = time.perf_counter()
         api.run(t["json"], t["lc"], E, mask=t["mask"], formula=t["formula"], precision="fp64", groups_per_pass=1)
         svc64[k] = time.perf_counter() - s0

@@ -1225,6 +1225,121 @@ __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_xc(Geom G, 
 	}
 }
 
+// y-line solve in the x-line form: one warp per (column, comp, KS slots of one wavelength), lane l
+// owning the rows [l*M, l*M+M) of the column, the chunk maps combined by warp shuffles
+// (line_combine) as in k_solve_xc, so that no barrier joins the warps of a line. A block of LT
+// warps takes LT adjacent columns: its threads form the right-hand sides of every (row, column)
+// pair of those columns together (consecutive threads take the columns of a row, so a warp's
+// loads are 32-byte row segments of eight rows) into the warps' shared buffers in the lane-chunk
+// layout, each warp solves its column, and the block writes the results back row by row. The
+// factor planes keep the plain [row][column] layout (each 32-byte sector of a row serves the LT
+// warps of the block). KIND: ST_EXPL_X (explicit x half-step) or ST_WOOD_Y (Woodbury term).
+// Restates BlockSparseMatrixDY::shifted_block_vmult_inv (BlockSparseMatrix.cpp:386-451) with the
+// right-hand sides of ParaxialPrimaryEvolutionOperator::apply (ParaxialPrimaryEvolutionOperator.
+// cpp:153-209). Outputs: dst = x (may be null), acc_out = (acc_in [+ acc_in2]) + x (may be null).
+template <typename R, int M, int KIND, int KS>
+__global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_yt(Geom G, int nch, const cx<R>* __restrict__ coef,
+		const cx<R>* __restrict__ fac, size_t plane, const cx<double>* __restrict__ lsc,
+		const cx<R>* __restrict__ src, cx<R>* __restrict__ dst, const cx<R>* acc_in, cx<R>* acc_out,
+		const cx<R>* acc_in2) {
+	extern __shared__ unsigned char smem_raw[];
+	const int LT = blockDim.x / 32;
+	const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+	const int Nx = G.Nx, Ny = G.Ny, N = G.N;
+	const int x0 = blockIdx.x * LT;
+	const int c = blockIdx.y % 2, bc = blockIdx.y / 2;
+	const int g = bc / nch, ch = bc % nch;
+	const int s0 = g * G.spg + ch * KS;
+	const int n_unk = Ny - 1;
+	const int PITCH = 32 * (M + 1);
+	cx<R>* const bufs = reinterpret_cast<cx<R>*>(smem_raw);
+	const Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
+	const cx<R>* f0 = src + (size_t)s0 * 2 * N;
+	const cx<R> one = mk<R>(1, 0), zero = mk<R>(0, 0);
+	// right-hand sides of every (row, column) pair of the block's columns
+	for(int e = threadIdx.x; e < n_unk * LT; e += blockDim.x) {
+		const int i = e / LT, w = e % LT, x = x0 + w;
+		if(x < Nx) {
+			cx<R> r[KS];
+			composite_m<R, KIND, KS>(st, c, x, i, f0, r);
+			cx<R>* b = bufs + (size_t)w * KS * PITCH + (i / M) * (M + 1) + i % M;
+#pragma unroll
+			for(int j = 0; j < KS; j++) b[j * PITCH] = r[j];
+		}
+	}
+	__syncthreads();
+	const int x = x0 + warp;
+	if(x < Nx) {
+		cx<R>* buf = bufs + (size_t)warp * KS * PITCH;
+		const cx<R>* Fc = fac + ((size_t)g * 2 + c) * NFAC * plane + x;
+		const cx<double>* ls = lsc + (((size_t)g * 2 + c) * Nx + x) * 2;
+		const cx<double> r0 = ls[0], rden = ls[1];
+		const int i0 = lane * M;
+		cx<R> d0[KS], S0[KS], G0[KS];
+		cx<R> P = one, S1 = zero, G1 = zero, Cp = one;
+#pragma unroll
+		for(int j = 0; j < KS; j++) { d0[j] = zero; S0[j] = zero; G0[j] = zero; }
+		cx<R>* vb = buf + lane * (M + 1);
+#pragma unroll
+		for(int k = 0; k < M; k++) {
+			if(i0 + k < n_unk) {
+				const size_t q = (size_t)(i0 + k) * Nx;
+				const cx<R> a = Fc[F_A * plane + q], rb = Fc[F_RB * plane + q];
+				const cx<R> w = Fc[F_W * plane + q], cc = Fc[F_C * plane + q];
+				P = a * P;
+				S1 += w * P;
+				G1 += Cp * P;
+#pragma unroll
+				for(int j = 0; j < KS; j++) {
+					const cx<R> b = vb[j * PITCH + k] * rb;
+					vb[j * PITCH + k] = b;
+					d0[j] = a * d0[j] + b;
+					S0[j] += w * d0[j];
+					G0[j] += Cp * d0[j];
+				}
+				Cp = Cp * cc;
+			}
+		}
+		cx<R> din[KS], xin[KS], fr[KS];
+		line_combine<R, KS>(P, d0, S0, S1, G0, G1, Cp, r0, rden, lane, din, xin, fr);
+#pragma unroll
+		for(int k = 0; k < M; k++) {
+			if(i0 + k < n_unk) {
+				const cx<R> a = Fc[F_A * plane + (size_t)(i0 + k) * Nx];
+#pragma unroll
+				for(int j = 0; j < KS; j++) { din[j] = a * din[j] + vb[j * PITCH + k]; vb[j * PITCH + k] = din[j]; }
+			}
+		}
+#pragma unroll
+		for(int k = M - 1; k >= 0; k--) {
+			if(i0 + k < n_unk) {
+				const size_t q = (size_t)(i0 + k) * Nx;
+				const cx<R> cc = Fc[F_C * plane + q], cr = Fc[F_COR * plane + q];
+#pragma unroll
+				for(int j = 0; j < KS; j++) {
+					xin[j] = cc * xin[j] + vb[j * PITCH + k];
+					vb[j * PITCH + k] = xin[j] - fr[j] * cr;
+				}
+			}
+		}
+	}
+	__syncthreads();
+	// results, row by row (row Ny-1 repeats row 0)
+	for(int e = threadIdx.x; e < Ny * LT; e += blockDim.x) {
+		const int i = e / LT, w = e % LT, xo = x0 + w;
+		if(xo >= Nx) continue;
+		const int ii = i == Ny - 1 ? 0 : i;
+		const cx<R>* b = bufs + (size_t)w * KS * PITCH + (ii / M) * (M + 1) + ii % M;
+#pragma unroll
+		for(int j = 0; j < KS; j++) {
+			const size_t off = (size_t)(s0 + j) * 2 * N + (size_t)c * N + (size_t)i * Nx + xo;
+			const cx<R> v = b[j * PITCH];
+			if(dst) dst[off] = v;
+			if(KIND != ST_EXPL_X && acc_out) acc_out[off] = (acc_in2 ? acc_in[off] + acc_in2[off] : acc_in[off]) + v;
+		}
+	}
+}
+
 // Whether k_solve_yc<M, KS, MAXT> keeps its chunk values in shared memory: the values
 // (KS*M*MAXT complex) and the combine arrays ((4 + 3 KS)*MAXT + 32 KS complex) within 224 KiB.
 __host__ __device__ constexpr bool yc_values_in_smem(int M, int KS, int MAXT, int csize) {

@@ -483,11 +483,11 @@ struct Plan : PlanBase {
 		CK(cudaFuncSetAttribute(k_shift_fused<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 			(int)((size_t)4 * (SHT + 6) * (SHT + 6) * sizeof(cx<R>))));
 		if(sizeof(R) == sizeof(float)) {
-			set_solve_smem_x_f32((int)smem_limit); set_solve_smem_y_f32((int)smem_limit);
+			set_solve_smem_x_f32((int)smem_limit); set_solve_smem_y_f32((int)smem_limit); set_solve_smem_yt_f32((int)smem_limit);
 			set_solve_smem_xs_f32((int)smem_limit); set_solve_smem_xw_f32((int)smem_limit);
 		}
 		else {
-			set_solve_smem_x_f64((int)smem_limit); set_solve_smem_y_f64((int)smem_limit);
+			set_solve_smem_x_f64((int)smem_limit); set_solve_smem_y_f64((int)smem_limit); set_solve_smem_yt_f64((int)smem_limit);
 			set_solve_smem_xs_f64((int)smem_limit); set_solve_smem_xw_f64((int)smem_limit);
 		}
 		CK(cudaGetLastError());
@@ -1196,7 +1196,7 @@ struct Plan : PlanBase {
 	// Whether the fused solve of direction dirn runs k_solve_xc / k_solve_yc, the kernels that take
 	// a second accumulator input.
 	bool solve_takes_acc2(const SolveCfg& sc, int dirn) const {
-		return dirn == 0 ? (sc.Mx > 0 && sc.WPLx == 1 && !sc.xs) : (sc.yq > 0 || (sc.My > 0 && !sc.ys));
+		return dirn == 0 ? (sc.Mx > 0 && sc.WPLx == 1 && !sc.xs) : (sc.yq > 0 || sc.Mt > 0 || (sc.My > 0 && !sc.ys));
 	}
 
 	// scr: a field-sized buffer the solve may overwrite (none of src, acc_in, acc_in2), used by the
@@ -1247,6 +1247,18 @@ struct Plan : PlanBase {
 				if(!launch_solve_xc<R>(L, Gm, slot0, nch, C, fx_cur, sc.plane_x, lx_cur, src,
 						dst, acc_in, acc_out, acc_in2))
 					throw BackendError(E_INTERNAL, "no x-solve instance");
+			});
+		}
+		else if(sc.Mt) {
+			const int LT = 4;
+			L.M = sc.Mt; L.KS = sc.KSy; L.kind = wood ? ST_WOOD_Y : ST_EXPL_X;
+			const int nch = h.spg / L.KS;
+			L.block = dim3(32 * LT);
+			L.grid = dim3((unsigned)((Gm.Nx + LT - 1) / LT), (unsigned)(ng * nch * 2));
+			L.smem = (size_t)LT * L.KS * 32 * (L.M + 1) * sizeof(cx<R>);
+			launch(wood ? "wood_solve_y" : "expl_solve_y", bytes, [&] {
+				if(!launch_solve_yt<R>(L, Gm, nch, C, fy_cur, sc.plane_y, ly_cur, src, dst, acc_in, acc_out, acc_in2))
+					throw BackendError(E_INTERNAL, "no y-solve instance");
 			});
 		}
 		else if(sc.yq) {
@@ -1307,7 +1319,7 @@ struct Plan : PlanBase {
 		const SolveCfg& cfg = scfg[h.index];
 		for(int dirn = 0; dirn < 2; dirn++) {
 			if(only_dirn >= 0 && dirn != only_dirn) continue;
-			bool fused = dirn == 0 ? cfg.Mx > 0 : (cfg.My > 0 || cfg.ys || cfg.yq > 0);
+			bool fused = dirn == 0 ? cfg.Mx > 0 : (cfg.My > 0 || cfg.ys || cfg.yq > 0 || cfg.Mt > 0);
 			if(fused) {
 				// t0 = solve(f + mu R f) written to T; Woodbury: t_k = solve(mu R' t_{k-1}),
 				// F = t0 + t1 + ... accumulated by the solves (the last t_k is not stored).

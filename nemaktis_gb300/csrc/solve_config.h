@@ -36,7 +36,8 @@ struct SolveCfg {
 	// a scratch field (k_solve_ys, KSy slots); My > 0 32 columns x WY warps of M-row chunks
 	// (k_solve_yc, KSy slots; y1024w: the Woodbury solves with 32 warps of 8-row chunks and 2
 	// slots per thread); else sequential (k_stencil + k_solve).
-	int My = 0, WY = 0, KSy = 1, yq = 0;
+	// Mt > 0: one warp per column with Mt-row lane chunks (k_solve_yt, KSy slots).
+	int My = 0, WY = 0, KSy = 1, yq = 0, Mt = 0;
 	bool ys = false, y1024w = false;
 	// factor plane sizes (elements per factor and line set), from the x layout
 	size_t plane_x = 0, plane_y = 0;
@@ -52,6 +53,7 @@ struct SolveCfg {
 	std::string ystr() const {
 		char b[64];
 		if(yq) std::snprintf(b, sizeof b, "yq:KS=%d", yq);
+		else if(Mt) std::snprintf(b, sizeof b, "yt:M=%d:KS=%d", Mt, KSy);
 		else if(ys) std::snprintf(b, sizeof b, "ys:KS=%d", KSy);
 		else if(My) std::snprintf(b, sizeof b, "yc:M=%d:KS=%d:W=%d%s", My, KSy, WY, y1024w ? ":W1024" : "");
 		else return "yseq";
@@ -59,7 +61,7 @@ struct SolveCfg {
 	}
 	std::string str() const { return xstr() + ";" + ystr(); }
 	void set_x(const SolveCfg& o) { Mx = o.Mx; KSx = o.KSx; WPLx = o.WPLx; xs = o.xs; }
-	void set_y(const SolveCfg& o) { My = o.My; WY = o.WY; KSy = o.KSy; yq = o.yq; ys = o.ys; y1024w = o.y1024w; }
+	void set_y(const SolveCfg& o) { My = o.My; WY = o.WY; KSy = o.KSy; yq = o.yq; Mt = o.Mt; ys = o.ys; y1024w = o.y1024w; }
 };
 
 // What the choice depends on.
@@ -142,6 +144,14 @@ inline std::vector<SolveCfg> y_candidates(const SolveShape& s0, bool relaxed = f
 				if(s.spg % ks == 0 && solve_pair_ok(M0, ks) && (M0 * ks <= s.cap() || ks == 1) && yc_fits(M0, ks, WY, s)) {
 					SolveCfg c; c.My = M0; c.WY = WY; c.KSy = ks; out.push_back(c);
 					if(uy > 128 && uy <= 256 && s.spg % 2 == 0 && ks >= 2) { c.y1024w = true; out.push_back(c); }
+				}
+		}
+		if(uy <= 1024) {
+			int Mt = 0;
+			for(int M = 2; M <= 32; M *= 2) if(32 * M >= uy) { Mt = M; break; }
+			for(int ks : {4, 2, 1})
+				if(s.spg % ks == 0 && solve_pair_ok(Mt, ks) && (Mt * ks <= s.cap() || ks == 1)) {
+					SolveCfg c; c.Mt = Mt; c.KSy = ks; out.push_back(c);
 				}
 		}
 		for(int ks : {4, 2, 1})

@@ -39,6 +39,13 @@ void set_solve_smem_xs_f64(int bytes);
 template <typename R>
 bool launch_solve_ys(const SolveLaunch& L, Geom G, int slot0, int nch, const cx<R>* coef, const cx<R>* fac,
 	size_t plane, const cx<double>* lsc, const cx<R>* src, cx<R>* dst, const cx<R>* ai, cx<R>* ao, cx<R>* vbuf);
+// y-line solve in the x-line form (k_solve_yt): grid (columns / LT, groups * nch * 2), block 32*LT,
+// shared memory LT * KS * 32 * (M + 1) complex; (M, KS) as for k_solve_xc.
+template <typename R>
+bool launch_solve_yt(const SolveLaunch& L, Geom G, int nch, const cx<R>* coef, const cx<R>* fac, size_t plane,
+	const cx<double>* lsc, const cx<R>* src, cx<R>* dst, const cx<R>* ai, cx<R>* ao, const cx<R>* ai2);
+void set_solve_smem_yt_f32(int bytes);
+void set_solve_smem_yt_f64(int bytes);
 // Sequential y-line solve (k_solve_yq): grid (columns / block.x, groups * nch), KS in {1, 2, 4}.
 // scr receives the forward values; it must alias none of src, ai, ai2 (it may be dst or ao).
 template <typename R>

@@ -92,4 +92,34 @@ bool launch_solve_yq<float>(const SolveLaunch& L, Geom G, int nch, const cx<floa
 	return false;
 }
 
+#define NBPM_YT(MM, KK, KD) \
+	if(L.M == MM && L.KS == KK && L.kind == KD) { \
+		k_solve_yt<float, MM, KD, KK><<<L.grid, L.block, L.smem, L.stream>>>(G, nch, coef, fac, plane, lsc, src, dst, ai, ao, \
+			ai2); \
+		return true; \
+	}
+#define NBPM_YT_PAIRS(KIND) \
+	NBPM_YT(2, 1, KIND) NBPM_YT(2, 2, KIND) NBPM_YT(2, 4, KIND) NBPM_YT(4, 1, KIND) NBPM_YT(4, 2, KIND) NBPM_YT(4, 4, KIND) \
+	NBPM_YT(8, 1, KIND) NBPM_YT(8, 2, KIND) NBPM_YT(8, 4, KIND) NBPM_YT(16, 1, KIND) NBPM_YT(16, 2, KIND) NBPM_YT(32, 1, KIND)
+
+template <>
+bool launch_solve_yt<float>(const SolveLaunch& L, Geom G, int nch, const cx<float>* coef, const cx<float>* fac,
+		size_t plane, const cx<double>* lsc, const cx<float>* src, cx<float>* dst, const cx<float>* ai, cx<float>* ao,
+		const cx<float>* ai2) {
+	NBPM_YT_PAIRS(ST_EXPL_X)
+	NBPM_YT_PAIRS(ST_WOOD_Y)
+	return false;
+}
+
+#define NBPM_YTA(MM, KK, KD) \
+	cudaFuncSetAttribute(k_solve_yt<float, MM, KD, KK>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+#define NBPM_YTA_PAIRS(KIND) \
+	NBPM_YTA(2, 1, KIND) NBPM_YTA(2, 2, KIND) NBPM_YTA(2, 4, KIND) NBPM_YTA(4, 1, KIND) NBPM_YTA(4, 2, KIND) NBPM_YTA(4, 4, KIND) \
+	NBPM_YTA(8, 1, KIND) NBPM_YTA(8, 2, KIND) NBPM_YTA(8, 4, KIND) NBPM_YTA(16, 1, KIND) NBPM_YTA(16, 2, KIND) NBPM_YTA(32, 1, KIND)
+
+void set_solve_smem_yt_f32(int bytes) {
+	NBPM_YTA_PAIRS(ST_EXPL_X)
+	NBPM_YTA_PAIRS(ST_WOOD_Y)
+}
+
 }  // namespace nbpm
