@@ -746,6 +746,45 @@ __device__ __forceinline__ cx<R> shfl_xor_c(cx<R> v, int m) {
 // accesses stay coalesced; the factor planes are stored chunk-interleaved (element l*M+k at
 // k*32+l) and are also loaded once for the KS slots. Block = LT warps = LT lines.
 // ---------------------------------------------------------------------------------------
+// The y-line solves as x-line solves of the transposed frame (x' = y, y' = x, components
+// exchanged): the stencil blocks b become 3 - b (00 <-> 11, 01 <-> 10), the DX and DY stencils
+// exchange, the DXDY corners (px,py), (mx,py), (px,my), (mx,my) become corners 0, 2, 1, 3, and the
+// duplicate-row/column folding and the period-(N-1) wraps map onto themselves. This kernel
+// writes, per wavelength group, the transposed planes those solves read: DY' (every block) from
+// DX, DX' (blocks 1 and 2) from DY, every DXDY' block from DXDY, and the diagonal stencils of the
+// transposed x-lines (diag' direction 0, component c') from the y diagonals of component 1 - c'.
+// Each block moves one 32x32 tile of one plane through shared memory (coalesced reads and writes).
+constexpr int NCT = 12 + 6 + 16 + 6;  // planes per group: DY', DX' (blocks 1, 2), DXDY', diag'
+template <typename S>
+__global__ void __launch_bounds__(256) k_coef_t(Geom G, const cx<S>* __restrict__ coef, const cx<S>* __restrict__ diag,
+		cx<S>* __restrict__ coefT, cx<S>* __restrict__ diagT) {
+	__shared__ cx<S> tile[32][33];
+	const int Nx = G.Nx, Ny = G.Ny, N = G.N;
+	const int g = blockIdx.z / NCT, k = blockIdx.z % NCT;
+	int sp, dp;  // source / destination plane
+	bool dg = false;
+	if(k < 12) { const int b = k / 3, kk = k % 3; dp = C_DY + 3 * b + kk; sp = C_DX + 3 * (3 - b) + kk; }
+	else if(k < 18) { const int b = 1 + (k - 12) / 3, kk = (k - 12) % 3; dp = C_DX + 3 * b + kk; sp = C_DY + 3 * (3 - b) + kk; }
+	else if(k < 34) {
+		const int b = (k - 18) / 4, kk = (k - 18) % 4;
+		const int sk = kk == 1 ? 2 : kk == 2 ? 1 : kk;
+		dp = C_DXDY + 4 * b + kk; sp = C_DXDY + 4 * (3 - b) + sk;
+	}
+	else { const int cp = (k - 34) / 3, kk = (k - 34) % 3; dp = 0 * 6 + cp * 3 + kk; sp = 1 * 6 + (1 - cp) * 3 + kk; dg = true; }
+	const cx<S>* src = (dg ? diag + (size_t)g * NDIAG * N : coef + (size_t)g * NCOEF * N) + (size_t)sp * N;
+	cx<S>* dst = (dg ? diagT + (size_t)g * NDIAG * N : coefT + (size_t)g * NCOEF * N) + (size_t)dp * N;
+	const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+	for(int r = threadIdx.y; r < 32; r += blockDim.y) {
+		const int x = x0 + threadIdx.x, y = y0 + r;
+		if(x < Nx && y < Ny) tile[r][threadIdx.x] = src[(size_t)y * Nx + x];
+	}
+	__syncthreads();
+	for(int r = threadIdx.y; r < 32; r += blockDim.y) {
+		const int y = y0 + threadIdx.x, x = x0 + r;  // destination row x, column y
+		if(x < Nx && y < Ny) dst[(size_t)x * Ny + y] = tile[threadIdx.x][r];
+	}
+}
+
 // Pre-factorisation of the periodic line solves (I - mu*R_cc) x = b per (group, comp, line), in
 // the plan's precision. Restates shifted_block_vmult_inv (BlockSparseMatrix.cpp:195-258 and
 // 386-449): Thomas sweep with beta0 = 2*mid0 and the Sherman-Morrison corner vector corr
@@ -1106,7 +1145,7 @@ __device__ __forceinline__ void line_combine(cx<R> P, const cx<R>* d0, const cx<
 // computed with coalesced loads into the warp's shared buffer in the lane-chunk layout (lane l
 // holds points [l M, l M + M)), one pass builds the chunk maps, line_combine joins them by
 // shuffles, and a last pass finishes the line, which goes back out coalesced.
-template <typename R, int M, int KIND, int KS>
+template <typename R, int M, int KIND, int KS, bool TOUT = false>
 // Resident blocks per SM requested from the compiler: 8 (64 registers) for the instances
 // whose chunk values fit, measured faster on GB300; the larger instances keep their registers.
 #ifndef NBPM_XC_MINB
@@ -1115,6 +1154,10 @@ template <typename R, int M, int KIND, int KS>
 #ifndef NBPM_YC_MINB
 #define NBPM_YC_MINB 1
 #endif
+// TOUT: the results go out transposed with the two components exchanged ((c, iy, e) -> (1 - c,
+// e, iy) of an Ny x Nx plane), written by the whole block so that each (point, LT lines) group
+// is one 32-byte segment: the hand-over between the x-line frame and the transposed frame in
+// which the y-lines are solved as x-lines (ADI with transposed y solves).
 __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_xc(Geom G, int slot0, int nch, const cx<R>* __restrict__ coef,
 		const cx<R>* __restrict__ fac, size_t plane, const cx<double>* __restrict__ lsc,
 		const cx<R>* __restrict__ src, cx<R>* __restrict__ dst, const cx<R>* acc_in, cx<R>* acc_out,
@@ -1124,13 +1167,14 @@ __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_xc(Geom G, 
 	const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
 	const int Nx = G.Nx, Ny = G.Ny, N = G.N;
 	const int iy = blockIdx.x * LT + warp;
-	if(iy >= Ny) return;
+	if(!TOUT && iy >= Ny) return;
 	const int c = blockIdx.y % 2, bc = blockIdx.y / 2;
 	const int g = bc / nch, ch = bc % nch;
 	const int s0 = g * G.spg + ch * KS;  // first slot (pass-relative)
 	const int n_unk = Nx - 1;
 	const int PITCH = 32 * (M + 1);
 	cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw) + (size_t)warp * KS * PITCH;
+	if(iy < Ny) {  // always true unless TOUT (whose block writes together after a barrier)
 	const cx<R>* Fc = fac + ((size_t)g * 2 + c) * NFAC * plane + (size_t)iy * 32 * M;
 	const cx<double>* ls = lsc + (((size_t)g * 2 + c) * Ny + iy) * 2;
 	const cx<double> r0 = ls[0], rden = ls[1];
@@ -1207,6 +1251,7 @@ __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_xc(Geom G, 
 			}
 		}
 	}
+	if(!TOUT) {
 	__syncwarp();
 	for(int j = 0; j < KS; j++) {
 		const size_t off = (size_t)(s0 + j) * 2 * N + (size_t)c * N + (size_t)iy * Nx;
@@ -1220,6 +1265,26 @@ __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_xc(Geom G, 
 				// the explicit-step solves never accumulate
 				if(KIND != ST_EXPL_Y && acc_out)
 					acc_out[off + e] = (acc_in2 ? acc_in[off + e] + acc_in2[off + e] : acc_in[off + e]) + x;
+			}
+		}
+	}
+	}
+	}  // iy < Ny
+	if(TOUT) {
+		__syncthreads();
+		const cx<R>* bufs = reinterpret_cast<const cx<R>*>(smem_raw);
+		for(int t = threadIdx.x; t < Nx * LT; t += blockDim.x) {
+			const int e = t / LT, w = t % LT, line = blockIdx.x * LT + w;
+			if(line >= Ny) continue;
+			const int ee = e == Nx - 1 ? 0 : e;
+			const cx<R>* bw = bufs + (size_t)w * KS * PITCH + (ee / M) * (M + 1) + ee % M;
+#pragma unroll
+			for(int j = 0; j < KS; j++) {
+				const size_t in = (size_t)(s0 + j) * 2 * N + (size_t)c * N + (size_t)line * Nx + e;
+				const size_t out = (size_t)(s0 + j) * 2 * N + (size_t)(1 - c) * N + (size_t)e * Ny + line;
+				const cx<R> x = bw[j * PITCH];
+				if(dst) dst[out] = x;
+				if(KIND != ST_EXPL_Y && acc_out) acc_out[out] = (acc_in2 ? acc_in[in] + acc_in2[in] : acc_in[in]) + x;
 			}
 		}
 	}

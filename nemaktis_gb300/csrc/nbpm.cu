@@ -163,6 +163,8 @@ struct SampleHost {
 		// coefficient rings, diagonal stencils, double-buffered factor planes / line scalars
 		// (slab iz uses half iz & 1), screen and widening buffers
 		DevBuf T, T2, T3, Qring, coef, diag, facx, facy, lscx, lscy, scr, stage;
+		// transposed-frame y solves: transposed coefficient ring (two slabs) and diagonal stencils
+		DevBuf coefT, diagT;
 		size_t facx_half = 0, facy_half = 0, lsc_half = 0;
 		std::vector<cudaEvent_t*> events() {
 			return {&eFork, &eJoin, &eCoef, &eFac, &eTrans, &eAdi[0], &eAdi[1], &eNref, &eNrefFork, &eEnd};
@@ -273,6 +275,7 @@ struct Plan : PlanBase {
 	cudaEvent_t eBatch = nullptr;    // start of a batch recording on the plan's stream
 	SampleHost::Lane* W = nullptr;   // workspace of the sample being recorded
 	cx<R>* fx_cur = nullptr;
+	const cx<R>* ct_cur = nullptr;   // transposed coefficients of the slab being recorded
 	cx<R>* fy_cur = nullptr;
 	cx<double>* lx_cur = nullptr;
 	cx<double>* ly_cur = nullptr;
@@ -507,9 +510,16 @@ struct Plan : PlanBase {
 		else b.alloc(bytes);
 	}
 
+	// The frame in which the y-lines are x-lines (x' = y, y' = x).
+	static Geom transposed(const Geom& G) {
+		Geom t = G;
+		t.Nx = G.Ny; t.Ny = G.Nx;
+		return t;
+	}
+
 	SolveShape shape_of(const SampleHost& h) const {
 		SolveShape sh;
-		sh.Nx = h.s.Nx; sh.Ny = h.s.Ny; sh.spg = h.spg; sh.ng = gpp(h);
+		sh.Nx = h.s.Nx; sh.Ny = h.s.Ny; sh.spg = h.spg; sh.ng = gpp(h); sh.nw = h.s.n_woodbury;
 		sh.fp32 = sizeof(R) == sizeof(float); sh.nsm = nsm;
 		if(smem_limit) sh.smem = smem_limit;
 		return sh;
@@ -528,8 +538,10 @@ struct Plan : PlanBase {
 			size_t px = sc.plane_x;
 			for(auto& c : x_candidates(sh, true)) px = std::max(px, c.plane_x);
 			sc.plane_x = px;
-			bool need_t3 = sc.ys;
-			for(auto& c : y_candidates(sh, true)) need_t3 |= c.ys;
+			bool need_t3 = sc.ys, need_t = sc.Mxt > 0;
+			size_t py = sc.plane_y;
+			for(auto& c : y_candidates(sh, true)) { need_t3 |= c.ys; need_t |= c.Mxt > 0; py = std::max(py, c.plane_y); }
+			sc.plane_y = py;
 			scfg.push_back(sc);
 			// the sample's workspace (its lane)
 			{
@@ -542,6 +554,10 @@ struct Plan : PlanBase {
 				dalloc(L.Qring, sizeof(R) * (size_t)2 * ng * NQ * N);
 				dalloc(L.coef, sizeof(cx<R>) * (size_t)2 * ng * NCOEF * N);  // two slabs (transition kernels)
 				dalloc(L.diag, sizeof(cx<R>) * (size_t)ng * NDIAG * N);
+				if(need_t) {
+					dalloc(L.coefT, sizeof(cx<R>) * (size_t)2 * ng * NCOEF * N);
+					dalloc(L.diagT, sizeof(cx<R>) * (size_t)ng * NDIAG * N);
+				}
 				L.facx_half = L.facy_half = nFx;
 				L.lsc_half = nL;
 				dalloc(L.facx, sizeof(cx<R>) * nFx * 2);
@@ -551,7 +567,7 @@ struct Plan : PlanBase {
 				dalloc(L.scr, sizeof(cx<R>) * (size_t)2 * ng * 2 * 2 * N);  // x and y halves
 				if(sizeof(R) != sizeof(double)) dalloc(L.stage, sizeof(cx<double>) * (size_t)h.slots * 2 * N);
 				for(DevBuf* b : {&L.T, &L.T2, &L.T3, &L.Qring, &L.coef, &L.diag, &L.facx, &L.facy, &L.lscx, &L.lscy,
-						&L.scr, &L.stage})
+						&L.scr, &L.stage, &L.coefT, &L.diagT})
 					dev_bytes += b->bytes;
 			}
 			// per-sample buffers
@@ -603,6 +619,9 @@ struct Plan : PlanBase {
 				};
 				if(fx != "auto") pick(xr, fx, true);
 				if(fy != "auto") pick(yr, fy, false);
+				if(sc.Mxt && !sc.x_is_xc())
+					throw BackendError(E_ARG, "solve configuration '" + forced + "': the transposed-frame y solves (yx) need "
+						"the x-lines on the one-warp-per-line kernel (xc)");
 				tune_notes[h.index] = "forced";
 				if(fx != "auto" && fy != "auto") { sc.plane_x = pmax; continue; }
 			}
@@ -631,6 +650,7 @@ struct Plan : PlanBase {
 				SolveCfg win = sc;
 				std::string times;
 				for(auto& c : cands) {
+					if(dirn == 1 && c.Mxt && !keep.x_is_xc()) continue;
 					SolveCfg t = keep;
 					if(dirn == 0) t.set_x(c); else t.set_y(c);
 					t.plane_x = pmax;
@@ -652,11 +672,12 @@ struct Plan : PlanBase {
 		}
 		launches = 0;
 		// the scratch field of the scratch-chunk y solve is kept only where that solve was chosen
-		for(auto& hp : S)
-			if(!scfg[hp->index].ys && hp->lane.T3.p) {
-				dev_bytes -= (long long)hp->lane.T3.bytes;
-				hp->lane.T3.alloc(0);
-			}
+		for(auto& hp : S) {
+			auto& L = hp->lane;
+			auto drop = [&](DevBuf& b) { dev_bytes -= (long long)b.bytes; b.alloc(0); };
+			if(!scfg[hp->index].ys && L.T3.p) drop(L.T3);
+			if(!scfg[hp->index].Mxt && L.coefT.p) { drop(L.coefT); drop(L.diagT); }
+		}
 		select(*S[0]);
 	}
 
@@ -672,7 +693,7 @@ struct Plan : PlanBase {
 	void zero_workspace() {
 		for(auto& hp : S) {
 			auto& L = hp->lane;
-			for(DevBuf* b : {&L.T, &L.T2, &L.T3, &L.coef, &L.facx, &L.facy, &L.lscx, &L.lscy, &hp->F})
+			for(DevBuf* b : {&L.T, &L.T2, &L.T3, &L.coef, &L.facx, &L.facy, &L.lscx, &L.lscy, &L.coefT, &L.diagT, &hp->F})
 				if(b->p) CK(cudaMemsetAsync(b->p, 0, b->bytes, stream0));
 		}
 		CK(cudaStreamSynchronize(stream0));
@@ -688,6 +709,7 @@ struct Plan : PlanBase {
 		select(h);
 		fx_cur = W->facx.as<cx<R>>(); fy_cur = W->facy.as<cx<R>>();
 		lx_cur = W->lscx.as<cx<double>>(); ly_cur = W->lscy.as<cx<double>>();
+		ct_cur = W->coefT.as<cx<R>>();
 		float best = 1e30f;
 		for(int r = 0; r < 4; r++) {
 			CK(cudaEventRecord(ev[2], stream));
@@ -1003,11 +1025,27 @@ struct Plan : PlanBase {
 				k_factor_chunked<R, 0><<<dim3((unsigned)((Ny + LT - 1) / LT), (unsigned)(ng * 2)), dim3(32, LT), 0, cs>>>(
 					Gm, ng, scf.Mx, 32 * scf.WPLx, 1, ps.Dg, fx, scf.plane_x, lx);
 			});
-			size_t smem = (size_t)WF * 32 * 8 * sizeof(cx<R>) + 64 * sizeof(cx<R>);
-			launch("factor_y", fb, [&] {
-				k_factor_chunked<R, 1><<<dim3((unsigned)((Nx + 31) / 32), (unsigned)(ng * 2)), dim3(32, WF), smem, cs>>>(
-					Gm, ng, 0, 32, WF, ps.Dg, fy, scf.plane_y, ly);
-			});
+			cx<R>* CT = scf.Mxt ? W->coefT.as<cx<R>>() + (size_t)(iz & 1) * ng * NCOEF * N : nullptr;
+			if(scf.Mxt) {
+				// y-lines as x-lines of the transposed frame: transposed coefficients and diagonals,
+				// then the x-line factorisation of that frame
+				const Geom Gt = transposed(Gm);
+				launch("coef_t", 2.0 * N * ng * NCT * sc, [&] {
+					k_coef_t<R><<<dim3((unsigned)((Nx + 31) / 32), (unsigned)((Ny + 31) / 32), (unsigned)(ng * NCT)), dim3(32, 8), 0,
+						cs>>>(Gm, C, ps.Dg, CT, W->diagT.as<cx<R>>());
+				});
+				launch("factor_y", fb, [&] {
+					k_factor_chunked<R, 0><<<dim3((unsigned)((Nx + LT - 1) / LT), (unsigned)(ng * 2)), dim3(32, LT), 0, cs>>>(
+						Gt, ng, scf.Mxt, 32, 1, W->diagT.as<cx<R>>(), fy, scf.plane_y, ly);
+				});
+			}
+			else {
+				size_t smem = (size_t)WF * 32 * 8 * sizeof(cx<R>) + 64 * sizeof(cx<R>);
+				launch("factor_y", fb, [&] {
+					k_factor_chunked<R, 1><<<dim3((unsigned)((Nx + 31) / 32), (unsigned)(ng * 2)), dim3(32, WF), smem, cs>>>(
+						Gm, ng, 0, 32, WF, ps.Dg, fy, scf.plane_y, ly);
+				});
+			}
 			CK(cudaEventRecord(eFac, streamB));
 			// ---- main stream ----
 			cs = stream;
@@ -1016,7 +1054,7 @@ struct Plan : PlanBase {
 			const cx<R>* xsrc = rec_transition(h, slot0, nsl, ps.Cprev, C, ps.Fp, ps.Tb, ps.T2b, iz > 0);
 			CK(cudaEventRecord(eTrans, stream));
 			CK(cudaStreamWaitEvent(stream, eFac, 0));
-			fx_cur = fx; fy_cur = fy; lx_cur = lx; ly_cur = ly;
+			fx_cur = fx; fy_cur = fy; lx_cur = lx; ly_cur = ly; ct_cur = CT;
 			rec_adi(h, Gm, slot0, nsl, ng, Nw, C, ps.Fp, ps.Tb, ps.T2b, xsrc);
 			rec_bulk(h, ps, iz + 1, C);
 			CK(cudaEventRecord(eAdi[iz & 1], stream));
@@ -1196,14 +1234,16 @@ struct Plan : PlanBase {
 	// Whether the fused solve of direction dirn runs k_solve_xc / k_solve_yc, the kernels that take
 	// a second accumulator input.
 	bool solve_takes_acc2(const SolveCfg& sc, int dirn) const {
-		return dirn == 0 ? (sc.Mx > 0 && sc.WPLx == 1 && !sc.xs) : (sc.yq > 0 || sc.Mt > 0 || (sc.My > 0 && !sc.ys));
+		return dirn == 0 ? (sc.Mx > 0 && sc.WPLx == 1 && !sc.xs) : (sc.yq > 0 || sc.Mt > 0 || sc.Mxt > 0 || (sc.My > 0 && !sc.ys));
 	}
 
 	// scr: a field-sized buffer the solve may overwrite (none of src, acc_in, acc_in2), used by the
 	// sequential y solve for its forward values.
+	// tout: k_solve_xc writes its results transposed with the components exchanged (the hand-over
+	// between the x frame and the transposed frame of the y solves).
 	void rec_solve_fused(int dirn, bool wood, SampleHost& h, const Geom& Gm, int slot0, int nsl, int ng,
 			const cx<R>* C, const cx<R>* src, cx<R>* dst, const cx<R>* acc_in, cx<R>* acc_out,
-			const cx<R>* acc_in2, cx<R>* scr) {
+			const cx<R>* acc_in2, cx<R>* scr, bool tout = false) {
 		const SolveCfg& sc = scfg[h.index];
 		const double sz = sizeof(cx<R>);
 		double fp = (double)Gm.N * nsl * 2 * sz;
@@ -1243,10 +1283,27 @@ struct Plan : PlanBase {
 			L.grid = dim3((unsigned)((Gm.Ny + LT - 1) / LT), (unsigned)(ng * nch * 2));
 			L.block = dim3(32 * LT);
 			L.smem = (size_t)LT * L.KS * 32 * (L.M + 1) * sizeof(cx<R>);
+			L.tout = tout;
 			launch(wood ? "wood_solve_x" : "expl_solve_x", bytes, [&] {
 				if(!launch_solve_xc<R>(L, Gm, slot0, nch, C, fx_cur, sc.plane_x, lx_cur, src,
 						dst, acc_in, acc_out, acc_in2))
 					throw BackendError(E_INTERNAL, "no x-solve instance");
+			});
+		}
+		else if(sc.Mxt) {
+			// y-lines as x-lines of the transposed frame (fields, coefficients and factors there)
+			const Geom Gt = transposed(Gm);
+			const int LT = 4;
+			L.M = sc.Mxt; L.KS = sc.KSy; L.kind = wood ? ST_WOOD_X : ST_EXPL_Y;
+			const int nch = h.spg / L.KS;
+			L.grid = dim3((unsigned)((Gt.Ny + LT - 1) / LT), (unsigned)(ng * nch * 2));
+			L.block = dim3(32 * LT);
+			L.smem = (size_t)LT * L.KS * 32 * (L.M + 1) * sizeof(cx<R>);
+			L.tout = tout;
+			launch(wood ? "wood_solve_y" : "expl_solve_y", bytes, [&] {
+				if(!launch_solve_xc<R>(L, Gt, slot0, nch, ct_cur, fy_cur, sc.plane_y, ly_cur, src, dst, acc_in, acc_out,
+						acc_in2))
+					throw BackendError(E_INTERNAL, "no y-solve instance");
 			});
 		}
 		else if(sc.Mt) {
@@ -1319,7 +1376,7 @@ struct Plan : PlanBase {
 		const SolveCfg& cfg = scfg[h.index];
 		for(int dirn = 0; dirn < 2; dirn++) {
 			if(only_dirn >= 0 && dirn != only_dirn) continue;
-			bool fused = dirn == 0 ? cfg.Mx > 0 : (cfg.My > 0 || cfg.ys || cfg.yq > 0 || cfg.Mt > 0);
+			bool fused = dirn == 0 ? cfg.Mx > 0 : (cfg.My > 0 || cfg.ys || cfg.yq > 0 || cfg.Mt > 0 || cfg.Mxt > 0);
 			if(fused) {
 				// t0 = solve(f + mu R f) written to T; Woodbury: t_k = solve(mu R' t_{k-1}),
 				// F = t0 + t1 + ... accumulated by the solves (the last t_k is not stored).
@@ -1352,7 +1409,9 @@ struct Plan : PlanBase {
 				const cx<R>* ai = it == 1 ? Tb : Fp;
 				if(acc2) {
 					if(it == 1) rec_solve_fused(dirn, true, h, Gm, slot0, nsl, ng, C, cur, oth, nullptr, nullptr, nullptr, oth);
-					else rec_solve_fused(dirn, true, h, Gm, slot0, nsl, ng, C, cur, nullptr, Tb, Fp, cur, Fp);
+					// with the transposed-frame y solves, each direction's last solve hands F over
+					// transposed (x frame -> transposed frame -> x frame)
+					else rec_solve_fused(dirn, true, h, Gm, slot0, nsl, ng, C, cur, nullptr, Tb, Fp, cur, Fp, cfg.Mxt > 0);
 				}
 				else if(fused) {
 					// oth holds t_{it-2} (or nothing), no longer needed: free for the forward values
@@ -1697,7 +1756,7 @@ int nbpm_solve_candidates(const char* json_str, int precision, int groups_per_pa
 		if(precision != NBPM_FP64 && precision != NBPM_FP32) return fail(E_ARG, "unknown precision");
 		BackendSettings s = parse_settings(json_str);
 		SolveShape sh;
-		sh.Nx = s.Nx; sh.Ny = s.Ny; sh.spg = 2 * (int)s.q.size();
+		sh.Nx = s.Nx; sh.Ny = s.Ny; sh.spg = 2 * (int)s.q.size(); sh.nw = s.n_woodbury;
 		int G = (int)s.wavelengths.size();
 		sh.ng = groups_per_pass <= 0 ? G : std::max(1, std::min(groups_per_pass, G));
 		sh.fp32 = precision == NBPM_FP32;

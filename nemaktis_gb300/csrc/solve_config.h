@@ -36,8 +36,11 @@ struct SolveCfg {
 	// a scratch field (k_solve_ys, KSy slots); My > 0 32 columns x WY warps of M-row chunks
 	// (k_solve_yc, KSy slots; y1024w: the Woodbury solves with 32 warps of 8-row chunks and 2
 	// slots per thread); else sequential (k_stencil + k_solve).
-	// Mt > 0: one warp per column with Mt-row lane chunks (k_solve_yt, KSy slots).
-	int My = 0, WY = 0, KSy = 1, yq = 0, Mt = 0;
+	// Mt > 0: one warp per column with Mt-row lane chunks (k_solve_yt, KSy slots). Mxt > 0: the
+	// y-lines solved as x-lines of the transposed frame (k_solve_xc on transposed fields and
+	// coefficients, Mxt-point lane chunks, KSy slots); needs the x-lines on k_solve_xc, whose last
+	// Woodbury solve hands the fields over transposed, and two Woodbury steps.
+	int My = 0, WY = 0, KSy = 1, yq = 0, Mt = 0, Mxt = 0;
 	bool ys = false, y1024w = false;
 	// factor plane sizes (elements per factor and line set), from the x layout
 	size_t plane_x = 0, plane_y = 0;
@@ -54,6 +57,7 @@ struct SolveCfg {
 		char b[64];
 		if(yq) std::snprintf(b, sizeof b, "yq:KS=%d", yq);
 		else if(Mt) std::snprintf(b, sizeof b, "yt:M=%d:KS=%d", Mt, KSy);
+		else if(Mxt) std::snprintf(b, sizeof b, "yx:M=%d:KS=%d", Mxt, KSy);
 		else if(ys) std::snprintf(b, sizeof b, "ys:KS=%d", KSy);
 		else if(My) std::snprintf(b, sizeof b, "yc:M=%d:KS=%d:W=%d%s", My, KSy, WY, y1024w ? ":W1024" : "");
 		else return "yseq";
@@ -61,7 +65,11 @@ struct SolveCfg {
 	}
 	std::string str() const { return xstr() + ";" + ystr(); }
 	void set_x(const SolveCfg& o) { Mx = o.Mx; KSx = o.KSx; WPLx = o.WPLx; xs = o.xs; }
-	void set_y(const SolveCfg& o) { My = o.My; WY = o.WY; KSy = o.KSy; yq = o.yq; Mt = o.Mt; ys = o.ys; y1024w = o.y1024w; }
+	void set_y(const SolveCfg& o) {
+		My = o.My; WY = o.WY; KSy = o.KSy; yq = o.yq; Mt = o.Mt; Mxt = o.Mxt; ys = o.ys; y1024w = o.y1024w;
+	}
+	// x on k_solve_xc (one warp per line, chunks in registers and a shared buffer)
+	bool x_is_xc() const { return Mx > 0 && WPLx == 1 && !xs; }
 };
 
 // What the choice depends on.
@@ -69,6 +77,7 @@ struct SolveShape {
 	int Nx = 0, Ny = 0;
 	int spg = 2;        // slots (q, pol) per wavelength
 	int ng = 1;         // wavelengths per pass
+	int nw = 2;         // Woodbury steps
 	bool fp32 = false;
 	int nsm = 152;      // streaming multiprocessors
 	size_t smem = 227 * 1024;  // opt-in shared memory per block
@@ -85,7 +94,8 @@ inline size_t plane_x_of(const SolveCfg& c, const SolveShape& s) {
 
 inline void finalize(SolveCfg& c, const SolveShape& s) {
 	c.plane_x = plane_x_of(c, s);
-	c.plane_y = (size_t)s.Nx * s.Ny;
+	// transposed-frame y factors: the chunk-interleaved x layout of Nx lines of 32 * Mxt points
+	c.plane_y = std::max((size_t)s.Nx * s.Ny, c.Mxt ? (size_t)s.Nx * 32 * c.Mxt : (size_t)0);
 }
 
 inline bool xs_fits(int ks, int M, const SolveShape& s) { return (size_t)4 * ks * 32 * (M + 1) * s.csize() <= 100 * 1024; }
@@ -152,6 +162,7 @@ inline std::vector<SolveCfg> y_candidates(const SolveShape& s0, bool relaxed = f
 			for(int ks : {4, 2, 1})
 				if(s.spg % ks == 0 && solve_pair_ok(Mt, ks) && (Mt * ks <= s.cap() || ks == 1)) {
 					SolveCfg c; c.Mt = Mt; c.KSy = ks; out.push_back(c);
+					if(s.Nx > 3 && s.nw == 2) { SolveCfg t; t.Mxt = Mt; t.KSy = ks; out.push_back(t); }
 				}
 		}
 		for(int ks : {4, 2, 1})

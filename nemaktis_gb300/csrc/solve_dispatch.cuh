@@ -11,6 +11,7 @@ namespace nbpm {
 
 struct SolveLaunch {
 	int M, KS, kind;           // chunk length, slots per thread, stencil kind (ST_*)
+	bool tout = false;         // k_solve_xc: transposed, component-exchanged output (ST_WOOD_X only)
 	dim3 grid, block;
 	size_t smem;
 	cudaStream_t stream;

@@ -4,9 +4,14 @@
 namespace nbpm {
 
 #define NBPM_XC(MM, KK, KD) \
-	if(L.M == MM && L.KS == KK && L.kind == KD) { \
+	if(L.M == MM && L.KS == KK && L.kind == KD && !L.tout) { \
 		k_solve_xc<double, MM, KD, KK><<<L.grid, L.block, L.smem, L.stream>>>(G, slot0, nch, coef, fac, plane, lsc, \
 			src, dst, ai, ao, ai2); \
+		return true; \
+	} \
+	if(L.M == MM && L.KS == KK && L.kind == KD && L.tout && KD == ST_WOOD_X) { \
+		k_solve_xc<double, MM, ST_WOOD_X, KK, true><<<L.grid, L.block, L.smem, L.stream>>>(G, slot0, nch, coef, fac, plane, \
+			lsc, src, dst, ai, ao, ai2); \
 		return true; \
 	}
 #define NBPM_XC_PAIRS(KIND) \
@@ -28,9 +33,14 @@ bool launch_solve_xc<double>(const SolveLaunch& L, Geom G, int slot0, int nch, c
 	NBPM_XA(2, 1, KIND) NBPM_XA(2, 2, KIND) NBPM_XA(2, 4, KIND) NBPM_XA(4, 1, KIND) NBPM_XA(4, 2, KIND) NBPM_XA(4, 4, KIND) \
 	NBPM_XA(8, 1, KIND) NBPM_XA(8, 2, KIND) NBPM_XA(8, 4, KIND) NBPM_XA(16, 1, KIND) NBPM_XA(16, 2, KIND) NBPM_XA(32, 1, KIND)
 
+#define NBPM_XAT(MM, KK) \
+	cudaFuncSetAttribute(k_solve_xc<double, MM, ST_WOOD_X, KK, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+
 void set_solve_smem_x_f64(int bytes) {
 	NBPM_XA_PAIRS(ST_EXPL_Y)
 	NBPM_XA_PAIRS(ST_WOOD_X)
+	NBPM_XAT(2, 1) NBPM_XAT(2, 2) NBPM_XAT(2, 4) NBPM_XAT(4, 1) NBPM_XAT(4, 2) NBPM_XAT(4, 4)
+	NBPM_XAT(8, 1) NBPM_XAT(8, 2) NBPM_XAT(8, 4) NBPM_XAT(16, 1) NBPM_XAT(16, 2) NBPM_XAT(32, 1)
 }
 
 #define NBPM_XS(KK, KD) \

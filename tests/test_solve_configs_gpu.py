@@ -33,9 +33,17 @@ MESHES = {
 
 def configs(js, precision):
     c = _lib.solve_candidates(js, precision)
-    # every x candidate with the default y, every y candidate with the default x
+    # every x candidate with the default y, every y candidate with the default x (the transposed-
+    # frame y solves "yx" need an "xc" x solve: paired with the first one)
     dx, dy = c["default"].split(";")
-    return sorted({x + ";" + dy for x in c["x"]} | {dx + ";" + y for y in c["y"]})
+    xc = [x for x in c["x"] if x.startswith("xc:")]
+    out = {x + ";" + dy for x in c["x"]}
+    for y in c["y"]:
+        if not y.startswith("yx:"):
+            out.add(dx + ";" + y)
+        elif xc:
+            out.add((dx if dx.startswith("xc:") else xc[0]) + ";" + y)
+    return sorted(out)
 
 
 @pytest.mark.parametrize("name", sorted(MESHES))
