@@ -267,12 +267,14 @@ def run_ours(args):
     # DRAM bytes per launch of the dominant kernel from one ncu capture (dram__bytes_read.sum +
     # dram__bytes_write.sum), scaled to this workload's launch by the slots it processes; the
     # capture and its command are summarised under profiles/.
-    PROF = "profiles/slab_main_stream_koehler_256x256x8_fp32.md"
-    TRAFFIC = {("config3", "fp32", "wood_solve_y"): (2 * (505.1e6 + 762.8e6) / 2, PROF),
-               ("config3", "fp32", "expl_solve_y"): (2 * 532.3e6, PROF),
-               ("config3", "fp32", "wood_solve_x"): (2 * (504.0e6 + 753.7e6) / 2, PROF),
-               ("config3", "fp32", "expl_solve_x"): (2 * 545.6e6, PROF),
-               ("config3", "fp32", "shift_fused"): (2 * 432.0e6, PROF)}
+    PROF = "profiles/solve_xc_koehler_256x256x8_fp32.md"
+    PSF = "profiles/shift_fused_koehler_256x256x8_fp32.md"
+    W = 2 * (319.3e6 + 184.3e6 + 562.6e6 + 197.7e6) / 2  # mean of the two Woodbury launches, x2 slots
+    TRAFFIC = {("config3", "fp32", "wood_solve_x"): (W, PROF),
+               ("config3", "fp32", "wood_solve_y"): (W, PROF + " (the same kernel in the transposed frame)"),
+               ("config3", "fp32", "expl_solve_x"): (2 * (344.6e6 + 188.5e6), PROF),
+               ("config3", "fp32", "expl_solve_y"): (2 * (344.6e6 + 188.5e6), PROF + " (the same kernel in the transposed frame)"),
+               ("config3", "fp32", "shift_fused"): (2 * (242.5e6 + 189.5e6), PSF)}
     roof = None
     if prof:
         top = max(prof, key=lambda k: prof[k]["ms"])

@@ -1671,10 +1671,14 @@ __global__ void __launch_bounds__(128) k_solve_yq(Geom G, int nch, const cx<R>* 
 // x-line solve for long lines: one block of W warps per line, 32*W chunks of M points (the
 // chunk-interleaved factor layout with 32*W chunks). Within a warp the chunk maps combine with
 // shuffles as in k_solve_xc, across the warps of the line through shared memory.
-template <typename R, int M, int KIND, int KS>
+// acc_in2 (may be null): a second accumulator input, acc_out = (acc_in + acc_in2) + x. TOUT: the
+// results go out transposed with the components exchanged ((c, iy, e) -> (1 - c, e, iy) of an
+// Ny x Nx plane), as in k_solve_xc.
+template <typename R, int M, int KIND, int KS, bool TOUT = false>
 __global__ void __launch_bounds__(256) k_solve_xw(Geom G, int slot0, int nch, const cx<R>* __restrict__ coef,
 		const cx<R>* __restrict__ fac, size_t plane, const cx<double>* __restrict__ lsc,
-		const cx<R>* __restrict__ src, cx<R>* __restrict__ dst, const cx<R>* acc_in, cx<R>* acc_out) {
+		const cx<R>* __restrict__ src, cx<R>* __restrict__ dst, const cx<R>* acc_in, cx<R>* acc_out,
+		const cx<R>* acc_in2) {
 	extern __shared__ unsigned char smem_raw[];
 	const int W = blockDim.x / 32;
 	const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
@@ -1844,11 +1848,13 @@ __global__ void __launch_bounds__(256) k_solve_xw(Geom G, int slot0, int nch, co
 	__syncthreads();
 	for(int j = 0; j < KS; j++) {
 		const size_t off = (size_t)(s0 + j) * 2 * N + (size_t)c * N + (size_t)iy * Nx;
+		const size_t toff = (size_t)(s0 + j) * 2 * N + (size_t)(1 - c) * N + iy;
 		for(int e = threadIdx.x; e < Nx; e += blockDim.x) {
 			int ee = e == Nx - 1 ? 0 : e;
 			cx<R> x = buf[j * PITCH + (ee / M) * (M + 1) + ee % M];
-			if(dst) dst[off + e] = x;
-			if(acc_out) acc_out[off + e] = acc_in[off + e] + x;
+			const size_t o = TOUT ? toff + (size_t)e * Ny : off + e;
+			if(dst) dst[o] = x;
+			if(acc_out) acc_out[o] = (acc_in2 ? acc_in[off + e] + acc_in2[off + e] : acc_in[off + e]) + x;
 		}
 	}
 }
@@ -2335,6 +2341,9 @@ __global__ void __launch_bounds__(256) k_shift_fused(Geom G, int slot0, const Sh
 	const int wx = ax ? SHT + 3 * nsh : SHT, wy = ay ? SHT + 3 * nsh : SHT;
 	cx<R> ph = mk<R>((R)P.ph_re, (R)P.ph_im);
 	if(nsh == 2) ph = ph * ph;
+	// the interpolation weights in the arithmetic type, converted once
+	const R wx0 = (R)P.wx[0], wx1 = (R)P.wx[1], wx2 = (R)P.wx[2], wx3 = (R)P.wx[3];
+	const R wy0 = (R)P.wy[0], wy1 = (R)P.wy[1], wy2 = (R)P.wy[2], wy3 = (R)P.wy[3];
 	// every tap index of both passes stays above -(N-1): mod arithmetic equals the wrap rule
 	const bool regular = (!ax || P.msx - 1 > -Px) && (!ay || P.msy - 1 > -Py);
 	if(!regular) {
@@ -2375,8 +2384,7 @@ __global__ void __launch_bounds__(256) k_shift_fused(Geom G, int slot0, const Sh
 				int t = e % ow, v = e / ow;
 				for(int c = 0; c < 2; c++) {
 					const cx<R>* in = cur + c * PW * PW + v * PW + t;
-					nxt[c * PW * PW + v * PW + t] = (R)P.wx[0] * in[0] + (R)P.wx[1] * in[1] + (R)P.wx[2] * in[2] +
-						(R)P.wx[3] * in[3];
+					nxt[c * PW * PW + v * PW + t] = wx0 * in[0] + wx1 * in[1] + wx2 * in[2] + wx3 * in[3];
 				}
 			}
 			__syncthreads();
@@ -2393,8 +2401,7 @@ __global__ void __launch_bounds__(256) k_shift_fused(Geom G, int slot0, const Sh
 				int t = e % SHT, v = e / SHT;
 				for(int c = 0; c < 2; c++) {
 					const cx<R>* in = cur + c * PW * PW + v * PW + t;
-					nxt[c * PW * PW + v * PW + t] = (R)P.wy[0] * in[0] + (R)P.wy[1] * in[PW] +
-						(R)P.wy[2] * in[2 * PW] + (R)P.wy[3] * in[3 * PW];
+					nxt[c * PW * PW + v * PW + t] = wy0 * in[0] + wy1 * in[PW] + wy2 * in[2 * PW] + wy3 * in[3 * PW];
 				}
 			}
 			__syncthreads();

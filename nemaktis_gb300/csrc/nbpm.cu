@@ -619,9 +619,9 @@ struct Plan : PlanBase {
 				};
 				if(fx != "auto") pick(xr, fx, true);
 				if(fy != "auto") pick(yr, fy, false);
-				if(sc.Mxt && !sc.x_is_xc())
+				if(sc.Mxt && !sc.x_hands_over())
 					throw BackendError(E_ARG, "solve configuration '" + forced + "': the transposed-frame y solves (yx) need "
-						"the x-lines on the one-warp-per-line kernel (xc)");
+						"the x-lines on a kernel that hands the fields over (xc or xw)");
 				tune_notes[h.index] = "forced";
 				if(fx != "auto" && fy != "auto") { sc.plane_x = pmax; continue; }
 			}
@@ -650,7 +650,7 @@ struct Plan : PlanBase {
 				SolveCfg win = sc;
 				std::string times;
 				for(auto& c : cands) {
-					if(dirn == 1 && c.Mxt && !keep.x_is_xc()) continue;
+					if(dirn == 1 && c.Mxt && !keep.x_hands_over()) continue;
 					SolveCfg t = keep;
 					if(dirn == 0) t.set_x(c); else t.set_y(c);
 					t.plane_x = pmax;
@@ -1036,7 +1036,7 @@ struct Plan : PlanBase {
 				});
 				launch("factor_y", fb, [&] {
 					k_factor_chunked<R, 0><<<dim3((unsigned)((Nx + LT - 1) / LT), (unsigned)(ng * 2)), dim3(32, LT), 0, cs>>>(
-						Gt, ng, scf.Mxt, 32, 1, W->diagT.as<cx<R>>(), fy, scf.plane_y, ly);
+						Gt, ng, scf.Mxt, 32 * scf.WPLt, 1, W->diagT.as<cx<R>>(), fy, scf.plane_y, ly);
 				});
 			}
 			else {
@@ -1234,7 +1234,7 @@ struct Plan : PlanBase {
 	// Whether the fused solve of direction dirn runs k_solve_xc / k_solve_yc, the kernels that take
 	// a second accumulator input.
 	bool solve_takes_acc2(const SolveCfg& sc, int dirn) const {
-		return dirn == 0 ? (sc.Mx > 0 && sc.WPLx == 1 && !sc.xs) : (sc.yq > 0 || sc.Mt > 0 || sc.Mxt > 0 || (sc.My > 0 && !sc.ys));
+		return dirn == 0 ? (sc.Mx > 0 && !sc.xs) : (sc.yq > 0 || sc.Mt > 0 || sc.Mxt > 0 || (sc.My > 0 && !sc.ys));
 	}
 
 	// scr: a field-sized buffer the solve may overwrite (none of src, acc_in, acc_in2), used by the
@@ -1264,8 +1264,9 @@ struct Plan : PlanBase {
 				L.grid = dim3((unsigned)Gm.Ny, (unsigned)(ng * nch * 2));
 				L.block = dim3(32 * sc.WPLx);
 				L.smem = ((size_t)L.KS * 32 * sc.WPLx * (L.M + 1) + 4 * L.KS * sc.WPLx + 2 * L.KS) * sizeof(cx<R>);
+				L.tout = tout;
 				launch(wood ? "wood_solve_x" : "expl_solve_x", bytes, [&] {
-					if(!launch_solve_xw<R>(L, Gm, slot0, nch, C, fx_cur, sc.plane_x, lx_cur, src, dst, acc_in, acc_out))
+					if(!launch_solve_xw<R>(L, Gm, slot0, nch, C, fx_cur, sc.plane_x, lx_cur, src, dst, acc_in, acc_out, acc_in2))
 						throw BackendError(E_INTERNAL, "no x-solve instance");
 				});
 				return;
@@ -1288,6 +1289,20 @@ struct Plan : PlanBase {
 				if(!launch_solve_xc<R>(L, Gm, slot0, nch, C, fx_cur, sc.plane_x, lx_cur, src,
 						dst, acc_in, acc_out, acc_in2))
 					throw BackendError(E_INTERNAL, "no x-solve instance");
+			});
+		}
+		else if(sc.Mxt && sc.WPLt > 1) {
+			// long y-lines as several-warps-per-line x-lines of the transposed frame
+			const Geom Gt = transposed(Gm);
+			L.M = sc.Mxt; L.KS = sc.KSy; L.kind = wood ? ST_WOOD_X : ST_EXPL_Y;
+			const int nch = h.spg / L.KS;
+			L.grid = dim3((unsigned)Gt.Ny, (unsigned)(ng * nch * 2));
+			L.block = dim3(32 * sc.WPLt);
+			L.smem = ((size_t)L.KS * 32 * sc.WPLt * (L.M + 1) + 4 * L.KS * sc.WPLt + 2 * L.KS) * sizeof(cx<R>);
+			L.tout = tout;
+			launch(wood ? "wood_solve_y" : "expl_solve_y", bytes, [&] {
+				if(!launch_solve_xw<R>(L, Gt, slot0, nch, ct_cur, fy_cur, sc.plane_y, ly_cur, src, dst, acc_in, acc_out, acc_in2))
+					throw BackendError(E_INTERNAL, "no y-solve instance");
 			});
 		}
 		else if(sc.Mxt) {

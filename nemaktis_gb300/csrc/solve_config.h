@@ -40,7 +40,8 @@ struct SolveCfg {
 	// y-lines solved as x-lines of the transposed frame (k_solve_xc on transposed fields and
 	// coefficients, Mxt-point lane chunks, KSy slots); needs the x-lines on k_solve_xc, whose last
 	// Woodbury solve hands the fields over transposed, and two Woodbury steps.
-	int My = 0, WY = 0, KSy = 1, yq = 0, Mt = 0, Mxt = 0;
+	// WPLt > 1: the transposed frame's x-lines on k_solve_xw (WPLt warps per line, Mxt = 8).
+	int My = 0, WY = 0, KSy = 1, yq = 0, Mt = 0, Mxt = 0, WPLt = 1;
 	bool ys = false, y1024w = false;
 	// factor plane sizes (elements per factor and line set), from the x layout
 	size_t plane_x = 0, plane_y = 0;
@@ -57,6 +58,7 @@ struct SolveCfg {
 		char b[64];
 		if(yq) std::snprintf(b, sizeof b, "yq:KS=%d", yq);
 		else if(Mt) std::snprintf(b, sizeof b, "yt:M=%d:KS=%d", Mt, KSy);
+		else if(Mxt && WPLt > 1) std::snprintf(b, sizeof b, "yx:M=%d:KS=%d:W=%d", Mxt, KSy, WPLt);
 		else if(Mxt) std::snprintf(b, sizeof b, "yx:M=%d:KS=%d", Mxt, KSy);
 		else if(ys) std::snprintf(b, sizeof b, "ys:KS=%d", KSy);
 		else if(My) std::snprintf(b, sizeof b, "yc:M=%d:KS=%d:W=%d%s", My, KSy, WY, y1024w ? ":W1024" : "");
@@ -66,10 +68,12 @@ struct SolveCfg {
 	std::string str() const { return xstr() + ";" + ystr(); }
 	void set_x(const SolveCfg& o) { Mx = o.Mx; KSx = o.KSx; WPLx = o.WPLx; xs = o.xs; }
 	void set_y(const SolveCfg& o) {
-		My = o.My; WY = o.WY; KSy = o.KSy; yq = o.yq; Mt = o.Mt; Mxt = o.Mxt; ys = o.ys; y1024w = o.y1024w;
+		My = o.My; WY = o.WY; KSy = o.KSy; yq = o.yq; Mt = o.Mt; Mxt = o.Mxt; WPLt = o.WPLt; ys = o.ys;
+		y1024w = o.y1024w;
 	}
-	// x on k_solve_xc (one warp per line, chunks in registers and a shared buffer)
-	bool x_is_xc() const { return Mx > 0 && WPLx == 1 && !xs; }
+	// x on k_solve_xc or k_solve_xw: the kernels whose last Woodbury solve can hand the fields over
+	// to the transposed frame
+	bool x_hands_over() const { return Mx > 0 && !xs; }
 };
 
 // What the choice depends on.
@@ -95,7 +99,7 @@ inline size_t plane_x_of(const SolveCfg& c, const SolveShape& s) {
 inline void finalize(SolveCfg& c, const SolveShape& s) {
 	c.plane_x = plane_x_of(c, s);
 	// transposed-frame y factors: the chunk-interleaved x layout of Nx lines of 32 * Mxt points
-	c.plane_y = std::max((size_t)s.Nx * s.Ny, c.Mxt ? (size_t)s.Nx * 32 * c.Mxt : (size_t)0);
+	c.plane_y = std::max((size_t)s.Nx * s.Ny, c.Mxt ? (size_t)s.Nx * 32 * c.WPLt * c.Mxt : (size_t)0);
 }
 
 inline bool xs_fits(int ks, int M, const SolveShape& s) { return (size_t)4 * ks * 32 * (M + 1) * s.csize() <= 100 * 1024; }
@@ -163,6 +167,14 @@ inline std::vector<SolveCfg> y_candidates(const SolveShape& s0, bool relaxed = f
 				if(s.spg % ks == 0 && solve_pair_ok(Mt, ks) && (Mt * ks <= s.cap() || ks == 1)) {
 					SolveCfg c; c.Mt = Mt; c.KSy = ks; out.push_back(c);
 					if(s.Nx > 3 && s.nw == 2) { SolveCfg t; t.Mxt = Mt; t.KSy = ks; out.push_back(t); }
+				}
+		}
+		// long y-lines as several-warps-per-line x-lines of the transposed frame
+		if(uy > 256 && uy <= 2048 && s.Nx > 3 && s.nw == 2) {
+			const int wpl = (uy + 255) / 256;
+			for(int ks : {4, 2, 1})
+				if(s.spg % ks == 0 && (8 * ks <= s.cap() || ks == 1) && xw_fits(ks, wpl, s)) {
+					SolveCfg t; t.Mxt = 8; t.WPLt = wpl; t.KSy = ks; out.push_back(t);
 				}
 		}
 		for(int ks : {4, 2, 1})

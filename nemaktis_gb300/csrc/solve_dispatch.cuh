@@ -29,7 +29,7 @@ bool launch_solve_yc(const SolveLaunch& L, Geom G, int slot0, int nch, const cx<
 	const cx<R>* ai2 = nullptr);
 template <typename R>
 bool launch_solve_xw(const SolveLaunch& L, Geom G, int slot0, int nch, const cx<R>* coef, const cx<R>* fac,
-	size_t plane, const cx<double>* lsc, const cx<R>* src, cx<R>* dst, const cx<R>* ai, cx<R>* ao);
+	size_t plane, const cx<double>* lsc, const cx<R>* src, cx<R>* dst, const cx<R>* ai, cx<R>* ao, const cx<R>* ai2 = nullptr);
 void set_solve_smem_xw_f32(int bytes);
 void set_solve_smem_xw_f64(int bytes);
 template <typename R>

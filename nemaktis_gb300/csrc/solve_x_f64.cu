@@ -66,16 +66,21 @@ void set_solve_smem_xs_f64(int bytes) {
 }
 
 #define NBPM_XW(KK, KD) \
-	if(L.M == 8 && L.KS == KK && L.kind == KD) { \
+	if(L.M == 8 && L.KS == KK && L.kind == KD && !L.tout) { \
 		k_solve_xw<double, 8, KD, KK><<<L.grid, L.block, L.smem, L.stream>>>(G, slot0, nch, coef, fac, plane, lsc, \
-			src, dst, ai, ao); \
+			src, dst, ai, ao, ai2); \
+		return true; \
+	} \
+	if(L.M == 8 && L.KS == KK && L.kind == KD && L.tout && KD == ST_WOOD_X) { \
+		k_solve_xw<double, 8, ST_WOOD_X, KK, true><<<L.grid, L.block, L.smem, L.stream>>>(G, slot0, nch, coef, fac, plane, \
+			lsc, src, dst, ai, ao, ai2); \
 		return true; \
 	}
 
 template <>
 bool launch_solve_xw<double>(const SolveLaunch& L, Geom G, int slot0, int nch, const cx<double>* coef,
 		const cx<double>* fac, size_t plane, const cx<double>* lsc, const cx<double>* src, cx<double>* dst,
-		const cx<double>* ai, cx<double>* ao) {
+		const cx<double>* ai, cx<double>* ao, const cx<double>* ai2) {
 	NBPM_XW(1, ST_EXPL_Y) NBPM_XW(2, ST_EXPL_Y) NBPM_XW(4, ST_EXPL_Y)
 	NBPM_XW(1, ST_WOOD_X) NBPM_XW(2, ST_WOOD_X) NBPM_XW(4, ST_WOOD_X)
 	return false;
@@ -85,6 +90,9 @@ void set_solve_smem_xw_f64(int bytes) {
 #define NBPM_XWA(KK, KD) cudaFuncSetAttribute(k_solve_xw<double, 8, KD, KK>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 	NBPM_XWA(1, ST_EXPL_Y) NBPM_XWA(2, ST_EXPL_Y) NBPM_XWA(4, ST_EXPL_Y)
 	NBPM_XWA(1, ST_WOOD_X) NBPM_XWA(2, ST_WOOD_X) NBPM_XWA(4, ST_WOOD_X)
+	cudaFuncSetAttribute(k_solve_xw<double, 8, ST_WOOD_X, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+	cudaFuncSetAttribute(k_solve_xw<double, 8, ST_WOOD_X, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+	cudaFuncSetAttribute(k_solve_xw<double, 8, ST_WOOD_X, 4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
 }  // namespace nbpm

@@ -34,15 +34,15 @@ MESHES = {
 def configs(js, precision):
     c = _lib.solve_candidates(js, precision)
     # every x candidate with the default y, every y candidate with the default x (the transposed-
-    # frame y solves "yx" need an "xc" x solve: paired with the first one)
+    # frame y solves "yx" need an x solve that hands the fields over, "xc" or "xw")
     dx, dy = c["default"].split(";")
-    xc = [x for x in c["x"] if x.startswith("xc:")]
+    hand = [x for x in c["x"] if x.startswith(("xc:", "xw:"))]
     out = {x + ";" + dy for x in c["x"]}
     for y in c["y"]:
         if not y.startswith("yx:"):
             out.add(dx + ";" + y)
-        elif xc:
-            out.add((dx if dx.startswith("xc:") else xc[0]) + ";" + y)
+        elif hand:
+            out.add((dx if dx.startswith(("xc:", "xw:")) else hand[0]) + ";" + y)
     return sorted(out)
 
 
