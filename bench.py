@@ -326,6 +326,7 @@ def config4_record(steps=2):
     vs = voxel_steps(samples)
     bufs = [{"json": c["json"], "lc": c["lc"], "E": np.zeros(c["shape"], np.complex128)} for c in samples]
     plan = api.Plan(bufs, precision="fp32", groups_per_pass=0)
+    tuned_cfg = [plan.solve_config(i)[0] for i in range(len(samples))]
     plan.upload()
     plan.execute()
     torch.cuda.synchronize()
@@ -333,6 +334,13 @@ def config4_record(steps=2):
     launches = plan.execute()["kernel_launches"]
     plan.download()
     plan.close()
+    # the rule-based line-solve configuration on the same batch, for the tuner's gain
+    rb = [{"json": c["json"], "lc": c["lc"], "E": np.zeros(c["shape"], np.complex128)} for c in samples]
+    with api.Plan(rb, precision="fp32", groups_per_pass=0, tune=False) as pr:
+        pr.upload()
+        pr.execute()
+        rule_ms = float(pr.execute()["compute_ms"])
+        rule_cfg = [pr.solve_config(i)[0] for i in range(len(samples))]
     # each sample alone (its own plan), for the gain of running the samples side by side
     alone_ms = []
     for c in samples:
@@ -350,6 +358,7 @@ def config4_record(steps=2):
             "value": vs * steps / (float(np.sum(ms)) / 1e3), "unit": "voxel-steps/s",
             "ms_per_step": float(np.mean(ms)), "steps": steps, "warmup": 1, "gpu_launches_per_step": launches,
             "samples_alone_ms": alone_ms, "samples_alone_sum_ms": float(np.sum(alone_ms)),
+            "line_solves": {"configs": tuned_cfg, "rule_based_configs": rule_cfg, "rule_based_ms_per_step": rule_ms},
             "e2e": e2e, "fp32_rel_l2_vs_fp64": {"sample": "512x512x96", "value": err}}
 
 

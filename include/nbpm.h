@@ -87,9 +87,10 @@ typedef struct nbpm_sample {
 	int n_E_vals;
 } nbpm_sample;
 
-/* Propagates several samples of possibly different mesh sizes in one run (each slab step
- * advances every sample that still has slabs left). Results are identical to separate
- * nbpm_run_backend_ex calls. This entry and the ones built on it (nbpm_run_backend_ex,
+/* Propagates several samples of possibly different mesh sizes in one run: every sample runs on
+ * its own streams and workspace, the samples being parallel branches of one CUDA graph, so the
+ * device interleaves their kernels (each sample keeps the line-solve configuration of its own
+ * mesh). Results are identical to separate nbpm_run_backend_ex calls. This entry and the ones built on it (nbpm_run_backend_ex,
  * nbpm_run_backend_with/without_mask) keep the device plan of a call without bulk output and
  * reuse it when the next call has the same settings, sizes, mask formula and options: its
  * device buffers and recorded CUDA graph stay, the inputs (director, mask and its z weights)

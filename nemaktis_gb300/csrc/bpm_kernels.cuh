@@ -2341,9 +2341,6 @@ __global__ void __launch_bounds__(256) k_shift_fused(Geom G, int slot0, const Sh
 	const int wx = ax ? SHT + 3 * nsh : SHT, wy = ay ? SHT + 3 * nsh : SHT;
 	cx<R> ph = mk<R>((R)P.ph_re, (R)P.ph_im);
 	if(nsh == 2) ph = ph * ph;
-	// the interpolation weights in the arithmetic type, converted once
-	const R wx0 = (R)P.wx[0], wx1 = (R)P.wx[1], wx2 = (R)P.wx[2], wx3 = (R)P.wx[3];
-	const R wy0 = (R)P.wy[0], wy1 = (R)P.wy[1], wy2 = (R)P.wy[2], wy3 = (R)P.wy[3];
 	// every tap index of both passes stays above -(N-1): mod arithmetic equals the wrap rule
 	const bool regular = (!ax || P.msx - 1 > -Px) && (!ay || P.msy - 1 > -Py);
 	if(!regular) {
@@ -2384,7 +2381,8 @@ __global__ void __launch_bounds__(256) k_shift_fused(Geom G, int slot0, const Sh
 				int t = e % ow, v = e / ow;
 				for(int c = 0; c < 2; c++) {
 					const cx<R>* in = cur + c * PW * PW + v * PW + t;
-					nxt[c * PW * PW + v * PW + t] = wx0 * in[0] + wx1 * in[1] + wx2 * in[2] + wx3 * in[3];
+					nxt[c * PW * PW + v * PW + t] = (R)P.wx[0] * in[0] + (R)P.wx[1] * in[1] + (R)P.wx[2] * in[2] +
+						(R)P.wx[3] * in[3];
 				}
 			}
 			__syncthreads();
@@ -2401,7 +2399,8 @@ __global__ void __launch_bounds__(256) k_shift_fused(Geom G, int slot0, const Sh
 				int t = e % SHT, v = e / SHT;
 				for(int c = 0; c < 2; c++) {
 					const cx<R>* in = cur + c * PW * PW + v * PW + t;
-					nxt[c * PW * PW + v * PW + t] = wy0 * in[0] + wy1 * in[PW] + wy2 * in[2 * PW] + wy3 * in[3 * PW];
+					nxt[c * PW * PW + v * PW + t] = (R)P.wy[0] * in[0] + (R)P.wy[1] * in[PW] +
+						(R)P.wy[2] * in[2 * PW] + (R)P.wy[3] * in[3 * PW];
 				}
 			}
 			__syncthreads();
