@@ -681,10 +681,15 @@ struct Plan : PlanBase {
 		select(*S[0]);
 	}
 
+	// Wavelengths per pass the tuner times with (and keys on): at most four. Beyond that every
+	// candidate's grid already fills the device many times over, the ranking does not change, and
+	// timing fewer wavelengths keeps the tuning of large plans (serving: many shapes) short.
+	int tune_groups(const SampleHost& h) const { return std::min(gpp(h), 4); }
+
 	std::string tune_key(const SampleHost& h) const {
 		char b[160];
 		std::snprintf(b, sizeof b, "%s|%dx%d|spg%d|ng%d|nw%d|sm%d", sizeof(R) == sizeof(float) ? "fp32" : "fp64", h.s.Nx,
-			h.s.Ny, h.spg, gpp(h), h.s.n_woodbury, nsm);
+			h.s.Ny, h.spg, tune_groups(h), h.s.n_woodbury, nsm);
 		return b;
 	}
 
@@ -704,7 +709,7 @@ struct Plan : PlanBase {
 	// three runs after one warm-up.
 	double time_direction(SampleHost& h, int dirn) {
 		const Geom Gm = h.geom;
-		const int ng = gpp(h), nsl = ng * h.spg;
+		const int ng = tune_groups(h), nsl = ng * h.spg;
 		cx<R>* Fp = h.F.as<cx<R>>();
 		select(h);
 		fx_cur = W->facx.as<cx<R>>(); fy_cur = W->facy.as<cx<R>>();
