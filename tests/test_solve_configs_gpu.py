@@ -116,3 +116,32 @@ def test_tuner_picks_a_candidate_and_is_reproducible(gpu):
     with api.Plan([{"json": js, "lc": lc, "E": np.zeros(shape, np.complex128)}], precision="fp32", tune=True) as p2:
         cfg2, report2 = p2.solve_config(0)
     assert cfg2 == cfg and "cached" in report2
+
+
+def test_tune_cache_file_is_reused_by_a_new_process(gpu, tmp_path):
+    """With NBPM_TUNE_CACHE set, the tuned configuration of a shape is written to the file, and a
+    later process reads it from there instead of timing the candidates again."""
+    import json
+    import os
+    import subprocess
+    import sys
+    cache = tmp_path / "tune.tsv"
+    script = (
+        "import json, numpy as np\n"
+        "from tests.helpers import case\n"
+        "from nemaktis_gb300 import api\n"
+        "js, lc, shape = case((40, 24, 5), q=((0.0, 0.0), (0.1, 0.0), (0.0, 0.1)), seed=4)\n"
+        "with api.Plan([{'json': js, 'lc': lc, 'E': np.zeros(shape, np.complex128)}], precision='fp32') as p:\n"
+        "    print(json.dumps(p.solve_config(0)))\n")
+    env = dict(os.environ, NBPM_TUNE_CACHE=str(cache))
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    runs = []
+    for _ in range(2):
+        out = subprocess.run([sys.executable, "-c", script], env=env, cwd=root, capture_output=True, text=True,
+                             timeout=600)
+        assert out.returncode == 0, out.stderr
+        runs.append(json.loads(out.stdout.strip().splitlines()[-1]))
+    assert cache.exists() and cache.read_text().count("\t") >= 2
+    (cfg1, rep1), (cfg2, rep2) = runs
+    assert "tuned" in rep1 and cfg1 == cfg2
+    assert "cached" in rep2 and "tuned" not in rep2
