@@ -115,31 +115,31 @@ class Clocks:
 
 def workload(name):
     from nemaktis_gb300 import workloads as W
-    if name == "config3":
-        c = W.config3()
+    if name == "koehler":
+        c = W.koehler_micrograph()
         c["desc"] = "batched Koehler micrograph 256x256x64 d=0.25um, 16 wavelengths x 13 q x 2 pol (416 propagations)"
         c["Nz"] = 64
         return [c]
-    if name == "config3s":
-        c = W.config3(dims=(256, 256, 8), n_wavelengths=8)
+    if name == "koehler_small":
+        c = W.koehler_micrograph(dims=(256, 256, 8), n_wavelengths=8)
         c["desc"] = "reduced batched Koehler case for profiling: 256x256x8, 8 wavelengths x 13 q x 2 pol"
         c["Nz"] = 8
         return [c]
-    if name == "config1":
-        c = W.config1()
+    if name == "tn":
+        c = W.twisted_nematic_cell()
         c["desc"] = "twisted nematic 64x64x40 d=0.25um, 1 wavelength x 1 q x 2 pol"
         c["Nz"] = 40
         return [c]
-    if name == "config2":
-        c = W.config2()
+    if name == "droplet":
+        c = W.droplet_cell()
         c["desc"] = "cholesteric droplet 512x512x128 d=0.2um (mask + formula), 1 wavelength x 1 q x 2 pol"
         c["Nz"] = 128
         return [c]
-    if name == "config4":
+    if name == "uneven":
         out = []
         for i in range(4):
-            c = W.config4_sample(i)
-            c["Nz"] = W.CONFIG4_MESHES[i][2]
+            c = W.uneven_sample(i)
+            c["Nz"] = W.UNEVEN_MESHES[i][2]
             out.append(c)
         out[0]["desc"] = "4 uneven samples 1024^2x200, 768^2x160, 512^2x96, 256^2x48 d=0.2um, 4 wl x 7 q x 2 pol"
         return out
@@ -270,11 +270,11 @@ def run_ours(args):
     PROF = "profiles/solve_xc_koehler_256x256x8_fp32.md"
     PSF = "profiles/shift_fused_koehler_256x256x8_fp32.md"
     W = 2 * (319.3e6 + 184.3e6 + 562.6e6 + 197.7e6) / 2  # mean of the two Woodbury launches, x2 slots
-    TRAFFIC = {("config3", "fp32", "wood_solve_x"): (W, PROF),
-               ("config3", "fp32", "wood_solve_y"): (W, PROF + " (the same kernel in the transposed frame)"),
-               ("config3", "fp32", "expl_solve_x"): (2 * (344.6e6 + 188.5e6), PROF),
-               ("config3", "fp32", "expl_solve_y"): (2 * (344.6e6 + 188.5e6), PROF + " (the same kernel in the transposed frame)"),
-               ("config3", "fp32", "shift_fused"): (2 * (242.5e6 + 189.5e6), PSF)}
+    TRAFFIC = {("koehler", "fp32", "wood_solve_x"): (W, PROF),
+               ("koehler", "fp32", "wood_solve_y"): (W, PROF + " (the same kernel in the transposed frame)"),
+               ("koehler", "fp32", "expl_solve_x"): (2 * (344.6e6 + 188.5e6), PROF),
+               ("koehler", "fp32", "expl_solve_y"): (2 * (344.6e6 + 188.5e6), PROF + " (the same kernel in the transposed frame)"),
+               ("koehler", "fp32", "shift_fused"): (2 * (242.5e6 + 189.5e6), PSF)}
     roof = None
     if prof:
         top = max(prof, key=lambda k: prof[k]["ms"])
@@ -289,9 +289,9 @@ def run_ours(args):
     peaks_meas = None
     if not args.only_value:
         peaks_meas = fma_peaks()
-    c4 = None
-    if rank == 0 and args.workload == "config3" and not args.skip_config4:
-        c4 = config4_record()
+    unev = None
+    if rank == 0 and args.workload == "koehler" and not args.skip_uneven:
+        unev = uneven_batch_record()
     cpu = None
     if rank == 0 and not args.skip_cpu:
         cpu = cpu_baseline(samples, args.cpu_seconds)
@@ -307,14 +307,14 @@ def run_ours(args):
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "clocks": clocks, "gpu_launches": launches, "wall_s": wall,
         "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "fp64_plain": fp64, "fma_peaks_measured": peaks_meas,
-        "config4": c4, "line_solves": tuning,
+        "uneven": unev, "line_solves": tuning,
         "kernel_profile": {k: {"ms_per_step": v["ms"], "launches_per_step": v["launches"]} for k, v in (prof or {}).items()},
     }
     if rank == 0:
         print(json.dumps(line))
 
 
-def config4_record(steps=2):
+def uneven_batch_record(steps=2):
     """Sub-record for the largest single-GPU configuration (four uneven samples 1024^2x200,
     768^2x160, 512^2x96, 256^2x48, FP32 batched, one plan): device-resident value over `steps`
     timed executions after one warm-up, e2e through nbpm_run_batch with pinned host buffers (one
@@ -322,7 +322,7 @@ def config4_record(steps=2):
     an FP64 plain run of that sample alone."""
     import torch
     from nemaktis_gb300 import api
-    samples = workload("config4")
+    samples = workload("uneven")
     vs = voxel_steps(samples)
     bufs = [{"json": c["json"], "lc": c["lc"], "E": np.zeros(c["shape"], np.complex128)} for c in samples]
     plan = api.Plan(bufs, precision="fp32", groups_per_pass=0)
@@ -667,13 +667,13 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="config3", choices=["config1", "config2", "config3", "config3s", "config4", "serve"])
+    ap.add_argument("--workload", default="koehler", choices=["tn", "droplet", "koehler", "koehler_small", "uneven", "serve"])
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
-    ap.add_argument("--skip-config4", action="store_true", help="no config-4 sub-record in the default line")
+    ap.add_argument("--skip-uneven", action="store_true", help="no four-sample (uneven batch) sub-record in the default line")
     ap.add_argument("--no-tune", action="store_true", help="rule-based line-solve configuration (no timing runs)")
     ap.add_argument("--solve-config", default=None, help='force a line-solve configuration "<x>;<y>"')
     ap.add_argument("--only-value", action="store_true", help="time the device-resident run only")

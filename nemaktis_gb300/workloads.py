@@ -84,7 +84,7 @@ def _smooth(a, sigma_vox, axes):
 
 
 def twisted_nematic(dims=(64, 64, 40), d=0.25, tilt_sigma=0.05, corr_len=1.0, seed=0):
-    """Config 1 director: n = (cos phi cos t, sin phi cos t, sin t), phi = pi/2*z/L, t smoothed noise."""
+    """Twisted-nematic director: n = (cos phi cos t, sin phi cos t, sin t), phi = pi/2*z/L, t smoothed noise."""
     Nx, Ny, Nz = dims
     rng = np.random.default_rng(seed)
     L = d * (Nz - 1) if Nz > 1 else 1.0
@@ -99,7 +99,7 @@ def twisted_nematic(dims=(64, 64, 40), d=0.25, tilt_sigma=0.05, corr_len=1.0, se
 
 
 def cholesteric_droplet(dims=(512, 512, 128), d=0.2, radius=40.0, pitch=5.0):
-    """Config 2 director + mask: radial r^ rotated by 2*pi*|r|/p about the azimuthal axis z x r^."""
+    """Cholesteric-droplet director + mask: radial r^ rotated by 2*pi*|r|/p about the azimuthal axis z x r^."""
     Nx, Ny, Nz = dims
     x = (np.arange(Nx) - 0.5 * (Nx - 1)) * d
     y = (np.arange(Ny) - 0.5 * (Ny - 1)) * d
@@ -121,7 +121,7 @@ def cholesteric_droplet(dims=(512, 512, 128), d=0.2, radius=40.0, pitch=5.0):
 
 
 def point_defects(dims=(256, 256, 64), d=0.25, n_defects=8, smooth_len=1.0, seed=0):
-    """Config 3 director: in-plane angle sum_k s_k atan2(y-y_k, x-x_k), s_k = +-1/2."""
+    """Point-defect director: in-plane angle sum_k s_k atan2(y-y_k, x-x_k), s_k = +-1/2."""
     Nx, Ny, Nz = dims
     rng = np.random.default_rng(seed)
     x = (np.arange(Nx) - 0.5 * (Nx - 1)) * d
@@ -142,7 +142,7 @@ def point_defects(dims=(256, 256, 64), d=0.25, n_defects=8, smooth_len=1.0, seed
 
 
 def random_smooth(dims, d=0.2, corr_len=2.0, seed=0, dtype=np.float64):
-    """Config 4 director: seeded random unit vectors, Gaussian-filtered, normalised."""
+    """Random smooth director: seeded random unit vectors, Gaussian-filtered, normalised."""
     Nx, Ny, Nz = dims
     rng = np.random.default_rng(seed)
     n = rng.normal(size=(Nz, Ny, Nx, 3)).astype(np.float32)
@@ -153,24 +153,24 @@ def random_smooth(dims, d=0.2, corr_len=2.0, seed=0, dtype=np.float64):
     return np.ascontiguousarray(n)
 
 
-CONFIG3_WAVELENGTHS = list(np.linspace(0.40, 0.80, 16))
-CONFIG4_WAVELENGTHS = [0.45, 0.55, 0.65, 0.75]
-CONFIG4_MESHES = [(1024, 1024, 200), (768, 768, 160), (512, 512, 96), (256, 256, 48)]
+KOEHLER_WAVELENGTHS = list(np.linspace(0.40, 0.80, 16))
+UNEVEN_WAVELENGTHS = [0.45, 0.55, 0.65, 0.75]
+UNEVEN_MESHES = [(1024, 1024, 200), (768, 768, 160), (512, 512, 96), (256, 256, 48)]
 
 
-def config1(seed=0, dims=(64, 64, 40)):
+def twisted_nematic_cell(seed=0, dims=(64, 64, 40)):
     lc = twisted_nematic(dims=dims, seed=seed)
     js = settings_json(dims, (0.25, 0.25, 0.25), [0.6], (0.0, 0.0), no="1.5", ne="1.7", nhost="1.5", NA=1.0)
     return {"json": js, "lc": lc, "shape": (1, 1, 4, dims[1], dims[0])}
 
 
-def config2(dims=(512, 512, 128)):
+def droplet_cell(dims=(512, 512, 128)):
     lc, mask, formula = cholesteric_droplet(dims=dims)
     js = settings_json(dims, (0.2, 0.2, 0.2), [0.55], (0.0, 0.0), no="1.5", ne="1.7", nhost="1.55", NA=1.0)
     return {"json": js, "lc": lc, "mask": mask, "formula": formula, "shape": (1, 1, 4, dims[1], dims[0])}
 
 
-def config3(seed=0, dims=(256, 256, 64), n_wavelengths=16):
+def koehler_micrograph(seed=0, dims=(256, 256, 64), n_wavelengths=16):
     lc = point_defects(dims=dims, seed=seed)
     wl = list(np.linspace(0.40, 0.80, n_wavelengths))
     q = hex_lattice_13(0.1)
@@ -179,11 +179,11 @@ def config3(seed=0, dims=(256, 256, 64), n_wavelengths=16):
     return {"json": js, "lc": lc, "shape": (len(wl), len(q), 4, dims[1], dims[0])}
 
 
-def config4_sample(i, seed=0):
-    dims = CONFIG4_MESHES[i]
+def uneven_sample(i, seed=0):
+    dims = UNEVEN_MESHES[i]
     lc = random_smooth(dims, d=0.2, corr_len=2.0, seed=seed + i)
     q = hex_wavevectors(2, 0.15)
-    js = settings_json(dims, (0.2, 0.2, 0.2), CONFIG4_WAVELENGTHS, q, no="1.5", ne="1.75", nhost="1.5", NA=0.4)
+    js = settings_json(dims, (0.2, 0.2, 0.2), UNEVEN_WAVELENGTHS, q, no="1.5", ne="1.75", nhost="1.5", NA=0.4)
     return {"json": js, "lc": lc, "shape": (4, len(q), 4, dims[1], dims[0])}
 
 

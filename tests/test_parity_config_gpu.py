@@ -28,7 +28,7 @@ def _oracle(js, lc, shape, mask=None, formula=None):
 
 
 def droplet_case(dims=(128, 128, 32), d=0.2, radius=10.0, q=((0.0, 0.0), (0.08, -0.05))):
-    """Config 2 scaled down: cholesteric droplet (pitch 5 um) of radius 10 um in a 25.6 um box,
+    """The 512x512x128 droplet workload scaled down: cholesteric droplet (pitch 5 um) of radius 10 um in a 25.6 um box,
     nhost 1.55, mask formula r^2 - x^2 - y^2 - z^2, one normal and one tilted wave vector."""
     lc, mask, formula = workloads.cholesteric_droplet(dims=dims, d=d, radius=radius)
     js = workloads.settings_json(dims, (d, d, d), [0.55], np.asarray(q, float), no="1.5", ne="1.7",
@@ -45,9 +45,9 @@ def test_droplet_128_mask_formula_fp64(gpu):
 
 
 def koehler_case(Nz=8, n_wavelengths=2):
-    """Config 3 with its 256x256 planes, its 13-point hexagonal q grid and 2 polarisations
+    """The Koehler micrograph workload with its 256x256 planes, its 13-point hexagonal q grid and 2 polarisations
     (26 slots per wavelength, as in production), fewer wavelengths and planes."""
-    c = workloads.config3(dims=(256, 256, Nz), n_wavelengths=n_wavelengths)
+    c = workloads.koehler_micrograph(dims=(256, 256, Nz), n_wavelengths=n_wavelengths)
     return c["json"], c["lc"], c["shape"]
 
 
@@ -70,16 +70,16 @@ def _fp32_vs_fp64(samples, k=0):
     return rel_l2(bufs[k]["E"], e64)
 
 
-def test_config2_fp32_error_budget(gpu):
-    assert _fp32_vs_fp64([workloads.config2()]) <= FP32_TOL
+def test_droplet_fp32_error_budget(gpu):
+    assert _fp32_vs_fp64([workloads.droplet_cell()]) <= FP32_TOL
 
 
-def test_config3_fp32_error_budget(gpu):
-    assert _fp32_vs_fp64([workloads.config3()]) <= FP32_TOL
+def test_koehler_fp32_error_budget(gpu):
+    assert _fp32_vs_fp64([workloads.koehler_micrograph()]) <= FP32_TOL
 
 
-def test_config4_sample_fp32_error_budget(gpu):
+def test_uneven_sample_fp32_error_budget(gpu):
     """The 512x512x96 sample of the uneven workload, run in FP32 in one batch with the 256x256x48
     sample (uneven sizes in one plan), against its FP64 plain run."""
-    samples = [workloads.config4_sample(2), workloads.config4_sample(3)]
+    samples = [workloads.uneven_sample(2), workloads.uneven_sample(3)]
     assert _fp32_vs_fp64(samples, 0) <= FP32_TOL

@@ -98,8 +98,8 @@ def test_fp64_parity_beam_none(gpu):
     assert rel_l2(out, ref) <= FP64_TOL
 
 
-def test_config1_fp64_parity(gpu):
-    c = workloads.config1()
+def test_twisted_nematic_fp64_parity(gpu):
+    c = workloads.twisted_nematic_cell()
     out, ref = _both(c["json"], c["lc"], c["shape"])
     assert rel_l2(out, ref) <= FP64_TOL
 
@@ -130,8 +130,8 @@ def test_fp32_error_budget(gpu, name):
     assert rel_l2(e32, e64) <= FP32_TOL
 
 
-def test_config1_fp32_error_budget(gpu):
-    c = workloads.config1()
+def test_twisted_nematic_fp32_error_budget(gpu):
+    c = workloads.twisted_nematic_cell()
     e64 = np.zeros(c["shape"], np.complex128)
     e32 = np.zeros(c["shape"], np.complex128)
     api.run(c["json"], c["lc"], e64, precision="fp64")

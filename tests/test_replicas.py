@@ -61,5 +61,5 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch, capsys):
     monkeypatch.setenv("WORLD_SIZE", "2")
     monkeypatch.setenv("RANK", "1")
     monkeypatch.setenv("LOCAL_RANK", "1")
-    bench.run_reference(argparse.Namespace(workload="config1", steps=1, warmup=0, cpu_seconds=0.1))
+    bench.run_reference(argparse.Namespace(workload="tn", steps=1, warmup=0, cpu_seconds=0.1))
     assert capsys.readouterr().out == ""

@@ -77,7 +77,7 @@ def test_koehler_shape_fp32_candidates(gpu):
     candidate within 1e-4 of FP64, and the FP64 run of the configuration FP32 production uses
     matches the oracle."""
     from nemaktis_gb300 import workloads
-    c = workloads.config3(dims=(256, 256, 4), n_wavelengths=2)
+    c = workloads.koehler_micrograph(dims=(256, 256, 4), n_wavelengths=2)
     js, lc, shape = c["json"], c["lc"], c["shape"]
     e64 = np.zeros(shape, np.complex128)
     api.run(js, lc, e64, precision="fp64")
