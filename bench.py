@@ -222,7 +222,8 @@ def run_ours(args):
             print(json.dumps({"metric": "voxel-steps/s", "value": value, "unit": "voxel-steps/s", "steps": args.steps,
                               "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
                               "config": {"workload": samples[0]["desc"], "precision": prec,
-                                         "line_solves": [c for c, _ in solve_cfg]},
+                                         "line_solves": [c for c, _ in solve_cfg],
+                                         "tuning": [r for _, r in solve_cfg]},
                               "gpu_launches": launches, "clocks": clocks}))
         return
     prof = profile_kernels(plan, lib)

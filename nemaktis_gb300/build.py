@@ -16,7 +16,7 @@ LIB = os.path.join(BUILD, "libnbpm.so")
 SOURCES = ["nbpm.cu", "solve_x_f32.cu", "solve_x_f64.cu", "solve_y_f32.cu", "solve_y_f64.cu", "linesolve.cu",
            "linesolve_noalloc.cu", "micrograph.cu", "serve.cu"]
 HEADERS = ["bpm_kernels.cuh", "fft_kernels.cuh", "cplx.cuh", "host_settings.h", "host_expr.h", "host_json.h",
-           "solve_dispatch.cuh", "plan_iface.h", "vti_writer.h"]
+           "solve_dispatch.cuh", "solve_config.h", "plan_iface.h", "vti_writer.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 BENCH_SRC = os.path.join(HERE, "..", "bench_peaks.cu")
 BENCH_LIB = os.path.join(BUILD, "libnbpm_bench.so")

@@ -477,7 +477,7 @@ struct Stencil {
 #pragma unroll
 		for(int j = 0; j < KS; j++) {
 			const cx<R>* f = s + j * ss;
-			out[j] += c0 * f[mx + Nx * y] + c1 * f[p] + c2 * f[px + Nx * y];
+			out[j] = cfma(c2, f[px + Nx * y], cfma(c1, f[p], cfma(c0, f[mx + Nx * y], out[j])));
 		}
 	}
 	template <int KS>
@@ -489,7 +489,7 @@ struct Stencil {
 #pragma unroll
 		for(int j = 0; j < KS; j++) {
 			const cx<R>* f = s + j * ss;
-			out[j] += c0 * f[x + Nx * my] + c1 * f[p] + c2 * f[x + Nx * py];
+			out[j] = cfma(c2, f[x + Nx * py], cfma(c1, f[p], cfma(c0, f[x + Nx * my], out[j])));
 		}
 	}
 	template <int KS>
@@ -502,7 +502,7 @@ struct Stencil {
 #pragma unroll
 		for(int j = 0; j < KS; j++) {
 			const cx<R>* f = s + j * ss;
-			out[j] += c0 * f[px + Nx * py] + c1 * f[mx + Nx * py] + c2 * f[px + Nx * my] + c3 * f[mx + Nx * my];
+			out[j] = cfma(c3, f[mx + Nx * my], cfma(c2, f[px + Nx * my], cfma(c1, f[mx + Nx * py], cfma(c0, f[px + Nx * py], out[j]))));
 		}
 	}
 };
@@ -1001,7 +1001,7 @@ __global__ void __launch_bounds__(DIRN == 1 ? 512 : 256) k_factor_chunked(Geom G
 			if(i == 0) { cr = mk<T>(-0.5, 0); wv = one; }
 			else {
 				cx<T> gm = -cvt<T>(Fc[F_C * plane + Q(i - 1)]);  // gamma_{i-1}
-				cr = alpha * cr + (i == n - 1 ? sup(i) * rb : zero);
+				cr = cfma(alpha, cr, (i == n - 1 ? sup(i) * rb : zero));
 				wv = -(gm * wv);
 			}
 			Fc[F_COR * plane + Q(i)] = cvt<S>(cr);  // forward corr, replaced below
@@ -1101,7 +1101,7 @@ __device__ __forceinline__ void line_combine(cx<R> P, const cx<R>* d0, const cx<
 #pragma unroll
 		for(int j = 0; j < KS; j++) {
 			const cx<R> Bp = shfl_up_c(B[j], o);
-			if(lane >= o) B[j] = P * Bp + B[j];
+			if(lane >= o) B[j] = cfma(P, Bp, B[j]);
 		}
 		if(lane >= o) P = P * Pp;
 	}
@@ -1111,12 +1111,12 @@ __device__ __forceinline__ void line_combine(cx<R> P, const cx<R>* d0, const cx<
 	for(int j = 0; j < KS; j++) {
 		din[j] = shfl_up_c(B[j], 1);
 		if(lane == 0) din[j] = zero;
-		cx<R> t = S0[j] + S1 * din[j];
+		cx<R> t = cfma(S1, din[j], S0[j]);
 #pragma unroll
 		for(int o = 16; o > 0; o >>= 1) t += shfl_xor_c(t, o);
 		const cx<R> dl = shfl_idx_c(B[j], 31);
 		if(lane == j) { tsel = t; dsel = dl; }
-		G[j] = G0[j] + G1 * din[j];
+		G[j] = cfma(G1, din[j], G0[j]);
 	}
 	// the FP64 factor once per slot (lane j), then broadcast
 	cx<R> f = zero;
@@ -1129,7 +1129,7 @@ __device__ __forceinline__ void line_combine(cx<R> P, const cx<R>* d0, const cx<
 #pragma unroll
 		for(int j = 0; j < KS; j++) {
 			const cx<R> Gn = shfl_down_c(G[j], o);
-			if(lane + o < 32) G[j] = Cp * Gn + G[j];
+			if(lane + o < 32) G[j] = cfma(Cp, Gn, G[j]);
 		}
 		if(lane + o < 32) Cp = Cp * Cn;
 	}
@@ -1214,15 +1214,15 @@ __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_xc(Geom G, 
 			const cx<R> a = Fc[F_A * plane + k * 32 + lane], rb = Fc[F_RB * plane + k * 32 + lane];
 			const cx<R> w = Fc[F_W * plane + k * 32 + lane], cc = Fc[F_C * plane + k * 32 + lane];
 			P = a * P;
-			S1 += w * P;
-			G1 += Cp * P;
+			S1 = cfma(w, P, S1);
+			G1 = cfma(Cp, P, G1);
 #pragma unroll
 			for(int j = 0; j < KS; j++) {
 				const cx<R> b = vb[j * PITCH + k] * rb;
 				vb[j * PITCH + k] = b;
-				d0[j] = a * d0[j] + b;
-				S0[j] += w * d0[j];
-				G0[j] += Cp * d0[j];
+				d0[j] = cfma(a, d0[j], b);
+				S0[j] = cfma(w, d0[j], S0[j]);
+				G0[j] = cfma(Cp, d0[j], G0[j]);
 			}
 			Cp = Cp * cc;
 		}
@@ -1237,7 +1237,7 @@ __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_xc(Geom G, 
 		if(i0 + k < n_unk) {
 			const cx<R> a = Fc[F_A * plane + k * 32 + lane];
 #pragma unroll
-			for(int j = 0; j < KS; j++) { din[j] = a * din[j] + vb[j * PITCH + k]; vb[j * PITCH + k] = din[j]; }
+			for(int j = 0; j < KS; j++) { din[j] = cfma(a, din[j], vb[j * PITCH + k]); vb[j * PITCH + k] = din[j]; }
 		}
 	}
 #pragma unroll
@@ -1246,8 +1246,8 @@ __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_xc(Geom G, 
 			const cx<R> cc = Fc[F_C * plane + k * 32 + lane], cr = Fc[F_COR * plane + k * 32 + lane];
 #pragma unroll
 			for(int j = 0; j < KS; j++) {
-				xin[j] = cc * xin[j] + vb[j * PITCH + k];
-				vb[j * PITCH + k] = xin[j] - fr[j] * cr;
+				xin[j] = cfma(cc, xin[j], vb[j * PITCH + k]);
+				vb[j * PITCH + k] = cfnma(fr[j], cr, xin[j]);
 			}
 		}
 	}
@@ -1352,15 +1352,15 @@ __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_yt(Geom G, 
 				const cx<R> a = Fc[F_A * plane + q], rb = Fc[F_RB * plane + q];
 				const cx<R> w = Fc[F_W * plane + q], cc = Fc[F_C * plane + q];
 				P = a * P;
-				S1 += w * P;
-				G1 += Cp * P;
+				S1 = cfma(w, P, S1);
+				G1 = cfma(Cp, P, G1);
 #pragma unroll
 				for(int j = 0; j < KS; j++) {
 					const cx<R> b = vb[j * PITCH + k] * rb;
 					vb[j * PITCH + k] = b;
-					d0[j] = a * d0[j] + b;
-					S0[j] += w * d0[j];
-					G0[j] += Cp * d0[j];
+					d0[j] = cfma(a, d0[j], b);
+					S0[j] = cfma(w, d0[j], S0[j]);
+					G0[j] = cfma(Cp, d0[j], G0[j]);
 				}
 				Cp = Cp * cc;
 			}
@@ -1372,7 +1372,7 @@ __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_yt(Geom G, 
 			if(i0 + k < n_unk) {
 				const cx<R> a = Fc[F_A * plane + (size_t)(i0 + k) * Nx];
 #pragma unroll
-				for(int j = 0; j < KS; j++) { din[j] = a * din[j] + vb[j * PITCH + k]; vb[j * PITCH + k] = din[j]; }
+				for(int j = 0; j < KS; j++) { din[j] = cfma(a, din[j], vb[j * PITCH + k]); vb[j * PITCH + k] = din[j]; }
 			}
 		}
 #pragma unroll
@@ -1382,8 +1382,8 @@ __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_yt(Geom G, 
 				const cx<R> cc = Fc[F_C * plane + q], cr = Fc[F_COR * plane + q];
 #pragma unroll
 				for(int j = 0; j < KS; j++) {
-					xin[j] = cc * xin[j] + vb[j * PITCH + k];
-					vb[j * PITCH + k] = xin[j] - fr[j] * cr;
+					xin[j] = cfma(cc, xin[j], vb[j * PITCH + k]);
+					vb[j * PITCH + k] = cfnma(fr[j], cr, xin[j]);
 				}
 			}
 		}
@@ -1508,15 +1508,15 @@ __global__ void __launch_bounds__(MAXT, NBPM_YC_MINB) k_solve_yc(Geom G, int slo
 			cx<R> r[KS];
 			composite_m<R, KIND, KS>(st, c, ix, i, f0, r);
 			P = a * P;
-			S1 += wv * P;
-			G1 += Cp * P;
+			S1 = cfma(wv, P, S1);
+			G1 = cfma(Cp, P, G1);
 #pragma unroll
 			for(int j = 0; j < KS; j++) {
 				const cx<R> b = r[j] * rb;
 				V(j, k) = b;
-				d0[j] = a * d0[j] + b;
-				S0[j] += wv * d0[j];
-				G0[j] += Cp * d0[j];
+				d0[j] = cfma(a, d0[j], b);
+				S0[j] = cfma(wv, d0[j], S0[j]);
+				G0[j] = cfma(Cp, d0[j], G0[j]);
 			}
 			Cp = Cp * cc;
 		}
@@ -1545,7 +1545,7 @@ __global__ void __launch_bounds__(MAXT, NBPM_YC_MINB) k_solve_yc(Geom G, int slo
 		if(i < n_unk) {
 			const cx<R> a = Fc[F_A * plane + (size_t)ix + (size_t)Nx * i];
 #pragma unroll
-			for(int j = 0; j < KS; j++) { d[j] = a * d[j] + V(j, k); V(j, k) = d[j]; }
+			for(int j = 0; j < KS; j++) { d[j] = cfma(a, d[j], V(j, k)); V(j, k) = d[j]; }
 		}
 	}
 #pragma unroll
@@ -1556,8 +1556,8 @@ __global__ void __launch_bounds__(MAXT, NBPM_YC_MINB) k_solve_yc(Geom G, int slo
 			const cx<R> cc = Fc[F_C * plane + q], cr = Fc[F_COR * plane + q];
 #pragma unroll
 			for(int j = 0; j < KS; j++) {
-				x[j] = cc * x[j] + V(j, k);
-				const cx<R> y = x[j] - fr[j] * cr;
+				x[j] = cfma(cc, x[j], V(j, k));
+				const cx<R> y = cfnma(fr[j], cr, x[j]);
 				const size_t off = (size_t)(s0 + j) * 2 * N + (size_t)c * N;
 				if(dst) dst[off + q] = y;
 				// the explicit-step solves never accumulate
@@ -1620,10 +1620,10 @@ __global__ void __launch_bounds__(128) k_solve_yq(Geom G, int nch, const cx<R>* 
 #pragma unroll
 		for(int j = 0; j < KS; j++) {
 			const cx<R> b0 = r0[j] * B0, b1 = r1[j] * B1;
-			d0[j] = A0 * d0[j] + b0;
-			d1[j] = A1 * d1[j] + b1;
-			a0[j] += W0 * d0[j];
-			a1[j] += W1 * d1[j];
+			d0[j] = cfma(A0, d0[j], b0);
+			d1[j] = cfma(A1, d1[j], b1);
+			a0[j] = cfma(W0, d0[j], a0[j]);
+			a1[j] = cfma(W1, d1[j], a1[j]);
 			sc[j * ss + q] = d0[j];
 			sc[j * ss + N + q] = d1[j];
 		}
@@ -1648,8 +1648,8 @@ __global__ void __launch_bounds__(128) k_solve_yq(Geom G, int nch, const cx<R>* 
 #pragma unroll
 		for(int j = 0; j < KS; j++) {
 			const size_t o0 = (size_t)(s0 + j) * ss + q, o1 = o0 + N;
-			x0[j] = C0 * x0[j] + sc[j * ss + q];
-			x1[j] = C1 * x1[j] + sc[j * ss + N + q];
+			x0[j] = cfma(C0, x0[j], sc[j * ss + q]);
+			x1[j] = cfma(C1, x1[j], sc[j * ss + N + q]);
 			const cx<R> y0 = x0[j] - fr0[j] * K0, y1 = x1[j] - fr1[j] * K1;
 			if(dst) { dst[o0] = y0; dst[o1] = y1; }
 			if(KIND != ST_EXPL_X && acc_out) {
@@ -1727,7 +1727,7 @@ __global__ void __launch_bounds__(256) k_solve_xw(Geom G, int slot0, int nch, co
 			if(ok) {
 				cx<R> b = buf[j * PITCH + ci * (M + 1) + k] * rb;
 				v[j][k] = b;
-				B[j] = a * B[j] + b;
+				B[j] = cfma(a, B[j], b);
 				A[j] = a * A[j];
 			}
 		}
@@ -1769,9 +1769,9 @@ __global__ void __launch_bounds__(256) k_solve_xw(Geom G, int slot0, int nch, co
 			cx<R> a = Fc[F_A * plane + k * CH + ci], w = Fc[F_W * plane + k * CH + ci];
 #pragma unroll
 			for(int j = 0; j < KS; j++) {
-				d[j] = a * d[j] + v[j][k];
+				d[j] = cfma(a, d[j], v[j][k]);
 				v[j][k] = d[j];
-				acc[j] += w * d[j];
+				acc[j] = cfma(w, d[j], acc[j]);
 			}
 			if(i0 + k == last) {
 #pragma unroll
@@ -1800,7 +1800,7 @@ __global__ void __launch_bounds__(256) k_solve_xw(Geom G, int slot0, int nch, co
 		if(i0 + k < n_unk) {
 			cx<R> cc = Fc[F_C * plane + k * CH + ci];
 #pragma unroll
-			for(int j = 0; j < KS; j++) { B[j] = cc * B[j] + v[j][k]; A[j] = cc * A[j]; }
+			for(int j = 0; j < KS; j++) { B[j] = cfma(cc, B[j], v[j][k]); A[j] = cc * A[j]; }
 		}
 	}
 #pragma unroll
@@ -1840,8 +1840,8 @@ __global__ void __launch_bounds__(256) k_solve_xw(Geom G, int slot0, int nch, co
 			cx<R> cc = Fc[F_C * plane + k * CH + ci], cr = Fc[F_COR * plane + k * CH + ci];
 #pragma unroll
 			for(int j = 0; j < KS; j++) {
-				d[j] = cc * d[j] + v[j][k];
-				buf[j * PITCH + ci * (M + 1) + k] = d[j] - fr[j] * cr;
+				d[j] = cfma(cc, d[j], v[j][k]);
+				buf[j * PITCH + ci * (M + 1) + k] = cfnma(fr[j], cr, d[j]);
 			}
 		}
 	}
@@ -1904,7 +1904,7 @@ __global__ void __launch_bounds__(128) k_solve_xs(Geom G, int slot0, int nch, in
 			for(int j = 0; j < KS; j++) {
 				cx<R> b = V(j, k) * rb;
 				V(j, k) = b;
-				B[j] = a * B[j] + b;
+				B[j] = cfma(a, B[j], b);
 				A[j] = a * A[j];
 			}
 		}
@@ -1930,9 +1930,9 @@ __global__ void __launch_bounds__(128) k_solve_xs(Geom G, int slot0, int nch, in
 			cx<R> a = Fc[F_A * plane + k * 32 + lane], w = Fc[F_W * plane + k * 32 + lane];
 #pragma unroll
 			for(int j = 0; j < KS; j++) {
-				d[j] = a * d[j] + V(j, k);
+				d[j] = cfma(a, d[j], V(j, k));
 				V(j, k) = d[j];
-				acc[j] += w * d[j];
+				acc[j] = cfma(w, d[j], acc[j]);
 			}
 		}
 		if(k == k_last) {
@@ -1954,7 +1954,7 @@ __global__ void __launch_bounds__(128) k_solve_xs(Geom G, int slot0, int nch, in
 		if(i0 + k < n_unk) {
 			cx<R> cc = Fc[F_C * plane + k * 32 + lane];
 #pragma unroll
-			for(int j = 0; j < KS; j++) { B[j] = cc * B[j] + V(j, k); A[j] = cc * A[j]; }
+			for(int j = 0; j < KS; j++) { B[j] = cfma(cc, B[j], V(j, k)); A[j] = cc * A[j]; }
 		}
 	}
 #pragma unroll
@@ -1975,8 +1975,8 @@ __global__ void __launch_bounds__(128) k_solve_xs(Geom G, int slot0, int nch, in
 			cx<R> cc = Fc[F_C * plane + k * 32 + lane], cr = Fc[F_COR * plane + k * 32 + lane];
 #pragma unroll
 			for(int j = 0; j < KS; j++) {
-				d[j] = cc * d[j] + V(j, k);
-				V(j, k) = d[j] - fr[j] * cr;
+				d[j] = cfma(cc, d[j], V(j, k));
+				V(j, k) = cfnma(fr[j], cr, d[j]);
 			}
 		}
 	}
@@ -2044,7 +2044,7 @@ __global__ void __launch_bounds__(256) k_solve_ys(Geom G, int slot0, int nch, co
 			for(int j = 0; j < KS; j++) {
 				cx<R> b = r[j] * rb;
 				vbuf[va(j, i)] = b;
-				B[j] = a * B[j] + b;
+				B[j] = cfma(a, B[j], b);
 				A[j] = a * A[j];
 			}
 		}
@@ -2071,9 +2071,9 @@ __global__ void __launch_bounds__(256) k_solve_ys(Geom G, int slot0, int nch, co
 			cx<R> a = Fc[F_A * plane + q], wv = Fc[F_W * plane + q];
 #pragma unroll
 			for(int j = 0; j < KS; j++) {
-				d[j] = a * d[j] + vbuf[va(j, i)];
+				d[j] = cfma(a, d[j], vbuf[va(j, i)]);
 				vbuf[va(j, i)] = d[j];
-				acc[j] += wv * d[j];
+				acc[j] = cfma(wv, d[j], acc[j]);
 				if(i == n_unk - 1) sL[j * 32 + lane] = d[j];
 			}
 		}
@@ -2094,7 +2094,7 @@ __global__ void __launch_bounds__(256) k_solve_ys(Geom G, int slot0, int nch, co
 		for(int i = i1 - 1; i >= i0; i--) {
 			cx<R> cc = Fc[F_C * plane + (size_t)ix + (size_t)Nx * i];
 #pragma unroll
-			for(int j = 0; j < KS; j++) { B[j] = cc * B[j] + vbuf[va(j, i)]; A[j] = cc * A[j]; }
+			for(int j = 0; j < KS; j++) { B[j] = cfma(cc, B[j], vbuf[va(j, i)]); A[j] = cc * A[j]; }
 		}
 	}
 #pragma unroll
@@ -2119,8 +2119,8 @@ __global__ void __launch_bounds__(256) k_solve_ys(Geom G, int slot0, int nch, co
 			cx<R> cc = Fc[F_C * plane + q], cr = Fc[F_COR * plane + q];
 #pragma unroll
 			for(int j = 0; j < KS; j++) {
-				d[j] = cc * d[j] + vbuf[va(j, i)];
-				cx<R> x = d[j] - fr[j] * cr;
+				d[j] = cfma(cc, d[j], vbuf[va(j, i)]);
+				cx<R> x = cfnma(fr[j], cr, d[j]);
 				size_t off = (size_t)(s0 + j) * 2 * N + (size_t)c * N;
 				if(dst) dst[off + q] = x;
 				if(acc_out) acc_out[off + q] = acc_in[off + q] + x;
@@ -2161,7 +2161,7 @@ __device__ __forceinline__ int ref_wrap(int i, int n) {
 template <typename R>
 __device__ __forceinline__ void phase_apply(const cx<R>* C, size_t N, int p, cx<R>& a, cx<R>& b) {
 	cx<R> oxx = C[(C_PH + 0) * N + p], oyy = C[(C_PH + 1) * N + p], oxy = C[(C_PH + 2) * N + p];
-	cx<R> u = oxx * a + oxy * b, v = oxy * a + oyy * b;
+	cx<R> u = cfma(oxy, b, oxx * a), v = cfma(oyy, b, oxy * a);
 	a = u;
 	b = v;
 }
