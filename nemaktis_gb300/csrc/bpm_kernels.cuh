@@ -43,6 +43,25 @@ struct ShiftParams {
 	int msx, msy;     // integer parts of the shifts
 	double wx[4], wy[4];
 	double ph_re, ph_im;
+	// the same weights and phase factor rounded to FP32 (the FP32 transition reads these instead of
+	// converting the FP64 values at each use)
+	float fwx[4], fwy[4];
+	float fph_re, fph_im;
+};
+
+// Shift weights and phase factor in the arithmetic type R.
+template <typename R>
+struct ShiftW {
+	R wx[4], wy[4];
+	cx<R> ph;
+	__device__ __forceinline__ explicit ShiftW(const ShiftParams& P) {
+#pragma unroll
+		for(int k = 0; k < 4; k++) {
+			wx[k] = sizeof(R) == sizeof(float) ? (R)P.fwx[k] : (R)P.wx[k];
+			wy[k] = sizeof(R) == sizeof(float) ? (R)P.fwy[k] : (R)P.wy[k];
+		}
+		ph = sizeof(R) == sizeof(float) ? mk<R>((R)P.fph_re, (R)P.fph_im) : mk<R>((R)P.ph_re, (R)P.ph_im);
+	}
 };
 
 struct Geom {
@@ -1163,7 +1182,7 @@ __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_xc(Geom G, 
 		const cx<R>* __restrict__ src, cx<R>* __restrict__ dst, const cx<R>* acc_in, cx<R>* acc_out,
 		const cx<R>* acc_in2) {
 	extern __shared__ unsigned char smem_raw[];
-	const int LT = blockDim.x / 32;
+	constexpr int LT = 4;  // lines (warps) per block: launched with 128 threads
 	const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
 	const int Nx = G.Nx, Ny = G.Ny, N = G.N;
 	const int iy = blockIdx.x * LT + warp;
@@ -1251,20 +1270,39 @@ __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_xc(Geom G, 
 			}
 		}
 	}
+	// the explicit-step solves never accumulate; the accumulating ones load the accumulator inputs
+	// of several points before storing any (their latency would otherwise be paid point by point)
+	const bool acc = KIND != ST_EXPL_Y && acc_out;
 	if(!TOUT) {
 	__syncwarp();
-	for(int j = 0; j < KS; j++) {
-		const size_t off = (size_t)(s0 + j) * 2 * N + (size_t)c * N + (size_t)iy * Nx;
+	constexpr int U = 3;
 #pragma unroll 1
-		for(int t = 0; t <= M; t++) {
-			const int e = lane + 32 * t;
-			if(e < Nx) {
-				int ee = e == Nx - 1 ? 0 : e;
-				cx<R> x = buf[j * PITCH + (ee / M) * (M + 1) + ee % M];
-				if(dst) dst[off + e] = x;
-				// the explicit-step solves never accumulate
-				if(KIND != ST_EXPL_Y && acc_out)
-					acc_out[off + e] = (acc_in2 ? acc_in[off + e] + acc_in2[off + e] : acc_in[off + e]) + x;
+	for(int t0 = 0; t0 <= M; t0 += U) {
+		cx<R> a[U][KS];
+		if(acc) {
+#pragma unroll
+			for(int u = 0; u < U; u++) {
+				const int e = lane + 32 * (t0 + u);
+				if(t0 + u <= M && e < Nx)
+#pragma unroll
+					for(int j = 0; j < KS; j++) {
+						const size_t o = (size_t)(s0 + j) * 2 * N + (size_t)c * N + (size_t)iy * Nx + e;
+						a[u][j] = acc_in2 ? acc_in[o] + acc_in2[o] : acc_in[o];
+					}
+			}
+		}
+#pragma unroll
+		for(int u = 0; u < U; u++) {
+			const int e = lane + 32 * (t0 + u);
+			if(t0 + u <= M && e < Nx) {
+				const int ee = e == Nx - 1 ? 0 : e;
+#pragma unroll
+				for(int j = 0; j < KS; j++) {
+					const size_t o = (size_t)(s0 + j) * 2 * N + (size_t)c * N + (size_t)iy * Nx + e;
+					const cx<R> x = buf[j * PITCH + (ee / M) * (M + 1) + ee % M];
+					if(dst) dst[o] = x;
+					if(acc) acc_out[o] = a[u][j] + x;
+				}
 			}
 		}
 	}
@@ -1273,18 +1311,36 @@ __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_xc(Geom G, 
 	if(TOUT) {
 		__syncthreads();
 		const cx<R>* bufs = reinterpret_cast<const cx<R>*>(smem_raw);
-		for(int t = threadIdx.x; t < Nx * LT; t += blockDim.x) {
-			const int e = t / LT, w = t % LT, line = blockIdx.x * LT + w;
-			if(line >= Ny) continue;
-			const int ee = e == Nx - 1 ? 0 : e;
-			const cx<R>* bw = bufs + (size_t)w * KS * PITCH + (ee / M) * (M + 1) + ee % M;
+		const bool acc = KIND != ST_EXPL_Y && acc_out;
+		constexpr int U = 4, BT = 32 * LT;
+		for(int t0 = threadIdx.x; t0 < Nx * LT; t0 += U * BT) {
+			cx<R> a[U][KS];
+			if(acc) {
 #pragma unroll
-			for(int j = 0; j < KS; j++) {
-				const size_t in = (size_t)(s0 + j) * 2 * N + (size_t)c * N + (size_t)line * Nx + e;
-				const size_t out = (size_t)(s0 + j) * 2 * N + (size_t)(1 - c) * N + (size_t)e * Ny + line;
-				const cx<R> x = bw[j * PITCH];
-				if(dst) dst[out] = x;
-				if(KIND != ST_EXPL_Y && acc_out) acc_out[out] = (acc_in2 ? acc_in[in] + acc_in2[in] : acc_in[in]) + x;
+				for(int u = 0; u < U; u++) {
+					const int t = t0 + u * BT, e = t / LT, line = blockIdx.x * LT + t % LT;
+					if(t < Nx * LT && line < Ny)
+#pragma unroll
+						for(int j = 0; j < KS; j++) {
+							const size_t in = (size_t)(s0 + j) * 2 * N + (size_t)c * N + (size_t)line * Nx + e;
+							a[u][j] = acc_in2 ? acc_in[in] + acc_in2[in] : acc_in[in];
+						}
+				}
+			}
+#pragma unroll
+			for(int u = 0; u < U; u++) {
+				const int t = t0 + u * BT, e = t / LT, w = t % LT, line = blockIdx.x * LT + w;
+				if(t < Nx * LT && line < Ny) {
+					const int ee = e == Nx - 1 ? 0 : e;
+					const cx<R>* bw = bufs + (size_t)w * KS * PITCH + (ee / M) * (M + 1) + ee % M;
+#pragma unroll
+					for(int j = 0; j < KS; j++) {
+						const size_t out = (size_t)(s0 + j) * 2 * N + (size_t)(1 - c) * N + (size_t)e * Ny + line;
+						const cx<R> x = bw[j * PITCH];
+						if(dst) dst[out] = x;
+						if(acc) acc_out[out] = a[u][j] + x;
+					}
+				}
 			}
 		}
 	}
@@ -2326,7 +2382,8 @@ __global__ void __launch_bounds__(256) k_shift_fused(Geom G, int slot0, const Sh
 	const int gs = slot0 + s;
 	const int g = gs / G.spg - slot0 / G.spg;
 	const int gq = (gs / G.spg) * G.Nq + (gs / 2) % G.Nq;
-	const ShiftParams P = sp[gq];
+	const ShiftParams& P = sp[gq];
+	const ShiftW<R> W(P);
 	const size_t N = G.N;
 	const int Nx = G.Nx, Ny = G.Ny;
 	const bool ax = Nx > 3, ay = Ny > 3;
@@ -2339,7 +2396,7 @@ __global__ void __launch_bounds__(256) k_shift_fused(Geom G, int slot0, const Sh
 	const int Px = Nx - 1, Py = Ny - 1;
 	const int bx = ax ? nsh * (P.msx - 1) : 0, by = ay ? nsh * (P.msy - 1) : 0;
 	const int wx = ax ? SHT + 3 * nsh : SHT, wy = ay ? SHT + 3 * nsh : SHT;
-	cx<R> ph = mk<R>((R)P.ph_re, (R)P.ph_im);
+	cx<R> ph = W.ph;
 	if(nsh == 2) ph = ph * ph;
 	// every tap index of both passes stays above -(N-1): mod arithmetic equals the wrap rule
 	const bool regular = (!ax || P.msx - 1 > -Px) && (!ay || P.msy - 1 > -Py);
@@ -2381,8 +2438,7 @@ __global__ void __launch_bounds__(256) k_shift_fused(Geom G, int slot0, const Sh
 				int t = e % ow, v = e / ow;
 				for(int c = 0; c < 2; c++) {
 					const cx<R>* in = cur + c * PW * PW + v * PW + t;
-					nxt[c * PW * PW + v * PW + t] = (R)P.wx[0] * in[0] + (R)P.wx[1] * in[1] + (R)P.wx[2] * in[2] +
-						(R)P.wx[3] * in[3];
+					nxt[c * PW * PW + v * PW + t] = W.wx[0] * in[0] + W.wx[1] * in[1] + W.wx[2] * in[2] + W.wx[3] * in[3];
 				}
 			}
 			__syncthreads();
@@ -2399,8 +2455,8 @@ __global__ void __launch_bounds__(256) k_shift_fused(Geom G, int slot0, const Sh
 				int t = e % SHT, v = e / SHT;
 				for(int c = 0; c < 2; c++) {
 					const cx<R>* in = cur + c * PW * PW + v * PW + t;
-					nxt[c * PW * PW + v * PW + t] = (R)P.wy[0] * in[0] + (R)P.wy[1] * in[PW] +
-						(R)P.wy[2] * in[2 * PW] + (R)P.wy[3] * in[3 * PW];
+					nxt[c * PW * PW + v * PW + t] = W.wy[0] * in[0] + W.wy[1] * in[PW] + W.wy[2] * in[2 * PW] +
+						W.wy[3] * in[3 * PW];
 				}
 			}
 			__syncthreads();

@@ -253,6 +253,8 @@ __global__ void k_shift_params(int ngroups, int Nq, int Nx, int Ny, const GroupP
 		P.wy[2] = nu * (1 + 4 * nu - 3 * nu * nu) / 2;
 		P.wy[3] = -nu * nu * (1 - nu) / 2;
 	}
+	for(int k = 0; k < 4; k++) { P.fwx[k] = (float)P.wx[k]; P.fwy[k] = (float)P.wy[k]; }
+	P.fph_re = (float)P.ph_re; P.fph_im = (float)P.ph_im;
 	sp[t] = P;
 }
 
