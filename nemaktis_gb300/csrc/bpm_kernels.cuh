@@ -2305,8 +2305,10 @@ __global__ void k_shift_y(Geom G, int slot0, const ShiftParams* __restrict__ sp,
 // shift_y(B)): F_out = phase_B(ph^n * Y^n X^n (phase_A(F))), n = nshift (1 or 2). X and Y are
 // the circulant cubic shifts of SimpleShiftOperator (period Nx-1 / Ny-1; they act on rows and
 // columns and commute, so Y X Y X = Y Y X X). For a tile of 32 x 32 outputs of one slot the
-// block stages the input window (phase_A applied) in shared memory, runs the n x-passes and
-// the n y-passes there, and writes the tile. Indices wrap with i mod (N-1), which equals the
+// block stages the input window (phase_A applied) in shared memory; each thread then runs the n
+// x-passes over 8 consecutive outputs of a window row in registers (the 8 + 3n inputs read once)
+// into a second buffer, and the n y-passes over 4 consecutive rows of an output column, and
+// writes the tile. Indices wrap with i mod (N-1), which equals the
 // reference's wrap rule for every index above -(N-1) (the composition of two wrapped passes
 // then also reduces to one mod); a slot whose integer shift reaches -(N-2) or below takes the
 // exact per-point path instead. The duplicate row and column of F are never read, as in the
@@ -2375,9 +2377,6 @@ __global__ void __launch_bounds__(256) k_shift_fused(Geom G, int slot0, const Sh
 		const cx<R>* __restrict__ CA, const cx<R>* __restrict__ CB, int nsh, const cx<R>* __restrict__ F,
 		cx<R>* __restrict__ Fo) {
 	extern __shared__ unsigned char smem_raw[];
-	const int PW = SHT + 6;                    // window pitch (room for two 4-tap passes)
-	cx<R>* A = reinterpret_cast<cx<R>*>(smem_raw);  // [2][PW][PW]
-	cx<R>* B = A + 2 * PW * PW;                     // [2][PW][PW]
 	const int s = blockIdx.z;
 	const int gs = slot0 + s;
 	const int g = gs / G.spg - slot0 / G.spg;
@@ -2415,66 +2414,99 @@ __global__ void __launch_bounds__(256) k_shift_fused(Geom G, int slot0, const Sh
 		}
 		return;
 	}
-	// 1. input window, phase_A applied (unrolled so several loads are in flight)
-#pragma unroll 4
-	for(int e = tid; e < wx * wy; e += blockDim.x) {
-		int u = e % wx, v = e / wx;
-		int xi = ax ? pmod(x0 + bx + u, Px) : x0 + u;
-		int yi = ay ? pmod(y0 + by + v, Py) : y0 + v;
-		cx<R> a = mk<R>(0, 0), b = mk<R>(0, 0);
-		if(xi < Nx && yi < Ny) tap_in(f, Ca, N, xi + Nx * yi, a, b);
-		A[v * PW + u] = a;
-		A[PW * PW + v * PW + u] = b;
+	// 1. input window, phase_A applied: warp w takes the window rows w, w + 8, ..., lane l the
+	// columns l and l + 32; the wrapped source row and columns are computed once per row / thread
+	constexpr int PA = SHT + 7, PB = SHT + 1;  // odd pitches (8-byte words): no bank conflicts
+	cx<R>* A = reinterpret_cast<cx<R>*>(smem_raw);  // [2][wy][PA]: the window
+	cx<R>* B = A + 2 * (SHT + 6) * PA;             // [2][wy][PB]: the window after the x-passes
+	const int lane = tid % 32, warp = tid / 32, nwarp = blockDim.x / 32;
+	int xc[2];
+#pragma unroll
+	for(int h = 0; h < 2; h++) {
+		const int u = lane + 32 * h;
+		xc[h] = u >= wx ? -1 : ax ? pmod(x0 + bx + u, Px) : (x0 + u < Nx ? x0 + u : -1);
+	}
+	for(int v = warp; v < wy; v += nwarp) {
+		const int yi = ay ? pmod(y0 + by + v, Py) : (y0 + v < Ny ? y0 + v : -1);
+#pragma unroll
+		for(int h = 0; h < 2; h++) {
+			const int u = lane + 32 * h;
+			if(u < wx) {
+				cx<R> a = mk<R>(0, 0), b = mk<R>(0, 0);
+				if(xc[h] >= 0 && yi >= 0) tap_in(f, Ca, N, xc[h] + Nx * yi, a, b);
+				A[v * PA + u] = a;
+				A[(SHT + 6) * PA + v * PA + u] = b;
+			}
+		}
 	}
 	__syncthreads();
-	cx<R>* cur = A;
-	cx<R>* nxt = B;
-	int cw = wx;
-	// 2. x-passes on every window row
+	// 2. the n x-passes of one component over 8 consecutive outputs of a window row per thread, in
+	// registers (consecutive threads take consecutive rows)
+	const cx<R>* Y = A;  // what the y-passes read, with its pitch
+	int PY = PA;
 	if(ax) {
-		for(int pass = 0; pass < nsh; pass++) {
-			int ow = cw - 3;
-			for(int e = tid; e < ow * wy; e += blockDim.x) {
-				int t = e % ow, v = e / ow;
-				for(int c = 0; c < 2; c++) {
-					const cx<R>* in = cur + c * PW * PW + v * PW + t;
-					nxt[c * PW * PW + v * PW + t] = W.wx[0] * in[0] + W.wx[1] * in[1] + W.wx[2] * in[2] + W.wx[3] * in[3];
-				}
+		const int nin = 8 + 3 * nsh;
+		for(int t = tid; t < 2 * 4 * wy; t += blockDim.x) {
+			const int v = t % wy, r = t / wy, seg = r % 4, c = r / 4;
+			const cx<R>* in = A + c * (SHT + 6) * PA + v * PA + seg * 8;
+			cx<R> w[14];
+#pragma unroll
+			for(int k = 0; k < 14; k++) w[k] = k < nin ? in[k] : mk<R>(0, 0);
+			// first pass: 8 + 3 (n - 1) values, second pass (n = 2): 8
+#pragma unroll
+			for(int k = 0; k < 11; k++) w[k] = W.wx[0] * w[k] + W.wx[1] * w[k + 1] + W.wx[2] * w[k + 2] + W.wx[3] * w[k + 3];
+			if(nsh == 2) {
+#pragma unroll
+				for(int k = 0; k < 8; k++) w[k] = W.wx[0] * w[k] + W.wx[1] * w[k + 1] + W.wx[2] * w[k + 2] + W.wx[3] * w[k + 3];
 			}
-			__syncthreads();
-			cx<R>* tmp = cur; cur = nxt; nxt = tmp;
-			cw = ow;
+			cx<R>* out = B + c * (SHT + 6) * PB + v * PB + seg * 8;
+#pragma unroll
+			for(int k = 0; k < 8; k++) out[k] = w[k];
 		}
+		__syncthreads();
+		Y = B;
+		PY = PB;
 	}
-	int ch = wy;
-	// 3. y-passes on the SHT columns of the tile
-	if(ay) {
-		for(int pass = 0; pass < nsh; pass++) {
-			int oh = ch - 3;
-			for(int e = tid; e < SHT * oh; e += blockDim.x) {
-				int t = e % SHT, v = e / SHT;
-				for(int c = 0; c < 2; c++) {
-					const cx<R>* in = cur + c * PW * PW + v * PW + t;
-					nxt[c * PW * PW + v * PW + t] = W.wy[0] * in[0] + W.wy[1] * in[PW] + W.wy[2] * in[2 * PW] +
-						W.wy[3] * in[3 * PW];
+	// 3. the n y-passes over 4 consecutive output rows of one column per thread (both components),
+	// then the phase factor, phase_B and the store (consecutive threads take consecutive columns)
+	for(int t = tid; t < SHT * (SHT / 4); t += blockDim.x) {
+		const int u = t % SHT, seg = t / SHT;
+		const int ix = x0 + u;
+		cx<R> o[2][4];
+#pragma unroll
+		for(int c = 0; c < 2; c++) {
+			const cx<R>* in = Y + c * (SHT + 6) * PY + seg * 4 * PY + u;
+			if(ay) {
+				const int nin = 4 + 3 * nsh;
+				cx<R> w[10];
+#pragma unroll
+				for(int k = 0; k < 10; k++) w[k] = k < nin ? in[k * PY] : mk<R>(0, 0);
+#pragma unroll
+				for(int k = 0; k < 7; k++) w[k] = W.wy[0] * w[k] + W.wy[1] * w[k + 1] + W.wy[2] * w[k + 2] + W.wy[3] * w[k + 3];
+				if(nsh == 2) {
+#pragma unroll
+					for(int k = 0; k < 4; k++) w[k] = W.wy[0] * w[k] + W.wy[1] * w[k + 1] + W.wy[2] * w[k + 2] + W.wy[3] * w[k + 3];
 				}
+#pragma unroll
+				for(int k = 0; k < 4; k++) o[c][k] = w[k];
 			}
-			__syncthreads();
-			cx<R>* tmp = cur; cur = nxt; nxt = tmp;
-			ch = oh;
+			else {
+#pragma unroll
+				for(int k = 0; k < 4; k++) o[c][k] = in[k * PY];
+			}
 		}
-	}
-	// 4. phase factor, phase_B, store
-#pragma unroll 4
-	for(int e = tid; e < SHT * SHT; e += blockDim.x) {
-		int t = e % SHT, v = e / SHT;
-		int ix = x0 + t, iy = y0 + v;
-		if(ix >= Nx || iy >= Ny) continue;
-		cx<R> o0 = cur[v * PW + t] * ph, o1 = cur[PW * PW + v * PW + t] * ph;
-		int p = ix + Nx * iy;
-		if(Cb) phase_apply(Cb, N, p, o0, o1);
-		fo[p] = o0;
-		fo[N + p] = o1;
+		if(ix >= Nx) continue;
+#pragma unroll
+		for(int k = 0; k < 4; k++) {
+			const int iy = y0 + seg * 4 + k;
+			if(iy < Ny) {
+				cx<R> o0 = o[0][k] * ph, o1 = o[1][k] * ph;
+				const int p = ix + Nx * iy;
+				if(Cb) phase_apply(Cb, N, p, o0, o1);
+				fo[p] = o0;
+				fo[N + p] = o1;
+			}
+		}
 	}
 }
 
