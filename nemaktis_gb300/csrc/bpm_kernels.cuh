@@ -6,8 +6,9 @@
 //                                            order as the (Nl,Nq,4,Ny,Nx) user buffer
 //   eps ring  Q[2][group][NQ][iy][ix]        FP64 per-voxel derived permittivity, planes iz
 //                                            and iz+1 of every wavelength group
-//   coef      C[group][NCOEF][iy][ix]        cx<R>: 3 phase-operator entries and the 40
-//                                            entries of mu*R (DX, DY, DXDY stencils x 4 blocks)
+//   coef      C[group][p/32][NCOEF][p%32]    cx<R>: 3 phase-operator entries and the 40
+//                                            entries of mu*R (DX, DY, DXDY stencils x 4 blocks),
+//                                            p = iy*Nx + ix, in tiles of 32 points (cidx)
 //   factors   X/Y[group][comp][NFAC][p]      cx<R>: pre-factored periodic line solves
 // A "group" is one wavelength: every (q, pol) slot of the group shares eps, R, the phase
 // operator and the line-solve factorisations.
@@ -23,6 +24,13 @@ namespace nbpm {
 enum { Q_XXTR = 0, Q_YYTR, Q_XYTR, Q_XXS, Q_YYS, Q_XYS, Q_VX, Q_VY, Q_IZZ, NQ };
 // Coefficient planes: phase operator (xx, yy, xy), then mu*R stencils.
 enum { C_PH = 0, C_DX = 3, C_DY = 15, C_DXDY = 27, NCOEF = 43 };
+// A group's coefficient set is stored in tiles of 32 points with every plane of a tile together:
+// entry (plane k, point p) at ((p / 32) * NCOEF + k) * 32 + p % 32, NCOEF * ceil(N / 32) * 32
+// entries per group. The planes a kernel reads at one point are then fixed multiples of 32
+// entries apart (compile-time offsets from one address), and 32 consecutive points of a plane
+// starting at a multiple of 32 are one contiguous segment.
+__host__ __device__ __forceinline__ size_t coef_set_size(int N) { return (size_t)NCOEF * (((size_t)N + 31) & ~(size_t)31); }
+__host__ __device__ __forceinline__ size_t cidx(int k, int p) { return ((size_t)(p >> 5) * NCOEF + k) * 32 + (p & 31); }
 // FP64 copies of the diagonal-block stencils used by the line factorisations:
 // index dir*6 + comp*3 + k (dir 0 = DX, 1 = DY; comp 0 = block 00, 1 = block 11).
 enum { NDIAG = 12 };
@@ -349,7 +357,7 @@ __global__ void k_coef(const S* __restrict__ QA, const S* __restrict__ QB,
 	const GroupParams gp = gps[g];
 	const T* A = QA + (size_t)g * NQ * N;
 	const T* B = QB + (size_t)g * NQ * N;
-	cx<S>* C = coef + (size_t)g * NCOEF * N + p;
+	cx<S>* C = coef + (size_t)g * coef_set_size(N);
 	cx<S>* Dg = diag + (size_t)g * NDIAG * N + p;
 
 	// Phase operator.
@@ -358,9 +366,9 @@ __global__ void k_coef(const S* __restrict__ QA, const S* __restrict__ QB,
 		if(wts) { size_t vi = (size_t)iz * N + p; w0 = (T)wts[2 * vi]; w1 = (T)wts[2 * vi + 1]; }
 		cx<T> oxx, oyy, oxy;
 		phase_op<T>(A, B, N, p, w0, w1, gp, oxx, oyy, oxy);
-		C[(size_t)(C_PH + 0) * N] = oxx;
-		C[(size_t)(C_PH + 1) * N] = oyy;
-		C[(size_t)(C_PH + 2) * N] = oxy;
+		C[cidx(C_PH + 0, p)] = oxx;
+		C[cidx(C_PH + 1, p)] = oyy;
+		C[cidx(C_PH + 2, p)] = oxy;
 	}
 
 	CoefCtx<T> X;
@@ -399,7 +407,7 @@ __global__ void k_coef(const S* __restrict__ QA, const S* __restrict__ QB,
 				X.entry(c1[k] * kxx, c1[k] * kxy, (T)0, L[k], cxp, iy, dd[k], 0, r);
 			}
 			else r[0] = r[1] = r[2] = r[3] = z;
-			for(int b = 0; b < 4; b++) C[(size_t)(C_DX + 3 * b + k) * N] = cvt<S>(r[b]);
+			for(int b = 0; b < 4; b++) C[cidx(C_DX + 3 * b + k, p)] = cvt<S>(r[b]);
 			Dg[(size_t)(0 * 6 + 0 * 3 + k) * N] = r[0];
 			Dg[(size_t)(0 * 6 + 1 * 3 + k) * N] = r[3];
 		}
@@ -424,7 +432,7 @@ __global__ void k_coef(const S* __restrict__ QA, const S* __restrict__ QB,
 				X.entry(L[k], (T)0, c1[k] * kxy, c1[k] * kyy, ix, cyp, dd[k], 1, r);
 			}
 			else r[0] = r[1] = r[2] = r[3] = z;
-			for(int b = 0; b < 4; b++) C[(size_t)(C_DY + 3 * b + k) * N] = cvt<S>(r[b]);
+			for(int b = 0; b < 4; b++) C[cidx(C_DY + 3 * b + k, p)] = cvt<S>(r[b]);
 			Dg[(size_t)(1 * 6 + 0 * 3 + k) * N] = r[0];
 			Dg[(size_t)(1 * 6 + 1 * 3 + k) * N] = r[3];
 		}
@@ -451,7 +459,7 @@ __global__ void k_coef(const S* __restrict__ QA, const S* __restrict__ QB,
 					cxs[k], cys[k], (T)0, 0, r);
 			}
 			else r[0] = r[1] = r[2] = r[3] = z;
-			for(int b = 0; b < 4; b++) C[(size_t)(C_DXDY + 4 * b + k) * N] = cvt<S>(r[b]);
+			for(int b = 0; b < 4; b++) C[cidx(C_DXDY + 4 * b + k, p)] = cvt<S>(r[b]);
 		}
 	}
 }
@@ -463,7 +471,7 @@ template <typename R>
 struct Stencil {
 	const cx<R>* C;
 	int N, Nx, Ny;
-	__device__ __forceinline__ cx<R> c(int plane, int p) const { return C[(size_t)plane * N + p]; }
+	__device__ __forceinline__ cx<R> c(int plane, int p) const { return C[cidx(plane, p)]; }
 	// DX block b at row (x, y): columns mx, x, px with period Nx-1.
 	__device__ __forceinline__ cx<R> dx(int b, int x, int y, const cx<R>* s) const {
 		int p = x + Nx * y;
@@ -670,7 +678,7 @@ __global__ void k_stencil(Geom G, int slot0, const cx<R>* __restrict__ coef, con
 	if(p >= N) return;
 	int s = blockIdx.y;
 	int g = (slot0 + s) / G.spg - slot0 / G.spg;
-	Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
+	Stencil<R> st{coef + (size_t)g * coef_set_size(N), N, Nx, Ny};
 	const cx<R>* f0 = src + (size_t)s * 2 * N;
 	const cx<R>* f1 = f0 + N;
 	int ix = p % Nx, iy = p / Nx;
@@ -790,17 +798,19 @@ __global__ void __launch_bounds__(256) k_coef_t(Geom G, const cx<S>* __restrict_
 		dp = C_DXDY + 4 * b + kk; sp = C_DXDY + 4 * (3 - b) + sk;
 	}
 	else { const int cp = (k - 34) / 3, kk = (k - 34) % 3; dp = 0 * 6 + cp * 3 + kk; sp = 1 * 6 + (1 - cp) * 3 + kk; dg = true; }
-	const cx<S>* src = (dg ? diag + (size_t)g * NDIAG * N : coef + (size_t)g * NCOEF * N) + (size_t)sp * N;
-	cx<S>* dst = (dg ? diagT + (size_t)g * NDIAG * N : coefT + (size_t)g * NCOEF * N) + (size_t)dp * N;
+	// diagonal stencils: plain planes; coefficient planes: the tiled layout (cidx)
+	const cx<S>* src = dg ? diag + (size_t)g * NDIAG * N : coef + (size_t)g * coef_set_size(N);
+	cx<S>* dst = dg ? diagT + (size_t)g * NDIAG * N : coefT + (size_t)g * coef_set_size(N);
+	auto at = [&](int plane, int q) { return dg ? (size_t)plane * N + q : cidx(plane, q); };
 	const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
 	for(int r = threadIdx.y; r < 32; r += blockDim.y) {
 		const int x = x0 + threadIdx.x, y = y0 + r;
-		if(x < Nx && y < Ny) tile[r][threadIdx.x] = src[(size_t)y * Nx + x];
+		if(x < Nx && y < Ny) tile[r][threadIdx.x] = src[at(sp, y * Nx + x)];
 	}
 	__syncthreads();
 	for(int r = threadIdx.y; r < 32; r += blockDim.y) {
 		const int y = y0 + threadIdx.x, x = x0 + r;  // destination row x, column y
-		if(x < Nx && y < Ny) dst[(size_t)x * Ny + y] = tile[threadIdx.x][r];
+		if(x < Nx && y < Ny) dst[at(dp, x * Ny + y)] = tile[threadIdx.x][r];
 	}
 }
 
@@ -1199,7 +1209,7 @@ __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_xc(Geom G, 
 	const cx<double> r0 = ls[0], rden = ls[1];
 	const int i0 = lane * M;
 	const cx<R> one = mk<R>(1, 0), zero = mk<R>(0, 0);
-	const Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
+	const Stencil<R> st{coef + (size_t)g * coef_set_size(N), N, Nx, Ny};
 	const cx<R>* f0 = src + (size_t)s0 * 2 * N;
 	// right-hand sides, coalesced (point e = lane + 32 t), into the lane-chunk layout of buf; the
 	// fixed trip count (rolled, unroll 2 and 4 measured slower on GB300) beats a loop to n_unk
@@ -1374,7 +1384,7 @@ __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_yt(Geom G, 
 	const int n_unk = Ny - 1;
 	const int PITCH = 32 * (M + 1);
 	cx<R>* const bufs = reinterpret_cast<cx<R>*>(smem_raw);
-	const Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
+	const Stencil<R> st{coef + (size_t)g * coef_set_size(N), N, Nx, Ny};
 	const cx<R>* f0 = src + (size_t)s0 * 2 * N;
 	const cx<R> one = mk<R>(1, 0), zero = mk<R>(0, 0);
 	// right-hand sides of every (row, column) pair of the block's columns
@@ -1540,7 +1550,7 @@ __global__ void __launch_bounds__(MAXT, NBPM_YC_MINB) k_solve_yc(Geom G, int slo
 	const cx<R>* Fc = fac + ((size_t)g * 2 + c) * NFAC * plane;
 	const int i0 = w * M;
 	const cx<R> one = mk<R>(1, 0), zero = mk<R>(0, 0);
-	const Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
+	const Stencil<R> st{coef + (size_t)g * coef_set_size(N), N, Nx, Ny};
 	const cx<R>* f0 = src + (size_t)s0 * 2 * N;
 	// chunk pass: right-hand sides b (kept in v) and the chunk maps of line_combine
 	cx<R> v[VS ? 1 : KS][VS ? 1 : M];
@@ -1656,7 +1666,7 @@ __global__ void __launch_bounds__(128) k_solve_yq(Geom G, int nch, const cx<R>* 
 	const int s0 = g * G.spg + ch * KS;
 	const int n = Ny - 1;
 	const size_t ss = 2 * (size_t)N;
-	const Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
+	const Stencil<R> st{coef + (size_t)g * coef_set_size(N), N, Nx, Ny};
 	const cx<R>* f0 = src + (size_t)s0 * ss;
 	const cx<R>* F0 = fac + ((size_t)g * 2 + 0) * NFAC * plane;
 	const cx<R>* F1 = fac + ((size_t)g * 2 + 1) * NFAC * plane;
@@ -1759,7 +1769,7 @@ __global__ void __launch_bounds__(256) k_solve_xw(Geom G, int slot0, int nch, co
 	const int i0 = ci * M;
 	const int last = n_unk - 1;
 	const cx<R> one = mk<R>(1, 0), zero = mk<R>(0, 0);
-	const Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
+	const Stencil<R> st{coef + (size_t)g * coef_set_size(N), N, Nx, Ny};
 	const cx<R>* f0 = src + (size_t)s0 * 2 * N;
 	for(int e = threadIdx.x; e < n_unk; e += blockDim.x) {
 		cx<R> r[KS];
@@ -1940,7 +1950,7 @@ __global__ void __launch_bounds__(128) k_solve_xs(Geom G, int slot0, int nch, in
 	const int i0 = lane * M;
 	const int last = n_unk - 1, lane_last = last / M, k_last = last % M;
 	const cx<R> one = mk<R>(1, 0), zero = mk<R>(0, 0);
-	const Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
+	const Stencil<R> st{coef + (size_t)g * coef_set_size(N), N, Nx, Ny};
 	const cx<R>* f0 = src + (size_t)s0 * 2 * N;
 	for(int e = lane; e < n_unk; e += 32) {
 		cx<R> r[KS];
@@ -2084,7 +2094,7 @@ __global__ void __launch_bounds__(256) k_solve_ys(Geom G, int slot0, int nch, co
 		r0 = ls[0];
 		rden = ls[1];
 	}
-	const Stencil<R> st{coef + (size_t)g * NCOEF * N, N, Nx, Ny};
+	const Stencil<R> st{coef + (size_t)g * coef_set_size(N), N, Nx, Ny};
 	const cx<R>* f0 = src + (size_t)s0 * 2 * N;
 	auto va = [&](int j, int i) { return (size_t)(s0 + j) * 2 * N + (size_t)c * N + (size_t)ix + (size_t)Nx * i; };
 	cx<R> A[KS], B[KS];
@@ -2198,8 +2208,8 @@ __global__ void k_phase(Geom G, int slot0, const cx<R>* __restrict__ coef, cx<R>
 	int s = blockIdx.y;
 	int N = G.N;
 	int g = (slot0 + s) / G.spg - slot0 / G.spg;
-	const cx<R>* C = coef + (size_t)g * NCOEF * N + p;
-	cx<R> oxx = C[(C_PH + 0) * (size_t)N], oyy = C[(C_PH + 1) * (size_t)N], oxy = C[(C_PH + 2) * (size_t)N];
+	const cx<R>* C = coef + (size_t)g * coef_set_size(N);
+	cx<R> oxx = C[cidx(C_PH + 0, p)], oyy = C[cidx(C_PH + 1, p)], oxy = C[cidx(C_PH + 2, p)];
 	cx<R>* f = F + (size_t)s * 2 * N + p;
 	cx<R> a = f[0], b = f[N];
 	f[0] = oxx * a + oxy * b;
@@ -2216,7 +2226,7 @@ __device__ __forceinline__ int ref_wrap(int i, int n) {
 
 template <typename R>
 __device__ __forceinline__ void phase_apply(const cx<R>* C, size_t N, int p, cx<R>& a, cx<R>& b) {
-	cx<R> oxx = C[(C_PH + 0) * N + p], oyy = C[(C_PH + 1) * N + p], oxy = C[(C_PH + 2) * N + p];
+	cx<R> oxx = C[cidx(C_PH + 0, p)], oyy = C[cidx(C_PH + 1, p)], oxy = C[cidx(C_PH + 2, p)];
 	cx<R> u = cfma(oxy, b, oxx * a), v = cfma(oyy, b, oxy * a);
 	a = u;
 	b = v;
@@ -2239,7 +2249,7 @@ __global__ void k_shift_x(Geom G, int slot0, const ShiftParams* __restrict__ sp,
 	const int Nx = G.Nx;
 	int ix = p % Nx, iy = p / Nx;
 	const cx<R>* f = F + (size_t)s * 2 * N;
-	const cx<R>* Cg = CA ? CA + (size_t)g * NCOEF * N : nullptr;
+	const cx<R>* Cg = CA ? CA + (size_t)g * coef_set_size(N) : nullptr;
 	cx<R> v0, v1;
 	if(Nx > 3) {
 		v0 = mk<R>(0, 0);
@@ -2296,7 +2306,7 @@ __global__ void k_shift_y(Geom G, int slot0, const ShiftParams* __restrict__ sp,
 	}
 	v0 = v0 * ph;
 	v1 = v1 * ph;
-	if(CB) phase_apply(CB + (size_t)g * NCOEF * N, N, p, v0, v1);
+	if(CB) phase_apply(CB + (size_t)g * coef_set_size(N), N, p, v0, v1);
 	F[(size_t)s * 2 * N + p] = v0;
 	F[(size_t)s * 2 * N + N + p] = v1;
 }
@@ -2390,8 +2400,8 @@ __global__ void __launch_bounds__(256) k_shift_fused(Geom G, int slot0, const Sh
 	const int tid = threadIdx.x;
 	const cx<R>* f = F + (size_t)s * 2 * N;
 	cx<R>* fo = Fo + (size_t)s * 2 * N;
-	const cx<R>* Ca = CA ? CA + (size_t)g * NCOEF * N : nullptr;
-	const cx<R>* Cb = CB ? CB + (size_t)g * NCOEF * N : nullptr;
+	const cx<R>* Ca = CA ? CA + (size_t)g * coef_set_size(N) : nullptr;
+	const cx<R>* Cb = CB ? CB + (size_t)g * coef_set_size(N) : nullptr;
 	const int Px = Nx - 1, Py = Ny - 1;
 	const int bx = ax ? nsh * (P.msx - 1) : 0, by = ay ? nsh * (P.msy - 1) : 0;
 	const int wx = ax ? SHT + 3 * nsh : SHT, wy = ay ? SHT + 3 * nsh : SHT;
@@ -2527,8 +2537,8 @@ __global__ void k_phase_sync(Geom G, int slot0, const cx<R>* __restrict__ CA, co
 	int ix = p % Nx, iy = p / Nx;
 	if((ax && ix == Nx - 1) || (ay && iy == Ny - 1)) return;
 	cx<R>* f = F + (size_t)s * 2 * N;
-	const cx<R>* Ca = CA ? CA + (size_t)g * NCOEF * N : nullptr;
-	const cx<R>* Cb = CB ? CB + (size_t)g * NCOEF * N : nullptr;
+	const cx<R>* Ca = CA ? CA + (size_t)g * coef_set_size(N) : nullptr;
+	const cx<R>* Cb = CB ? CB + (size_t)g * coef_set_size(N) : nullptr;
 	cx<R> u0 = f[p], u1 = f[N + p];
 	if(Ca) phase_apply(Ca, N, p, u0, u1);
 	auto put = [&](int d) {

@@ -554,10 +554,10 @@ struct Plan : PlanBase {
 				dalloc(L.T2, sizeof(cx<R>) * nT);
 				if(need_t3) dalloc(L.T3, sizeof(cx<R>) * nT);
 				dalloc(L.Qring, sizeof(R) * (size_t)2 * ng * NQ * N);
-				dalloc(L.coef, sizeof(cx<R>) * (size_t)2 * ng * NCOEF * N);  // two slabs (transition kernels)
+				dalloc(L.coef, sizeof(cx<R>) * (size_t)2 * ng * coef_set_size((int)N));  // two slabs (transition kernels)
 				dalloc(L.diag, sizeof(cx<R>) * (size_t)ng * NDIAG * N);
 				if(need_t) {
-					dalloc(L.coefT, sizeof(cx<R>) * (size_t)2 * ng * NCOEF * N);
+					dalloc(L.coefT, sizeof(cx<R>) * (size_t)2 * ng * coef_set_size((int)N));
 					dalloc(L.diagT, sizeof(cx<R>) * (size_t)ng * NDIAG * N);
 				}
 				L.facx_half = L.facy_half = nFx;
@@ -962,7 +962,7 @@ struct Plan : PlanBase {
 		ps.Qr[0] = W->Qring.as<R>();
 		ps.Qr[1] = ps.Qr[0] + (size_t)ps.ng * NQ * N;
 		ps.Cring[0] = W->coef.as<cx<R>>();
-		ps.Cring[1] = W->coef.as<cx<R>>() + (size_t)ps.ng * NCOEF * N;
+		ps.Cring[1] = W->coef.as<cx<R>>() + (size_t)ps.ng * coef_set_size(N);
 		ps.Dg = W->diag.as<cx<R>>();
 		ps.eps_bytes = (double)N * ps.ng * (h.fd * 8 + (mk_ ? 1 : 0) + NQ * sizeof(R));
 		ps.field_pts = (double)N * ps.nsl;
@@ -1032,7 +1032,7 @@ struct Plan : PlanBase {
 				k_factor_chunked<R, 0><<<dim3((unsigned)((Ny + LT - 1) / LT), (unsigned)(ng * 2)), dim3(32, LT), 0, cs>>>(
 					Gm, ng, scf.Mx, 32 * scf.WPLx, 1, ps.Dg, fx, scf.plane_x, lx);
 			});
-			cx<R>* CT = scf.Mxt ? W->coefT.as<cx<R>>() + (size_t)(iz & 1) * ng * NCOEF * N : nullptr;
+			cx<R>* CT = scf.Mxt ? W->coefT.as<cx<R>>() + (size_t)(iz & 1) * ng * coef_set_size(N) : nullptr;
 			if(scf.Mxt) {
 				// y-lines as x-lines of the transposed frame: transposed coefficients and diagonals,
 				// then the x-line factorisation of that frame
