@@ -905,11 +905,13 @@ __global__ void __launch_bounds__(DIRN == 1 ? 512 : 256) k_factor_chunked(Geom G
 	const int stride = DIRN == 0 ? 1 : Nx;
 	const int base = DIRN == 0 ? Nx * line : line;
 	auto P = [&](int i) { return base + i * stride; };
-	// storage: natural layout, or the solves' chunk-interleaved x layout (chunksX chunks of
-	// chunkMx elements per line, element i = ci*chunkMx + k at k*chunksX + ci)
-	auto Q = [&](int i) -> size_t {
-		if(DIRN == 1 || chunkMx <= 0) return (size_t)P(i);
-		return (size_t)line * chunksX * chunkMx + (size_t)(i % chunkMx) * chunksX + (i / chunkMx);
+	// storage of factor f of element i: natural layout (plane f, point P(i)), or the solves'
+	// chunk-interleaved x layout: chunksX chunks of chunkMx elements per line, element
+	// i = ci*chunkMx + k of factor f at ((line*chunkMx + k)*NFAC + f)*chunksX + ci, so that the
+	// factors a lane reads for one element are compile-time offsets from one address
+	auto Q = [&](int f, int i) -> size_t {
+		if(DIRN == 1 || chunkMx <= 0) return (size_t)f * plane + P(i);
+		return (((size_t)line * chunkMx + i % chunkMx) * NFAC + f) * chunksX + (i / chunkMx);
 	};
 	const cx<T> one = mk<T>(1, 0), zero = mk<T>(0, 0);
 	auto sup = [&](int i) { return -Dg[2 * (size_t)N + P(i)]; };
@@ -976,9 +978,9 @@ __global__ void __launch_bounds__(DIRN == 1 ? 512 : 256) k_factor_chunked(Geom G
 			cx<T> beta = i == 0 ? (T)2 * m0 : midp(i) - cdiv(inf(i) * sup(i - 1), beta_prev);
 			cx<T> rb = crecip(beta);
 			cx<T> alpha = i == 0 ? zero : -(inf(i) * rb);
-			Fc[F_RB * plane + Q(i)] = cvt<S>(rb);
-			Fc[F_A * plane + Q(i)] = cvt<S>(alpha);
-			Fc[F_C * plane + Q(i)] = i < n - 1 ? cvt<S>(-(sup(i) * rb)) : mk<S>(0, 0);
+			Fc[Q(F_RB, i)] = cvt<S>(rb);
+			Fc[Q(F_A, i)] = cvt<S>(alpha);
+			Fc[Q(F_C, i)] = i < n - 1 ? cvt<S>(-(sup(i) * rb)) : mk<S>(0, 0);
 			// corr_0 = -1/2, corr_i = alpha_i corr_{i-1} (+ sup_{n-1} rb_{n-1} on the last row)
 			Aff<T> ec = i == 0 ? Aff<T>{zero, mk<T>(-0.5, 0)} : Aff<T>{alpha, i == n - 1 ? sup(i) * rb : zero};
 			Fcorr = aff_after(ec, Fcorr);
@@ -1025,16 +1027,16 @@ __global__ void __launch_bounds__(DIRN == 1 ? 512 : 256) k_factor_chunked(Geom G
 	if(active && i0 < i1) {
 		cx<T> cr = Ec.B, wv = Ew.B;  // values before the chunk (maps applied to 0)
 		for(int i = i0; i < i1; i++) {
-			cx<T> alpha = cvt<T>(Fc[F_A * plane + Q(i)]);
-			cx<T> rb = cvt<T>(Fc[F_RB * plane + Q(i)]);
+			cx<T> alpha = cvt<T>(Fc[Q(F_A, i)]);
+			cx<T> rb = cvt<T>(Fc[Q(F_RB, i)]);
 			if(i == 0) { cr = mk<T>(-0.5, 0); wv = one; }
 			else {
-				cx<T> gm = -cvt<T>(Fc[F_C * plane + Q(i - 1)]);  // gamma_{i-1}
+				cx<T> gm = -cvt<T>(Fc[Q(F_C, i - 1)]);  // gamma_{i-1}
 				cr = cfma(alpha, cr, (i == n - 1 ? sup(i) * rb : zero));
 				wv = -(gm * wv);
 			}
-			Fc[F_COR * plane + Q(i)] = cvt<S>(cr);  // forward corr, replaced below
-			Fc[F_W * plane + Q(i)] = cvt<S>(wv);
+			Fc[Q(F_COR, i)] = cvt<S>(cr);  // forward corr, replaced below
+			Fc[Q(F_W, i)] = cvt<S>(wv);
 			if(i == n - 1) corr_last = cr;
 		}
 	}
@@ -1053,7 +1055,7 @@ __global__ void __launch_bounds__(DIRN == 1 ? 512 : 256) k_factor_chunked(Geom G
 	if(active && i0 < i1) {
 		for(int j = i1 - 1; j >= i0; j--) {
 			Aff<T> e = j == n - 1 ? Aff<T>{zero, corr_last}
-				: Aff<T>{cvt<T>(Fc[F_C * plane + Q(j)]), cvt<T>(Fc[F_COR * plane + Q(j)])};
+				: Aff<T>{cvt<T>(Fc[Q(F_C, j)]), cvt<T>(Fc[Q(F_COR, j)])};
 			Bm = aff_after(e, Bm);
 		}
 	}
@@ -1088,19 +1090,19 @@ __global__ void __launch_bounds__(DIRN == 1 ? 512 : 256) k_factor_chunked(Geom G
 		cx<T> cv = Eb.B;  // cv of the element after the chunk
 		for(int j = i1 - 1; j >= i0; j--) {
 			cv = j == n - 1 ? corr_last
-				: cvt<T>(Fc[F_C * plane + Q(j)]) * cv + cvt<T>(Fc[F_COR * plane + Q(j)]);
-			Fc[F_COR * plane + Q(j)] = cvt<S>(cv);
+				: cvt<T>(Fc[Q(F_C, j)]) * cv + cvt<T>(Fc[Q(F_COR, j)]);
+			Fc[Q(F_COR, j)] = cvt<S>(cv);
 		}
 		if(i0 == 0) cv0 = cv;
 	}
 	// padding of the interleaved x layout: identity maps
 	if(DIRN == 0 && chunkMx > 0 && active) {
 		for(int i = n + lane; i < chunksX * chunkMx; i += 32) {
-			Fc[F_A * plane + Q(i)] = mk<S>(0, 0);
-			Fc[F_RB * plane + Q(i)] = mk<S>(0, 0);
-			Fc[F_W * plane + Q(i)] = mk<S>(0, 0);
-			Fc[F_C * plane + Q(i)] = mk<S>(0, 0);
-			Fc[F_COR * plane + Q(i)] = mk<S>(0, 0);
+			Fc[Q(F_A, i)] = mk<S>(0, 0);
+			Fc[Q(F_RB, i)] = mk<S>(0, 0);
+			Fc[Q(F_W, i)] = mk<S>(0, 0);
+			Fc[Q(F_C, i)] = mk<S>(0, 0);
+			Fc[Q(F_COR, i)] = mk<S>(0, 0);
 		}
 	}
 	// Sherman-Morrison scalars in FP64
@@ -1204,7 +1206,7 @@ __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_xc(Geom G, 
 	const int PITCH = 32 * (M + 1);
 	cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw) + (size_t)warp * KS * PITCH;
 	if(iy < Ny) {  // always true unless TOUT (whose block writes together after a barrier)
-	const cx<R>* Fc = fac + ((size_t)g * 2 + c) * NFAC * plane + (size_t)iy * 32 * M;
+	const cx<R>* Fc = fac + ((size_t)g * 2 + c) * NFAC * plane + (size_t)iy * 32 * M * NFAC;
 	const cx<double>* ls = lsc + (((size_t)g * 2 + c) * Ny + iy) * 2;
 	const cx<double> r0 = ls[0], rden = ls[1];
 	const int i0 = lane * M;
@@ -1240,8 +1242,8 @@ __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_xc(Geom G, 
 #pragma unroll
 	for(int k = 0; k < M; k++) {
 		if(i0 + k < n_unk) {
-			const cx<R> a = Fc[F_A * plane + k * 32 + lane], rb = Fc[F_RB * plane + k * 32 + lane];
-			const cx<R> w = Fc[F_W * plane + k * 32 + lane], cc = Fc[F_C * plane + k * 32 + lane];
+			const cx<R> a = Fc[(k * NFAC + F_A) * 32 + lane], rb = Fc[(k * NFAC + F_RB) * 32 + lane];
+			const cx<R> w = Fc[(k * NFAC + F_W) * 32 + lane], cc = Fc[(k * NFAC + F_C) * 32 + lane];
 			P = a * P;
 			S1 = cfma(w, P, S1);
 			G1 = cfma(Cp, P, G1);
@@ -1264,7 +1266,7 @@ __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_xc(Geom G, 
 #pragma unroll
 	for(int k = 0; k < M; k++) {
 		if(i0 + k < n_unk) {
-			const cx<R> a = Fc[F_A * plane + k * 32 + lane];
+			const cx<R> a = Fc[(k * NFAC + F_A) * 32 + lane];
 #pragma unroll
 			for(int j = 0; j < KS; j++) { din[j] = cfma(a, din[j], vb[j * PITCH + k]); vb[j * PITCH + k] = din[j]; }
 		}
@@ -1272,7 +1274,7 @@ __global__ void __launch_bounds__(128, NBPM_XC_MINB(M * KS)) k_solve_xc(Geom G, 
 #pragma unroll
 	for(int k = M - 1; k >= 0; k--) {
 		if(i0 + k < n_unk) {
-			const cx<R> cc = Fc[F_C * plane + k * 32 + lane], cr = Fc[F_COR * plane + k * 32 + lane];
+			const cx<R> cc = Fc[(k * NFAC + F_C) * 32 + lane], cr = Fc[(k * NFAC + F_COR) * 32 + lane];
 #pragma unroll
 			for(int j = 0; j < KS; j++) {
 				xin[j] = cfma(cc, xin[j], vb[j * PITCH + k]);
@@ -1763,7 +1765,7 @@ __global__ void __launch_bounds__(256) k_solve_xw(Geom G, int slot0, int nch, co
 	cx<R>* sD = sB + KS * W;
 	cx<R>* sP = sD + KS * W;
 	cx<R>* sX = sP + KS * W;                          // [KS][2]: d at the last unknown, fr
-	const cx<R>* Fc = fac + ((size_t)g * 2 + c) * NFAC * plane + (size_t)iy * CH * M;
+	const cx<R>* Fc = fac + ((size_t)g * 2 + c) * NFAC * plane + (size_t)iy * CH * M * NFAC;
 	const cx<double>* ls = lsc + (((size_t)g * 2 + c) * Ny + iy) * 2;
 	const cx<double> r0 = ls[0], rden = ls[1];
 	const int i0 = ci * M;
@@ -1786,7 +1788,7 @@ __global__ void __launch_bounds__(256) k_solve_xw(Geom G, int slot0, int nch, co
 	for(int k = 0; k < M; k++) {
 		bool ok = i0 + k < n_unk;
 		cx<R> a = zero, rb = zero;
-		if(ok) { a = Fc[F_A * plane + k * CH + ci]; rb = Fc[F_RB * plane + k * CH + ci]; }
+		if(ok) { a = Fc[(k * NFAC + F_A) * CH + ci]; rb = Fc[(k * NFAC + F_RB) * CH + ci]; }
 #pragma unroll
 		for(int j = 0; j < KS; j++) {
 			v[j][k] = zero;
@@ -1832,7 +1834,7 @@ __global__ void __launch_bounds__(256) k_solve_xw(Geom G, int slot0, int nch, co
 #pragma unroll
 	for(int k = 0; k < M; k++) {
 		if(i0 + k < n_unk) {
-			cx<R> a = Fc[F_A * plane + k * CH + ci], w = Fc[F_W * plane + k * CH + ci];
+			cx<R> a = Fc[(k * NFAC + F_A) * CH + ci], w = Fc[(k * NFAC + F_W) * CH + ci];
 #pragma unroll
 			for(int j = 0; j < KS; j++) {
 				d[j] = cfma(a, d[j], v[j][k]);
@@ -1864,7 +1866,7 @@ __global__ void __launch_bounds__(256) k_solve_xw(Geom G, int slot0, int nch, co
 #pragma unroll
 	for(int k = M - 1; k >= 0; k--) {
 		if(i0 + k < n_unk) {
-			cx<R> cc = Fc[F_C * plane + k * CH + ci];
+			cx<R> cc = Fc[(k * NFAC + F_C) * CH + ci];
 #pragma unroll
 			for(int j = 0; j < KS; j++) { B[j] = cfma(cc, B[j], v[j][k]); A[j] = cc * A[j]; }
 		}
@@ -1903,7 +1905,7 @@ __global__ void __launch_bounds__(256) k_solve_xw(Geom G, int slot0, int nch, co
 #pragma unroll
 	for(int k = M - 1; k >= 0; k--) {
 		if(i0 + k < n_unk) {
-			cx<R> cc = Fc[F_C * plane + k * CH + ci], cr = Fc[F_COR * plane + k * CH + ci];
+			cx<R> cc = Fc[(k * NFAC + F_C) * CH + ci], cr = Fc[(k * NFAC + F_COR) * CH + ci];
 #pragma unroll
 			for(int j = 0; j < KS; j++) {
 				d[j] = cfma(cc, d[j], v[j][k]);
@@ -1944,7 +1946,7 @@ __global__ void __launch_bounds__(128) k_solve_xs(Geom G, int slot0, int nch, in
 	const int n_unk = Nx - 1;
 	const int PITCH = 32 * (M + 1);
 	cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw) + (size_t)warp * KS * PITCH;
-	const cx<R>* Fc = fac + ((size_t)g * 2 + c) * NFAC * plane + (size_t)iy * 32 * M;
+	const cx<R>* Fc = fac + ((size_t)g * 2 + c) * NFAC * plane + (size_t)iy * 32 * M * NFAC;
 	const cx<double>* ls = lsc + (((size_t)g * 2 + c) * Ny + iy) * 2;
 	const cx<double> r0 = ls[0], rden = ls[1];
 	const int i0 = lane * M;
@@ -1965,7 +1967,7 @@ __global__ void __launch_bounds__(128) k_solve_xs(Geom G, int slot0, int nch, in
 	for(int j = 0; j < KS; j++) { A[j] = one; B[j] = zero; }
 	for(int k = 0; k < M; k++) {
 		if(i0 + k < n_unk) {
-			cx<R> a = Fc[F_A * plane + k * 32 + lane], rb = Fc[F_RB * plane + k * 32 + lane];
+			cx<R> a = Fc[(k * NFAC + F_A) * 32 + lane], rb = Fc[(k * NFAC + F_RB) * 32 + lane];
 #pragma unroll
 			for(int j = 0; j < KS; j++) {
 				cx<R> b = V(j, k) * rb;
@@ -1993,7 +1995,7 @@ __global__ void __launch_bounds__(128) k_solve_xs(Geom G, int slot0, int nch, in
 	}
 	for(int k = 0; k < M; k++) {
 		if(i0 + k < n_unk) {
-			cx<R> a = Fc[F_A * plane + k * 32 + lane], w = Fc[F_W * plane + k * 32 + lane];
+			cx<R> a = Fc[(k * NFAC + F_A) * 32 + lane], w = Fc[(k * NFAC + F_W) * 32 + lane];
 #pragma unroll
 			for(int j = 0; j < KS; j++) {
 				d[j] = cfma(a, d[j], V(j, k));
@@ -2018,7 +2020,7 @@ __global__ void __launch_bounds__(128) k_solve_xs(Geom G, int slot0, int nch, in
 	}
 	for(int k = M - 1; k >= 0; k--) {
 		if(i0 + k < n_unk) {
-			cx<R> cc = Fc[F_C * plane + k * 32 + lane];
+			cx<R> cc = Fc[(k * NFAC + F_C) * 32 + lane];
 #pragma unroll
 			for(int j = 0; j < KS; j++) { B[j] = cfma(cc, B[j], V(j, k)); A[j] = cc * A[j]; }
 		}
@@ -2038,7 +2040,7 @@ __global__ void __launch_bounds__(128) k_solve_xs(Geom G, int slot0, int nch, in
 	}
 	for(int k = M - 1; k >= 0; k--) {
 		if(i0 + k < n_unk) {
-			cx<R> cc = Fc[F_C * plane + k * 32 + lane], cr = Fc[F_COR * plane + k * 32 + lane];
+			cx<R> cc = Fc[(k * NFAC + F_C) * 32 + lane], cr = Fc[(k * NFAC + F_COR) * 32 + lane];
 #pragma unroll
 			for(int j = 0; j < KS; j++) {
 				d[j] = cfma(cc, d[j], V(j, k));
