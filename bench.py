@@ -270,12 +270,12 @@ def run_ours(args):
     # capture and its command are summarised under profiles/.
     PROF = "profiles/solve_xc_koehler_256x256x8_fp32.md"
     PSF = "profiles/shift_fused_koehler_256x256x8_fp32.md"
-    W = 2 * (319.3e6 + 184.3e6 + 562.6e6 + 197.7e6) / 2  # mean of the two Woodbury launches, x2 slots
+    W = 2 * (319.7e6 + 190.0e6 + 560.9e6 + 196.6e6) / 2  # mean of the two Woodbury launches, x2 slots
     TRAFFIC = {("koehler", "fp32", "wood_solve_x"): (W, PROF),
                ("koehler", "fp32", "wood_solve_y"): (W, PROF + " (the same kernel in the transposed frame)"),
-               ("koehler", "fp32", "expl_solve_x"): (2 * (344.6e6 + 188.5e6), PROF),
-               ("koehler", "fp32", "expl_solve_y"): (2 * (344.6e6 + 188.5e6), PROF + " (the same kernel in the transposed frame)"),
-               ("koehler", "fp32", "shift_fused"): (2 * (242.5e6 + 189.5e6), PSF)}
+               ("koehler", "fp32", "expl_solve_x"): (2 * (345.0e6 + 188.0e6), PROF),
+               ("koehler", "fp32", "expl_solve_y"): (2 * (345.0e6 + 188.0e6), PROF + " (the same kernel in the transposed frame)"),
+               ("koehler", "fp32", "shift_fused"): (2 * (242.6e6 + 181.1e6), PSF)}
     roof = None
     if prof:
         top = max(prof, key=lambda k: prof[k]["ms"])
