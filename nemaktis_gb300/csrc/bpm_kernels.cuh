@@ -1914,15 +1914,36 @@ __global__ void __launch_bounds__(256) k_solve_xw(Geom G, int slot0, int nch, co
 		}
 	}
 	__syncthreads();
-	for(int j = 0; j < KS; j++) {
-		const size_t off = (size_t)(s0 + j) * 2 * N + (size_t)c * N + (size_t)iy * Nx;
-		const size_t toff = (size_t)(s0 + j) * 2 * N + (size_t)(1 - c) * N + iy;
-		for(int e = threadIdx.x; e < Nx; e += blockDim.x) {
-			int ee = e == Nx - 1 ? 0 : e;
-			cx<R> x = buf[j * PITCH + (ee / M) * (M + 1) + ee % M];
-			const size_t o = TOUT ? toff + (size_t)e * Ny : off + e;
-			if(dst) dst[o] = x;
-			if(acc_out) acc_out[o] = (acc_in2 ? acc_in[off + e] + acc_in2[off + e] : acc_in[off + e]) + x;
+	// write-out: the accumulator inputs of several points are loaded before any store
+	constexpr int U = 4;
+	for(int e0 = threadIdx.x; e0 < Nx; e0 += U * blockDim.x) {
+		cx<R> a[U][KS];
+		if(acc_out) {
+#pragma unroll
+			for(int u = 0; u < U; u++) {
+				const int e = e0 + u * blockDim.x;
+				if(e < Nx)
+#pragma unroll
+					for(int j = 0; j < KS; j++) {
+						const size_t o = (size_t)(s0 + j) * 2 * N + (size_t)c * N + (size_t)iy * Nx + e;
+						a[u][j] = acc_in2 ? acc_in[o] + acc_in2[o] : acc_in[o];
+					}
+			}
+		}
+#pragma unroll
+		for(int u = 0; u < U; u++) {
+			const int e = e0 + u * blockDim.x;
+			if(e < Nx) {
+				const int ee = e == Nx - 1 ? 0 : e;
+#pragma unroll
+				for(int j = 0; j < KS; j++) {
+					const cx<R> x = buf[j * PITCH + (ee / M) * (M + 1) + ee % M];
+					const size_t o = TOUT ? (size_t)(s0 + j) * 2 * N + (size_t)(1 - c) * N + iy + (size_t)e * Ny
+						: (size_t)(s0 + j) * 2 * N + (size_t)c * N + (size_t)iy * Nx + e;
+					if(dst) dst[o] = x;
+					if(acc_out) acc_out[o] = a[u][j] + x;
+				}
+			}
 		}
 	}
 }
