@@ -780,59 +780,37 @@ __device__ __forceinline__ cx<R> shfl_xor_c(cx<R> v, int m) {
 // writes, per wavelength group, the transposed planes those solves read: DY' (every block) from
 // DX, DX' (blocks 1 and 2) from DY, every DXDY' block from DXDY, and the diagonal stencils of the
 // transposed x-lines (diag' direction 0, component c') from the y diagonals of component 1 - c'.
-// Each block moves one 32x32 tile of points of one group, plane after plane, through shared memory
-// (coalesced reads and writes).
+// Each block moves one 32x32 tile of one plane through shared memory (coalesced reads and writes).
 constexpr int NCT = 12 + 6 + 16 + 6;  // planes per group: DY', DX' (blocks 1, 2), DXDY', diag'
 template <typename S>
 __global__ void __launch_bounds__(256) k_coef_t(Geom G, const cx<S>* __restrict__ coef, const cx<S>* __restrict__ diag,
 		cx<S>* __restrict__ coefT, cx<S>* __restrict__ diagT) {
-	// one block per 32x32 tile of points and group, looping over the NCT planes; block (32, 8)
-	__shared__ cx<S> tile[2][32][33];  // double-buffered: one barrier per plane
+	__shared__ cx<S> tile[32][33];
 	const int Nx = G.Nx, Ny = G.Ny, N = G.N;
-	const int g = blockIdx.z;
-	const cx<S>* Cs = coef + (size_t)g * coef_set_size(N);
-	cx<S>* Cd = coefT + (size_t)g * coef_set_size(N);
-	const cx<S>* Ds = diag + (size_t)g * NDIAG * N;
-	cx<S>* Dd = diagT + (size_t)g * NDIAG * N;
-	const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32, tx = threadIdx.x, ty = threadIdx.y;
-	// this thread's source points (x0 + tx, y0 + ty + 8 r) and destination points (x0 + ty + 8 r,
-	// y0 + tx) of the transposed frame; cs / cd: their plane-0 entries in the tiled layout
-	int ps[4], pd[4];
-	size_t cs[4], cd[4];
-	bool os[4], od[4];
-#pragma unroll
-	for(int r = 0; r < 4; r++) {
-		const int xs = x0 + tx, ys = y0 + ty + 8 * r, xd = x0 + ty + 8 * r, yd = y0 + tx;
-		os[r] = xs < Nx && ys < Ny;
-		od[r] = xd < Nx && yd < Ny;
-		ps[r] = os[r] ? ys * Nx + xs : 0;
-		pd[r] = od[r] ? xd * Ny + yd : 0;
-		cs[r] = cidx(0, ps[r]);
-		cd[r] = cidx(0, pd[r]);
+	const int g = blockIdx.z / NCT, k = blockIdx.z % NCT;
+	int sp, dp;  // source / destination plane
+	bool dg = false;
+	if(k < 12) { const int b = k / 3, kk = k % 3; dp = C_DY + 3 * b + kk; sp = C_DX + 3 * (3 - b) + kk; }
+	else if(k < 18) { const int b = 1 + (k - 12) / 3, kk = (k - 12) % 3; dp = C_DX + 3 * b + kk; sp = C_DY + 3 * (3 - b) + kk; }
+	else if(k < 34) {
+		const int b = (k - 18) / 4, kk = (k - 18) % 4;
+		const int sk = kk == 1 ? 2 : kk == 2 ? 1 : kk;
+		dp = C_DXDY + 4 * b + kk; sp = C_DXDY + 4 * (3 - b) + sk;
 	}
-	for(int k = 0; k < NCT; k++) {
-		int sp, dp;  // source / destination plane
-		bool dg = false;
-		if(k < 12) { const int b = k / 3, kk = k % 3; dp = C_DY + 3 * b + kk; sp = C_DX + 3 * (3 - b) + kk; }
-		else if(k < 18) { const int b = 1 + (k - 12) / 3, kk = (k - 12) % 3; dp = C_DX + 3 * b + kk; sp = C_DY + 3 * (3 - b) + kk; }
-		else if(k < 34) {
-			const int b = (k - 18) / 4, kk = (k - 18) % 4;
-			const int sk = kk == 1 ? 2 : kk == 2 ? 1 : kk;
-			dp = C_DXDY + 4 * b + kk; sp = C_DXDY + 4 * (3 - b) + sk;
-		}
-		else { const int cp = (k - 34) / 3, kk = (k - 34) % 3; dp = 0 * 6 + cp * 3 + kk; sp = 1 * 6 + (1 - cp) * 3 + kk; dg = true; }
-		cx<S>(*t)[33] = tile[k & 1];
-#pragma unroll
-		for(int r = 0; r < 4; r++)
-			if(os[r]) t[ty + 8 * r][tx] = dg ? Ds[(size_t)sp * N + ps[r]] : Cs[cs[r] + (size_t)sp * 32];
-		__syncthreads();
-#pragma unroll
-		for(int r = 0; r < 4; r++)
-			if(od[r]) {
-				const cx<S> v = t[tx][ty + 8 * r];
-				if(dg) Dd[(size_t)dp * N + pd[r]] = v;
-				else Cd[cd[r] + (size_t)dp * 32] = v;
-			}
+	else { const int cp = (k - 34) / 3, kk = (k - 34) % 3; dp = 0 * 6 + cp * 3 + kk; sp = 1 * 6 + (1 - cp) * 3 + kk; dg = true; }
+	// diagonal stencils: plain planes; coefficient planes: the tiled layout (cidx)
+	const cx<S>* src = dg ? diag + (size_t)g * NDIAG * N : coef + (size_t)g * coef_set_size(N);
+	cx<S>* dst = dg ? diagT + (size_t)g * NDIAG * N : coefT + (size_t)g * coef_set_size(N);
+	auto at = [&](int plane, int q) { return dg ? (size_t)plane * N + q : cidx(plane, q); };
+	const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+	for(int r = threadIdx.y; r < 32; r += blockDim.y) {
+		const int x = x0 + threadIdx.x, y = y0 + r;
+		if(x < Nx && y < Ny) tile[r][threadIdx.x] = src[at(sp, y * Nx + x)];
+	}
+	__syncthreads();
+	for(int r = threadIdx.y; r < 32; r += blockDim.y) {
+		const int y = y0 + threadIdx.x, x = x0 + r;  // destination row x, column y
+		if(x < Nx && y < Ny) dst[at(dp, x * Ny + y)] = tile[threadIdx.x][r];
 	}
 }
 

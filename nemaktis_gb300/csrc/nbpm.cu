@@ -1038,7 +1038,7 @@ struct Plan : PlanBase {
 				// then the x-line factorisation of that frame
 				const Geom Gt = transposed(Gm);
 				launch("coef_t", 2.0 * N * ng * NCT * sc, [&] {
-					k_coef_t<R><<<dim3((unsigned)((Nx + 31) / 32), (unsigned)((Ny + 31) / 32), (unsigned)ng), dim3(32, 8), 0,
+					k_coef_t<R><<<dim3((unsigned)((Nx + 31) / 32), (unsigned)((Ny + 31) / 32), (unsigned)(ng * NCT)), dim3(32, 8), 0,
 						cs>>>(Gm, C, ps.Dg, CT, W->diagT.as<cx<R>>());
 				});
 				launch("factor_y", fb, [&] {
